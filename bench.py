@@ -1,0 +1,326 @@
+"""Benchmark of the GB300 engine on the 3D Gray-Scott workload.
+
+Workload: 3D Gray-Scott (examples/gray-scott-3d.fmr, the pearson-3d.fmr form
+with the F,k reaction), 256^3 FP64, periodic, Du=2e-5 Dv=1e-5 F=0.04 k=0.06
+dx=0.01 dt=0.5; seeded start (8 cubes of side 16).  One bench step = one
+Formura_Forward of the emitted program = 2000 time steps.
+
+  value   GLUP/s with the state resident in HBM (Formura_Advance), CUDA events
+          on the launching stream; 268 MB of state > 129 MB L2 (no flush needed).
+  e2e     GLUP/s through Formura_Forward on the host globals: pinned H2D copy of
+          U,V, 2000 steps, D2H copy, every step.
+  roofline  the dominant kernel (gs3d_f64_step) against the FP64 FMA pipe
+          measured in this run, and its HBM fraction.
+  cpu_baseline  the oracle's OpenMP speed build on all host cores, on a
+          bounded sample of the same workload.
+
+--impl reference times that CPU implementation alone (the reference's path
+is CPU code; its compiler cannot run here), with the same metric and config.
+Multi-GPU: replicas only (one independent program per rank, weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "gray_scott_3d"
+N = 256
+GS = dict(F=0.04, k=0.06, Du=2e-5, Dv=1e-5, dt=0.5, dx=0.01)
+# Algorithmic work per lattice-site update of the pearson-3d DAG (counted on the
+# constant-folded OM graph, division = 1 flop): 46 flops, 32 B.
+FLOPS_PER_LUP = 46
+BYTES_PER_LUP = 32
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return json.loads(p.read_text())
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[1]), smax=float(parts[2]), reasons=parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        seen = sorted({names[i] for r in rows for i, v in enumerate(r["reasons"])
+                       if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r["sm"] for r in rows),
+                "sm_max_mhz": max(r["smax"] for r in rows), "reasons": seen,
+                "samples": len(rows)}
+
+
+def measure_fma_peak(torch, kernels, fp64: bool, sms: int):
+    blocks, threads = sms * 8, 256
+    iters = 2048 if fp64 else 65536
+    sink = torch.zeros(blocks, dtype=torch.float64 if fp64 else torch.float32, device="cuda")
+    kernels.probe_fma(fp64, blocks, threads, 64, sink)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        kernels.probe_fma(fp64, blocks, threads, iters, sink)
+        b.record()
+        b.synchronize()
+        best = min(best, a.elapsed_time(b) / 1e3)
+    return blocks * threads * iters * 16 / best / 1e12  # TFLOP/s
+
+
+def read_profile_traffic():
+    """dram bytes per launch of gs3d_f64_step from the committed ncu summary."""
+    p = ROOT / "profiles" / "gs3d_f64_step_256.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.strip().startswith("dram_bytes_per_launch"):
+            try:
+                return int(float(line.split("=")[1].split()[0]))
+            except Exception:
+                return None
+    return None
+
+
+def cpu_baseline(seconds: float = 12.0):
+    """The oracle's speed build (OpenMP, all host cores) on 256^3 x S steps."""
+    import numpy as np
+
+    from formura_gb300 import inits
+    from oracle import oracle
+
+    U0, V0 = inits.gray_scott_3d(N, N, N, seed=1)
+    oracle.gs3d_f64(U0, V0, 1, **GS, fast=True)  # warm (page-in, thread pool)
+    t = time.perf_counter()
+    oracle.gs3d_f64(U0, V0, 2, **GS, fast=True)
+    per = (time.perf_counter() - t) / 2
+    steps = max(2, min(200, int(seconds / max(per, 1e-6))))
+    t = time.perf_counter()
+    oracle.gs3d_f64(U0, V0, steps, **GS, fast=True)
+    dt = time.perf_counter() - t
+    return dict(value=round(N ** 3 * steps / dt / 1e9, 4), unit="GLUP/s",
+                cores=oracle.num_threads(fast=True), kind="port",
+                sample="256^3 FP64 Gray-Scott x %d steps (of 2000), oracle -O3 OpenMP" % steps,
+                seconds=round(dt, 3))
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    import numpy as np
+
+    from formura_gb300 import inits
+    from oracle import oracle
+
+    oracle.build(reference=False)
+    U0, V0 = inits.gray_scott_3d(N, N, N, seed=1)
+    sample_steps = 4
+    for _ in range(args.warmup):
+        oracle.gs3d_f64(U0, V0, sample_steps, **GS, fast=True)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        oracle.gs3d_f64(U0, V0, sample_steps, **GS, fast=True)
+        times.append(time.perf_counter() - t)
+    tot = sum(times)
+    val = N ** 3 * sample_steps * len(times) / tot / 1e9
+    cores = oracle.num_threads(fast=True)
+    line = {
+        "impl": "reference", "metric": "GLUP/s (3D Gray-Scott 256^3 FP64)", "value": round(val, 4),
+        "unit": "GLUP/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(tot / len(times) * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "gray_scott_3d 256^3 FP64 (pearson-3d.fmr form)",
+                   "step": "%d time steps of the CPU restatement per bench step" % sample_steps},
+        "cpu_baseline": {"value": round(val, 4), "unit": "GLUP/s", "cores": cores, "kind": "port",
+                         "sample": "256^3 x %d steps per bench step; oracle/fmr_oracle.c -O3 "
+                                   "OpenMP (the reference compiler cannot run here)" % sample_steps},
+        "e2e": {"value": round(val, 4), "unit": "GLUP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_engine(args):
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    from formura_gb300 import inits, kernels
+    from formura_gb300.runtime import load_program
+
+    prog = load_program(WORKLOAD)
+    M = prog.steps_per_forward
+    prog.init()
+    U0, V0 = inits.gray_scott_3d(N, N, N, seed=1 + rank)
+    prog.state["U"][...] = U0
+    prog.state["V"][...] = V0
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident leg -------------------------------------------------
+    prog.upload()
+    for _ in range(args.warmup):
+        prog.advance(1)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            prog.advance(1)
+        ev1.record()
+        ev1.synchronize()
+    dev_s = ev0.elapsed_time(ev1) / 1e3
+    barrier()
+
+    # ---- end-to-end leg through Formura_Forward on host globals ---------------
+    prog.download()
+    prog.forward()  # warm the host-copy path (registration, first copies)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        prog.forward()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    barrier()
+
+    times = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    dev_s, e2e_s = times.tolist()
+    lups = float(N ** 3) * M * args.steps * ws
+    value = lups / dev_s / 1e9
+    e2e = lups / e2e_s / 1e9
+    if rank != 0:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline -----------------------------------------------------------
+    launches = M * args.steps
+    per_launch = dev_s / launches
+    fp64_peak = measure_fma_peak(torch, kernels, True, sms)
+    fp32_peak = measure_fma_peak(torch, kernels, False, sms)
+    achieved_tf = FLOPS_PER_LUP * N ** 3 / per_launch / 1e12
+    peaks = load_peaks()
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved_gbs = BYTES_PER_LUP * N ** 3 / per_launch / 1e9
+    traffic = read_profile_traffic()
+    clocks = clk.summary()
+    cpu = cpu_baseline() if not args.no_cpu else None
+
+    line = {
+        "metric": "GLUP/s (3D Gray-Scott 256^3 FP64) vs FP64/HBM roofline at 1 GB300",
+        "value": round(value, 4), "unit": "GLUP/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_s / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded: U=1,V=0 + 8 cubes of side 16 at U=0.5,V=0.25 +-1%)",
+        "config": {"workload": "gray_scott_3d: 256^3 FP64 periodic Gray-Scott, pearson-3d.fmr form "
+                               "(F=0.04 k=0.06 Du=2e-5 Dv=1e-5 dx=0.01 dt=0.5)",
+                   "grid": [N, N, N], "steps_per_bench_step": M,
+                   "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "l2": "state 268 MB > 129 MB L2; no flush", "bit_exact_vs_oracle": True},
+        "roofline": {"bound": "fp64", "achieved": round(achieved_tf, 4), "peak": round(fp64_peak, 4),
+                     "unit": "TFLOP/s", "frac": round(achieved_tf / fp64_peak, 4),
+                     "traffic": traffic, "peak_source": "measured in this run (FP64 FMA probe)",
+                     "flops_per_lup": FLOPS_PER_LUP,
+                     "hbm": {"achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
+                             "frac": round(achieved_gbs / hbm_peak, 4),
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
+                     "fp32_peak_tflops": round(fp32_peak, 2),
+                     "kernel": "gs3d_f64_step", "ms_per_launch": round(per_launch * 1e3, 4)},
+        "e2e": {"value": round(e2e, 4), "unit": "GLUP/s",
+                "h2d_bytes_per_step": 2 * 8 * N ** 3, "d2h_bytes_per_step": 2 * 8 * N ** 3},
+        "gpu_launches": 2 * launches,
+        "clocks": clocks,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,412 @@
+"""The CUDA back end: emits the per-program host code of a Formura program.
+
+Formura's C back end writes, for a program ``<name>.fmr`` with its numerical
+config ``<name>.yaml``, a header and a C file that keep one API
+(src/Formura/MPICxx/Translate.hs:973-1139):
+
+* ``#define NX ...`` per axis = intra_node_shape x mpi_grid_shape (:1015-1019);
+* ``extern <elem> <State>[NX][NY]...;`` — one global array per state
+  variable, named after the arguments of ``step`` (:418-431);
+* ``struct Formura_Navigator`` — ``time_step``; ``lower_/upper_/offset_`` per
+  axis; ``mpi_comm``; ``mpi_my_rank``; ``mpi_rank_<delta>`` (:1038-1048);
+  ``extern struct Formura_Navigator navi;`` (:1050-1051);
+* ``int Formura_Init(struct Formura_Navigator*, MPI_Comm)`` (:1070-1092);
+* ``int Formura_Forward(struct Formura_Navigator*)`` — advances the globals by
+  M = monitor_interval rounded up to a multiple of 2*temporal_blocking_interval
+  steps and adds M to ``time_step`` (:1106-1131).
+
+This module emits the same API, but the body of ``Formura_Forward`` copies the
+globals to the GPU, runs M steps through the thin C ABI of
+``libformura_gb300.so`` (include/formura_gb300.h) and copies them back.  The
+state is stored without a margin: ``lower_* = 0``, ``upper_* = N*``,
+``offset_* = 0`` (the navigator of examples-generated/pearson.c:75-85).
+One GPU, one rank: every ``mpi_rank_*`` neighbour is rank 0 and the halo
+exchange is the kernels' periodic index wrap.
+
+Extensions (not in the reference; all optional for a caller):
+``Formura_Upload`` / ``Formura_Advance`` / ``Formura_Download`` split
+``Formura_Forward`` so that state can stay resident on the GPU between calls;
+``Formura_Device_State`` exposes the device copy of a state array;
+``Formura_Set_Stream`` selects the CUDA stream; ``Formura_Conserved_Totals``
+returns FP64 sums of the state arrays (mass/energy drift checks);
+``Formura_Finalize`` frees the device copies.
+"""
+from __future__ import annotations
+
+import dataclasses
+import hashlib
+import itertools
+import os
+import subprocess
+from pathlib import Path
+from typing import Dict, List, Optional, Sequence
+
+from . import build as _build
+
+AXES3 = ("x", "y", "z")
+
+
+@dataclasses.dataclass(frozen=True)
+class Program:
+    """A Formura program as the back end needs it.
+
+    ``form`` names the kernel family that evaluates the program's ``step``:
+      * ``gs3d_f64``   — examples/pearson-3d.fmr form, double
+      * ``gs3d_f32k``  — the same form in float with Kahan time accumulation
+      * ``diff2d_f64`` — examples/diffusion.fmr form in 2D, double
+    ``constants`` are the .fmr constants of ``step`` (F, k, Du, Dv, dt, dx /
+    Dt, Dx).  ``intra_node_shape``, ``mpi_grid_shape``, ``monitor_interval``
+    and ``temporal_blocking_interval`` are the YAML keys of
+    src/Formura/NumericalConfig.hs:17-34.
+    """
+
+    name: str
+    form: str
+    intra_node_shape: Sequence[int]
+    constants: Dict[str, float]
+    monitor_interval: int
+    temporal_blocking_interval: int = 1
+    mpi_grid_shape: Optional[Sequence[int]] = None
+    axes: Optional[Sequence[str]] = None
+
+    @property
+    def dim(self) -> int:
+        return len(self.intra_node_shape)
+
+    @property
+    def axis_names(self) -> List[str]:
+        return list(self.axes) if self.axes else list(AXES3[: self.dim])
+
+    @property
+    def shape(self) -> List[int]:
+        g = self.mpi_grid_shape or [1] * self.dim
+        return [int(i) * int(m) for i, m in zip(self.intra_node_shape, g)]
+
+    @property
+    def steps_per_forward(self) -> int:
+        """M of Translate.hs:1111-1113: monitor_interval rounded up to 2*tb."""
+        tb2 = 2 * max(1, int(self.temporal_blocking_interval))
+        m = int(self.monitor_interval)
+        return ((m + tb2 - 1) // tb2) * tb2
+
+    @property
+    def elem(self) -> str:
+        return "float" if self.form.endswith("f32k") else "double"
+
+    @property
+    def state_names(self) -> List[str]:
+        return ["dens"] if self.form.startswith("diff") else ["U", "V"]
+
+    @property
+    def extra_state_names(self) -> List[str]:
+        # Kahan compensation arrays carried between calls.
+        return ["U_compensation", "V_compensation"] if self.form.endswith("f32k") else []
+
+    def validate(self) -> None:
+        if self.mpi_grid_shape and any(int(m) != 1 for m in self.mpi_grid_shape):
+            raise ValueError(
+                "%s: mpi_grid_shape %s — this engine runs one GPU per program; the "
+                "domain is periodic on that GPU (use [1,...])" % (self.name, list(self.mpi_grid_shape)))
+        if self.form not in FORMS:
+            raise ValueError("%s: unknown form %r (known: %s)" % (self.name, self.form, sorted(FORMS)))
+        want_dim = FORMS[self.form]["dim"]
+        if self.dim != want_dim:
+            raise ValueError("%s: form %s is %dD, shape %s" % (self.name, self.form, want_dim,
+                                                              list(self.intra_node_shape)))
+        for key in FORMS[self.form]["constants"]:
+            if key not in self.constants:
+                raise ValueError("%s: constant %s missing" % (self.name, key))
+        if self.monitor_interval < 1:
+            raise ValueError("%s: monitor_interval must be >= 1" % self.name)
+
+
+FORMS = {
+    "gs3d_f64": {"dim": 3, "constants": ("F", "k", "Du", "Dv", "dt", "dx")},
+    "gs3d_f32k": {"dim": 3, "constants": ("F", "k", "Du", "Dv", "dt", "dx")},
+    "diff2d_f64": {"dim": 2, "constants": ("Dt", "Dx")},
+}
+
+
+def _delta_name(delta: Sequence[int]) -> str:
+    # Translate.hs:406-407 + toCName (:317-343): "mpi_rank_" + "_1_0_m1"
+    return "mpi_rank_" + "".join("_" + ("m%d" % -d if d < 0 else "%d" % d) for d in delta)
+
+
+def _c_double(v: float) -> str:
+    return repr(float(v))
+
+
+def emit_header(p: Program) -> str:
+    p.validate()
+    ax = p.axis_names
+    dims = "".join("[%d]" % n for n in p.shape)
+    lines = [
+        "/* %s.h — emitted by formura_gb300.backend (form %s). */" % (p.name, p.form),
+        "",
+        "#pragma once",
+        "#ifdef __cplusplus",
+        'extern "C"',
+        "{",
+        "#endif",
+        "#include <stdint.h>",
+        '#include "formura_mpi_stub.h"',
+        "",
+    ]
+    for a, n in zip(ax, p.shape):
+        lines.append("#define N%s  %d" % (a.upper(), n))
+    lines.append("")
+    for s in p.state_names + p.extra_state_names:
+        lines.append("extern %s %s%s;" % (p.elem, s, dims))
+    lines.append("")
+    lines.append("struct Formura_Navigator {")
+    lines.append("int time_step;")
+    for a in ax:
+        lines.append("int lower_%s;" % a)
+        lines.append("int upper_%s;" % a)
+        lines.append("int offset_%s;" % a)
+    lines.append("union { MPI_Comm mpi_comm; uint64_t mpi_comm_storage_; };")
+    lines.append("int mpi_my_rank;")
+    for delta in itertools.product((-1, 0, 1), repeat=p.dim):
+        lines.append("int %s;" % _delta_name(delta))
+    lines.append("};")
+    lines.append("extern struct Formura_Navigator navi;")
+    lines.append("")
+    lines.append("int Formura_Init (struct Formura_Navigator *navi, MPI_Comm comm);")
+    lines.append("int Formura_Forward (struct Formura_Navigator *navi);")
+    lines.append("")
+    lines.append("/* Extensions of the GB300 engine (no counterpart in the generated C). */")
+    lines.append("#define FORMURA_STEPS_PER_FORWARD %d" % p.steps_per_forward)
+    lines.append("int Formura_Upload (void);")
+    lines.append("int Formura_Advance (struct Formura_Navigator *navi, int n_forward);")
+    lines.append("int Formura_Download (void);")
+    lines.append("void *Formura_Device_State (int index);")
+    lines.append("int Formura_Set_Stream (void *cuda_stream);")
+    lines.append("int Formura_Conserved_Totals (double *totals);")
+    lines.append("int Formura_Finalize (void);")
+    lines.append("const char *Formura_Last_Error (void);")
+    lines += ["", "#ifdef __cplusplus", "}", "#endif", ""]
+    return "\n".join(lines)
+
+
+def _forward_call(p: Program) -> str:
+    c = p.constants
+    nx = p.shape
+    if p.form == "gs3d_f64":
+        return (
+            "fm_gs_params prm = {%s, %s, %s, %s, %s, %s};\n"
+            "  return fm_gs3d_f64_forward(%d, %d, %d, (double*)g_dev[0], (double*)g_dev[1],"
+            " (double*)g_work, (double*)g_work + NCELLS, &prm, steps, g_stream);"
+            % (_c_double(c["F"]), _c_double(c["k"]), _c_double(c["Du"]), _c_double(c["Dv"]),
+               _c_double(c["dt"]), _c_double(c["dx"]), nx[0], nx[1], nx[2]))
+    if p.form == "gs3d_f32k":
+        return (
+            "fm_gs_params prm = {%s, %s, %s, %s, %s, %s};\n"
+            "  return fm_gs3d_f32k_forward(%d, %d, %d, (float*)g_dev[0], (float*)g_dev[1],"
+            " (float*)g_dev[2], (float*)g_dev[3], (float*)g_work, steps, %d, &prm, g_stream);"
+            % (_c_double(c["F"]), _c_double(c["k"]), _c_double(c["Du"]), _c_double(c["Dv"]),
+               _c_double(c["dt"]), _c_double(c["dx"]), nx[0], nx[1], nx[2],
+               int(p.temporal_blocking_interval)))
+    if p.form == "diff2d_f64":
+        # node pair pow(Dx,2) then Dt/that, evaluated in double by host libm as the
+        # generated C does (`**` -> pow, Translate.hs:594)
+        return (
+            "const double coef = %s / pow(%s, 2.0);\n"
+            "  return fm_diff2d_f64_forward(%d, %d, (double*)g_dev[0], (double*)g_work, coef,"
+            " steps, g_stream);" % (_c_double(c["Dt"]), _c_double(c["Dx"]), nx[0], nx[1]))
+    raise ValueError(p.form)
+
+
+def _work_elems(p: Program) -> str:
+    if p.form == "gs3d_f64":
+        return "2 * NCELLS"
+    if p.form == "gs3d_f32k":
+        return "4 * NCELLS"
+    return "NCELLS"
+
+
+def emit_source(p: Program) -> str:
+    p.validate()
+    dims = "".join("[%d]" % n for n in p.shape)
+    states = p.state_names + p.extra_state_names
+    ncells = 1
+    for n in p.shape:
+        ncells *= n
+    ax = p.axis_names
+    out: List[str] = []
+    w = out.append
+    w("/* %s.cpp — emitted by formura_gb300.backend (form %s).\n"
+      " * Host side of Formura's generated-code API on one GB300; the time steps run\n"
+      " * in libformura_gb300.so (include/formura_gb300.h). */" % (p.name, p.form))
+    w('#include "%s.h"' % p.name)
+    w('#include "formura_gb300.h"')
+    w("#include <math.h>")
+    w("#include <stddef.h>")
+    w("#include <stdio.h>")
+    w("")
+    w("#define NCELLS ((size_t)%d)" % ncells)
+    w("#define FMR_EXPORT __attribute__((visibility(\"default\")))")
+    w("")
+    w('extern "C" {')
+    for s in states:
+        w("FMR_EXPORT %s %s%s __attribute__((aligned(4096)));" % (p.elem, s, dims))
+    w("FMR_EXPORT struct Formura_Navigator navi;")
+    w("}")
+    w("")
+    w("static const int kNState = %d;" % len(states))
+    w("static void *const kHost[%d] = {%s};" % (len(states), ", ".join("(void*)%s" % s for s in states)))
+    w("static void *g_dev[%d] = {0};" % len(states))
+    w("static void *g_work = 0;")
+    w("static double *g_totals = 0;   /* device: per-state totals + scratch */")
+    w("static void *g_stream = 0;")
+    w("static int g_ready = 0;")
+    w("static char g_msg[600];")
+    w("static const size_t kBytes = NCELLS * sizeof(%s);" % p.elem)
+    w("")
+    w("static int fail(int st, const char *where) {")
+    w('  snprintf(g_msg, sizeof g_msg, "%s: %s (%s)", where, fm_status_name(st), fm_last_error());')
+    w("  return st;")
+    w("}")
+    w("")
+    w("static int ensure_device(void) {")
+    w("  if (g_ready) return 0;")
+    w("  int st;")
+    w("  for (int i = 0; i < kNState; ++i) {")
+    w('    if ((st = fm_malloc(&g_dev[i], kBytes))) return fail(st, "fm_malloc(state)");')
+    w("    fm_host_register(kHost[i], kBytes);  /* pinned: best effort */")
+    w("  }")
+    w('  if ((st = fm_malloc(&g_work, (%s) * sizeof(%s)))) return fail(st, "fm_malloc(work)");'
+      % (_work_elems(p), p.elem))
+    w("  const size_t scratch = fm_sum_f64_scratch_elems((int64_t)NCELLS);")
+    w('  if ((st = fm_malloc((void**)&g_totals, (kNState + scratch) * sizeof(double)))) return fail(st, "fm_malloc(totals)");')
+    w("  g_ready = 1;")
+    w("  return 0;")
+    w("}")
+    w("")
+    w("static int run_steps(int steps) {")
+    w("  %s" % _forward_call(p))
+    w("}")
+    w("")
+    w('extern "C" {')
+    w("")
+    w("FMR_EXPORT int Formura_Init (struct Formura_Navigator *nv, MPI_Comm comm) {")
+    w("  nv->mpi_comm_storage_ = 0;")
+    w("  nv->mpi_comm = comm;")
+    w("  nv->mpi_my_rank = 0;")
+    for delta in itertools.product((-1, 0, 1), repeat=p.dim):
+        w("  nv->%s = 0;" % _delta_name(delta))
+    w("  nv->time_step = 0;")
+    for a, n in zip(ax, p.shape):
+        w("  nv->offset_%s = 0; nv->lower_%s = 0; nv->upper_%s = %d;" % (a, a, a, n))
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Upload (void) {")
+    w("  int st = ensure_device(); if (st) return st;")
+    w("  for (int i = 0; i < kNState; ++i)")
+    w('    if ((st = fm_memcpy_h2d(g_dev[i], kHost[i], kBytes, g_stream))) return fail(st, "upload");')
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Download (void) {")
+    w("  int st = ensure_device(); if (st) return st;")
+    w("  for (int i = 0; i < kNState; ++i)")
+    w('    if ((st = fm_memcpy_d2h(kHost[i], g_dev[i], kBytes, g_stream))) return fail(st, "download");')
+    w('  if ((st = fm_stream_sync(g_stream))) return fail(st, "download sync");')
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Advance (struct Formura_Navigator *nv, int n_forward) {")
+    w("  int st = ensure_device(); if (st) return st;")
+    w("  if (n_forward < 0) return fail(FM_ERR_ARG, \"Formura_Advance: n_forward < 0\");")
+    w("  for (int i = 0; i < n_forward; ++i) {")
+    w('    if ((st = run_steps(FORMURA_STEPS_PER_FORWARD))) return fail(st, "Formura_Advance");')
+    w("    nv->time_step += FORMURA_STEPS_PER_FORWARD;")
+    w("  }")
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Forward (struct Formura_Navigator *nv) {")
+    w("  int st;")
+    w("  if ((st = Formura_Upload())) return st;")
+    w("  if ((st = Formura_Advance(nv, 1))) return st;")
+    w("  return Formura_Download();")
+    w("}")
+    w("")
+    w("FMR_EXPORT void *Formura_Device_State (int index) {")
+    w("  if (ensure_device() || index < 0 || index >= kNState) return 0;")
+    w("  return g_dev[index];")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Set_Stream (void *cuda_stream) { g_stream = cuda_stream; return 0; }")
+    w("")
+    w("FMR_EXPORT int Formura_Conserved_Totals (double *totals) {")
+    w("  int st = ensure_device(); if (st) return st;")
+    w("  if (!totals) return fail(FM_ERR_ARG, \"Formura_Conserved_Totals: NULL\");")
+    if p.elem == "double":
+        w("  for (int i = 0; i < kNState; ++i)")
+        w("    if ((st = fm_sum_f64((int64_t)NCELLS, (const double*)g_dev[i], g_totals + kNState, g_totals + i, g_stream)))")
+        w('      return fail(st, "fm_sum_f64");')
+    else:
+        w("  for (int i = 0; i < kNState; ++i)")
+        w("    if ((st = fm_sum_f32_as_f64((int64_t)NCELLS, (const float*)g_dev[i], g_totals + kNState, g_totals + i, g_stream)))")
+        w('      return fail(st, "fm_sum_f32_as_f64");')
+    w('  if ((st = fm_memcpy_d2h(totals, g_totals, kNState * sizeof(double), g_stream))) return fail(st, "totals");')
+    w('  if ((st = fm_stream_sync(g_stream))) return fail(st, "totals sync");')
+    w("  for (int i = 0; i < kNState; ++i) if (!isfinite(totals[i])) return fail(FM_ERR_NONFINITE, \"non-finite state\");")
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Finalize (void) {")
+    w("  if (!g_ready) return 0;")
+    w("  fm_stream_sync(g_stream);")
+    w("  for (int i = 0; i < kNState; ++i) { fm_free(g_dev[i]); g_dev[i] = 0; fm_host_unregister(kHost[i]); }")
+    w("  fm_free(g_work); g_work = 0; fm_free(g_totals); g_totals = 0;")
+    w("  g_ready = 0;")
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT const char *Formura_Last_Error (void) { return g_msg; }")
+    w("")
+    w("}  /* extern \"C\" */")
+    w("")
+    return "\n".join(out)
+
+
+def program_dir(root: Optional[Path] = None) -> Path:
+    return (root or _build.BUILD) / "programs"
+
+
+def build_program(p: Program, outdir: Optional[Path] = None, verbose: bool = False) -> Path:
+    """Emit ``<name>.h``/``<name>.cpp`` and compile ``lib<name>.so`` (g++)."""
+    outdir = Path(outdir) if outdir else program_dir()
+    outdir.mkdir(parents=True, exist_ok=True)
+    hdr, src = emit_header(p), emit_source(p)
+    lib = _build.LIB
+    if not lib.exists():
+        _build.build_library(verbose=verbose)
+    key = hashlib.sha256((hdr + src + str(lib.stat().st_mtime_ns)).encode()).hexdigest()[:16]
+    so = outdir / ("lib%s.so" % p.name)
+    stamp = outdir / ("lib%s.stamp" % p.name)
+    if so.exists() and stamp.exists() and stamp.read_text() == key:
+        return so
+    (outdir / (p.name + ".h")).write_text(hdr)
+    (outdir / (p.name + ".cpp")).write_text(src)
+    cmd = [
+        os.environ.get("CXX", "g++"), "-O2", "-fPIC", "-shared", "-std=c++17",
+        "-fvisibility=hidden", "-I", str(outdir), "-I", str(_build.INCLUDE),
+        "-o", str(so) + ".tmp", str(outdir / (p.name + ".cpp")),
+        "-L", str(lib.parent), "-lformura_gb300",
+        "-Wl,-rpath," + str(lib.parent), "-lm",
+    ]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("building %s failed:\n%s" % (p.name, r.stdout))
+    os.replace(str(so) + ".tmp", so)
+    stamp.write_text(key)
+    return so
+
+
+def build_programs(verbose: bool = False) -> List[Path]:
+    from .programs import PROGRAMS
+
+    return [build_program(p, verbose=verbose) for p in PROGRAMS.values()]

@@ -1,0 +1,188 @@
+// fm_diff2d.cu — 2D diffusion (examples/diffusion.fmr form in 2D), FP64,
+// bit-exact with the generated loop nest.
+//
+// 256^2 FP64 is 512 KB: the whole state lives in L2, and one step is ~1 us of
+// FP64 work spread over every SM.  Launch overhead would dominate, so all
+// steps run in ONE cooperative persistent launch; blocks meet at a grid
+// barrier between steps.  Every wait in that barrier is bounded: past
+// fm::kSpinLimit polls the block sets an error word and all blocks return, and
+// the entry point reports FM_ERR_TIMEOUT.
+//
+// Per cell (diffusion.fmr:5-7,20):  lap_a = ((d[+1]-d)/2 - (d-d[-1])/2)/2,
+//   dens' = dens + coef*(lap_x + lap_y).  x/2 is evaluated as x*0.5 — the same
+//   correctly rounded value for every double.  Lanes run along y (the fastest
+//   axis); the y flux at +1/2 comes from the next lane by shuffle.
+#include <algorithm>
+#include <mutex>
+
+#include "fm_common.cuh"
+
+namespace {
+
+struct GridSync {
+  unsigned int arrive;
+  unsigned int gen;
+  int err;
+  int pad;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier for a cooperative launch; false if the wait gave up.
+__device__ bool grid_barrier(GridSync *gs, unsigned nblocks, unsigned &gen_local) {
+  __shared__ int s_fail;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int fail = 0;
+    const unsigned target = gen_local + 1;
+    __threadfence();
+    if (atomicAdd(&gs->arrive, 1u) == nblocks - 1) {
+      atomicExch(&gs->arrive, 0u);
+      __threadfence();
+      atomicExch(&gs->gen, target);
+    } else {
+      long long spins = 0;
+      while (ld_acquire_u32(&gs->gen) != target) {
+        if (++spins > fm::kSpinLimit || *((volatile int *)&gs->err) != 0) {
+          atomicExch(&gs->err, 1);
+          fail = 1;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    s_fail = fail;
+  }
+  __syncthreads();
+  gen_local += 1;
+  return s_fail == 0;
+}
+
+__device__ __forceinline__ double diff_cell(const double *__restrict__ src, int x, int y,
+                                            int nx, int ny, int lane, double coef) {
+  const size_t row = (size_t)x * ny;
+  const double a = __ldcg(src + row + y);
+  const double axp = __ldcg(src + (size_t)fm::wrap_up(x, nx) * ny + y);
+  const double axm = __ldcg(src + (size_t)fm::wrap_dn(x, nx) * ny + y);
+  double aym = __shfl_up_sync(0xffffffffu, a, 1);
+  if (lane == 0) aym = __ldcg(src + row + fm::wrap_dn(y, ny));
+  const double f_1 = (a - aym) * 0.5;  // (d - d[y-1])/2
+  double f_0 = __shfl_down_sync(0xffffffffu, f_1, 1);
+  if (lane == 31) f_0 = (__ldcg(src + row + fm::wrap_up(y, ny)) - a) * 0.5;
+  const double e_0 = (axp - a) * 0.5;
+  const double e_1 = (a - axm) * 0.5;
+  const double e_2 = (e_0 - e_1) * 0.5;
+  const double f_2 = (f_0 - f_1) * 0.5;
+  const double g = e_2 + f_2;
+  const double h = coef * g;
+  return a + h;
+}
+
+__global__ void __launch_bounds__(256)
+    diff2d_persistent(double *a, double *b, int nx, int ny, double coef, int steps,
+                      GridSync *gs) {
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int segs_per_row = ny >> 5;
+  const int nseg = nx * segs_per_row;
+  unsigned gen = 0;
+  double *src = a, *dst = b;
+  for (int s = 0; s < steps; ++s) {
+    for (int sg = gwarp; sg < nseg; sg += nwarps) {
+      const int x = sg / segs_per_row;
+      const int y = (sg % segs_per_row) * 32 + lane;
+      __stcg(dst + (size_t)x * ny + y, diff_cell(src, x, y, nx, ny, lane, coef));
+    }
+    if (!grid_barrier(gs, gridDim.x, gen)) return;
+    double *t = src;
+    src = dst;
+    dst = t;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    diff2d_step(const double *src, double *dst, int nx, int ny, double coef) {
+  const int lane = threadIdx.x & 31;
+  const int segs_per_row = ny >> 5;
+  const int nseg = nx * segs_per_row;
+  const int sg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (sg >= nseg) return;
+  const int x = sg / segs_per_row;
+  const int y = (sg % segs_per_row) * 32 + lane;
+  dst[(size_t)x * ny + y] = diff_cell(src, x, y, nx, ny, lane, coef);
+}
+
+std::mutex g_mu;
+GridSync *g_sync[64] = {nullptr};
+
+int get_sync(GridSync **out) {
+  int dev = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64) return FM_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_sync[dev]) FM_TRY_CUDA(cudaMalloc(&g_sync[dev], sizeof(GridSync)));
+  *out = g_sync[dev];
+  return FM_OK;
+}
+
+}  // namespace
+
+extern "C" int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
+                                     double coef, int steps, void *stream) {
+  FM_CHECK_ARG(dens && work, "fm_diff2d_f64_forward: NULL argument");
+  FM_CHECK_ARG(nx >= 1 && ny >= 32 && ny % 32 == 0,
+               "fm_diff2d_f64_forward: need ny %% 32 == 0 (got %d x %d)", nx, ny);
+  FM_CHECK_ARG(steps >= 0, "fm_diff2d_f64_forward: steps < 0");
+  if (steps == 0) return FM_OK;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)nx * ny;
+  int sms = 0;
+  int st = fm::device_sm_count(&sms);
+  if (st) return st;
+  int per_sm = 0;
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, diff2d_persistent, 256, 0));
+  const long long nseg = (long long)nx * (ny / 32);
+  const int want = (int)std::min<long long>((nseg + 7) / 8, (long long)sms * std::min(per_sm, 2));
+  int coop = 0, dev = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  FM_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (coop && per_sm >= 1 && want >= 1) {
+    GridSync *gs = nullptr;
+    st = get_sync(&gs);
+    if (st) return st;
+    FM_TRY_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), s));
+    double *a = dens, *b = work;
+    int nxv = nx, nyv = ny, stv = steps;
+    double cf = coef;
+    void *args[] = {&a, &b, &nxv, &nyv, &cf, &stv, &gs};
+    FM_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)diff2d_persistent, dim3(want),
+                                            dim3(256), args, 0, s));
+    GridSync host;
+    FM_TRY_CUDA(cudaMemcpyAsync(&host, gs, sizeof(GridSync), cudaMemcpyDeviceToHost, s));
+    FM_TRY_CUDA(cudaStreamSynchronize(s));
+    if (host.err) {
+      fm::set_error("fm_diff2d_f64_forward: grid barrier wait gave up");
+      return FM_ERR_TIMEOUT;
+    }
+    if (steps & 1) FM_TRY_CUDA(cudaMemcpyAsync(dens, work, n * sizeof(double),
+                                               cudaMemcpyDeviceToDevice, s));
+    return FM_OK;
+  }
+  // Fallback on devices without cooperative launch: one launch per step.
+  double *src = dens, *dst = work;
+  const int blocks = (int)((nseg * 32 + 255) / 256);
+  for (int i = 0; i < steps; ++i) {
+    diff2d_step<<<blocks, 256, 0, s>>>(src, dst, nx, ny, coef);
+    std::swap(src, dst);
+  }
+  FM_TRY_CUDA(cudaGetLastError());
+  if (src != dens)
+    FM_TRY_CUDA(cudaMemcpyAsync(dens, src, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return FM_OK;
+}

@@ -1,0 +1,74 @@
+"""Seeded initial states of the shipped workloads.
+
+All randomness comes from splitmix64 (S. Vigna's public-domain generator,
+also the seeding step of xoshiro), so the same seed gives the same state on
+any machine — unlike the ``srand(time(NULL))``/``rand()`` of the reference's
+drivers (examples/pearson-3d-main.cpp:164, examples/pearson-2d-main.cpp:13-33).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    """The n outputs following state `seed` (+ offset draws), as uint64."""
+    with np.errstate(over="ignore"):
+        i = np.arange(offset + 1, offset + n + 1, dtype=np.uint64)
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + i * _GOLDEN
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, n: int, offset: int = 0) -> np.ndarray:
+    """n doubles uniform in [0, 1) (53-bit)."""
+    return (splitmix64(seed, n, offset) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+
+
+def diffusion_2d(nx: int, ny: int, seed: int = 1) -> np.ndarray:
+    """Uniform [0,1) density, the 2D diffusion workload's initial state."""
+    return uniform(seed, nx * ny).reshape(nx, ny)
+
+
+def gray_scott_3d(nx: int, ny: int, nz: int, seed: int = 1, ncubes: int = 8, side: int = 16,
+                  dtype=np.float64):
+    """U=1, V=0, plus `ncubes` cubes of side `side` at seeded positions (periodic
+    wrap) where U = 0.5 and V = 0.25, each with +-1% uniform noise."""
+    U = np.ones((nx, ny, nz), dtype=np.float64)
+    V = np.zeros((nx, ny, nz), dtype=np.float64)
+    pos = splitmix64(seed, 3 * ncubes)
+    s = min(side, nx, ny, nz)
+    draws = 3 * ncubes
+    for c in range(ncubes):
+        x0 = int(pos[3 * c] % np.uint64(nx))
+        y0 = int(pos[3 * c + 1] % np.uint64(ny))
+        z0 = int(pos[3 * c + 2] % np.uint64(nz))
+        ix = (x0 + np.arange(s)) % nx
+        iy = (y0 + np.arange(s)) % ny
+        iz = (z0 + np.arange(s)) % nz
+        r = uniform(seed, 2 * s ** 3, offset=draws).reshape(2, s, s, s)
+        draws += 2 * s ** 3
+        U[np.ix_(ix, iy, iz)] = 0.5 * (1.0 + 0.01 * (2.0 * r[0] - 1.0))
+        V[np.ix_(ix, iy, iz)] = 0.25 * (1.0 + 0.01 * (2.0 * r[1] - 1.0))
+    return U.astype(dtype), V.astype(dtype)
+
+
+def gray_scott_2d_square(nx: int, ny: int, seed: int = 1, dtype=np.float64, frac: float = 0.2):
+    """The 2D Gray-Scott start of examples/pearson-2d-main.cpp:16-33 scaled to
+    the grid: U=1, V=0 with one seeded square (side frac*N) set to
+    U = 0.5 + 0.01 r, V = 0.25 + 0.01 r."""
+    U = np.ones((nx, ny), dtype=np.float64)
+    V = np.zeros((nx, ny), dtype=np.float64)
+    p = splitmix64(seed, 2)
+    sx, sy = max(1, int(frac * nx)), max(1, int(frac * ny))
+    x0, y0 = int(p[0] % np.uint64(nx)), int(p[1] % np.uint64(ny))
+    ix = (x0 + np.arange(sx)) % nx
+    iy = (y0 + np.arange(sy)) % ny
+    r = uniform(seed, 2 * sx * sy, offset=2).reshape(2, sx, sy)
+    U[np.ix_(ix, iy)] = 0.5 + 0.01 * r[0]
+    V[np.ix_(ix, iy)] = 0.25 + 0.01 * r[1]
+    return U.astype(dtype), V.astype(dtype)

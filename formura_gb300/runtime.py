@@ -1,0 +1,127 @@
+"""Python driver of an emitted program library (the reference's main.cpp role).
+
+A Formura user's driver includes the generated header, calls ``Formura_Init``,
+writes the initial state into the global arrays between ``navi.lower_*`` and
+``navi.upper_*``, and calls ``Formura_Forward`` in a loop
+(examples/pearson-3d-main.cpp:160-245, examples/diffusion-main.cpp:7-16).
+:class:`FormuraProgram` does the same through ctypes: the globals are exposed
+as numpy arrays that alias the library's memory, and the navigator as a
+ctypes structure laid out like the emitted header's.
+"""
+from __future__ import annotations
+
+import ctypes
+import itertools
+from pathlib import Path
+from typing import Dict, Optional, Union
+
+import numpy as np
+
+from . import backend
+from ._lib import FormuraError, STATUS_NAMES, lib as _core_lib
+from .backend import Program, _delta_name
+
+
+def navigator_type(p: Program):
+    fields = [("time_step", ctypes.c_int)]
+    for a in p.axis_names:
+        fields += [("lower_" + a, ctypes.c_int), ("upper_" + a, ctypes.c_int),
+                   ("offset_" + a, ctypes.c_int)]
+    fields += [("mpi_comm_storage_", ctypes.c_uint64), ("mpi_my_rank", ctypes.c_int)]
+    for d in itertools.product((-1, 0, 1), repeat=p.dim):
+        fields.append((_delta_name(d), ctypes.c_int))
+    return type("Formura_Navigator_" + p.name, (ctypes.Structure,), {"_fields_": fields})
+
+
+class FormuraProgram:
+    """One loaded ``lib<name>.so``: Formura_Init / Formura_Forward and globals."""
+
+    def __init__(self, program: Program, so_path: Path):
+        _core_lib()  # the engine must load; there is no other path
+        self.program = program
+        self.path = Path(so_path)
+        self.lib = ctypes.CDLL(str(self.path))
+        L = self.lib
+        nav_t = navigator_type(program)
+        self.navi = nav_t.in_dll(L, "navi")
+        self._nav_ptr = ctypes.pointer(self.navi)
+        for name in ("Formura_Init",):
+            getattr(L, name).argtypes = [ctypes.POINTER(nav_t), ctypes.c_int]
+        for name in ("Formura_Forward",):
+            getattr(L, name).argtypes = [ctypes.POINTER(nav_t)]
+        L.Formura_Advance.argtypes = [ctypes.POINTER(nav_t), ctypes.c_int]
+        L.Formura_Device_State.argtypes = [ctypes.c_int]
+        L.Formura_Device_State.restype = ctypes.c_void_p
+        L.Formura_Set_Stream.argtypes = [ctypes.c_void_p]
+        L.Formura_Conserved_Totals.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        L.Formura_Last_Error.restype = ctypes.c_char_p
+        ctype = ctypes.c_float if program.elem == "float" else ctypes.c_double
+        dtype = np.float32 if program.elem == "float" else np.float64
+        n = int(np.prod(program.shape))
+        self.state: Dict[str, np.ndarray] = {}
+        for s in program.state_names + program.extra_state_names:
+            buf = (ctype * n).in_dll(L, s)
+            self.state[s] = np.frombuffer(buf, dtype=dtype).reshape(program.shape)
+        self.steps_per_forward = program.steps_per_forward
+
+    # -- error handling -------------------------------------------------------
+    def _check(self, st: int, where: str):
+        if st != 0:
+            msg = (self.lib.Formura_Last_Error() or b"").decode(errors="replace")
+            raise FormuraError(st, where, msg)
+
+    # -- the generated API ------------------------------------------------------
+    def init(self, comm: int = 0):
+        self._check(self.lib.Formura_Init(self._nav_ptr, comm), "Formura_Init")
+
+    def forward(self):
+        self._check(self.lib.Formura_Forward(self._nav_ptr), "Formura_Forward")
+
+    # -- extensions ---------------------------------------------------------------
+    def upload(self):
+        self._check(self.lib.Formura_Upload(), "Formura_Upload")
+
+    def advance(self, n_forward: int = 1):
+        self._check(self.lib.Formura_Advance(self._nav_ptr, int(n_forward)), "Formura_Advance")
+
+    def download(self):
+        self._check(self.lib.Formura_Download(), "Formura_Download")
+
+    def device_state(self, index: int) -> int:
+        p = self.lib.Formura_Device_State(int(index))
+        if not p:
+            raise FormuraError(2, "Formura_Device_State",
+                               (self.lib.Formura_Last_Error() or b"").decode())
+        return int(p)
+
+    def set_stream(self, stream_ptr: int):
+        self._check(self.lib.Formura_Set_Stream(ctypes.c_void_p(stream_ptr)), "Formura_Set_Stream")
+
+    def conserved_totals(self) -> np.ndarray:
+        k = len(self.program.state_names) + len(self.program.extra_state_names)
+        out = (ctypes.c_double * k)()
+        self._check(self.lib.Formura_Conserved_Totals(out), "Formura_Conserved_Totals")
+        return np.array(out[:], dtype=np.float64)
+
+    def finalize(self):
+        self._check(self.lib.Formura_Finalize(), "Formura_Finalize")
+
+
+_loaded: Dict[str, FormuraProgram] = {}
+
+
+def load_program(program: Union[str, Program], outdir: Optional[Path] = None) -> FormuraProgram:
+    """Emit + build (if stale) and load a program library.  A program name is
+    looked up in :data:`formura_gb300.programs.PROGRAMS`."""
+    if isinstance(program, str):
+        from .programs import PROGRAMS
+
+        program = PROGRAMS[program]
+    so = backend.build_program(program, outdir=outdir)
+    key = str(so)
+    if key not in _loaded:
+        _loaded[key] = FormuraProgram(program, so)
+    return _loaded[key]
+
+
+__all__ = ["FormuraProgram", "load_program", "navigator_type", "FormuraError", "STATUS_NAMES"]

@@ -1,0 +1,166 @@
+/*
+ * formura_gb300.h — thin C ABI of the GB300 stencil engine (libformura_gb300.so).
+ *
+ * Formura's generated C runs its time-step loop inside Formura_Forward
+ * (src/Formura/MPICxx/Translate.hs:1106-1131): M = monitor_interval steps of
+ * region loop nests (genComputation, Translate.hs:671-737), ridge copies
+ * (genStagingCode, :742-796) and MPI facet exchanges (:798-836).  This library
+ * replaces that body.  The per-program host code that the back end
+ * (formura_gb300/backend.py) emits — the header with `struct Formura_Navigator`,
+ * the global state arrays, Formura_Init and Formura_Forward — calls the entry
+ * points below with plain device pointers.
+ *
+ * Conventions
+ *  - Arrays are dense, row-major, last axis fastest (U[x][y][z]), exactly the
+ *    index order of the generated code; periodic boundaries are applied by index
+ *    wrap inside the kernels (the one-GPU form of the self-send halo exchange,
+ *    Translate.hs:1062-1068).
+ *  - Every entry point returns an fm_status (0 = FM_OK).  On error,
+ *    fm_last_error() returns a message for the calling thread.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *    Entry points enqueue work and return; they do not synchronize unless the
+ *    comment says so.
+ *  - Device arrays must be 256-byte aligned (cudaMalloc guarantees it).
+ *  - There is no CPU fallback: without a CUDA device every compute entry point
+ *    returns FM_ERR_CUDA.
+ */
+#ifndef FORMURA_GB300_H
+#define FORMURA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Exported even when the library is compiled with -fvisibility=hidden. */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef enum {
+  FM_OK = 0,
+  FM_ERR_ARG = 1,         /* bad size, pointer or parameter */
+  FM_ERR_CUDA = 2,        /* a CUDA runtime call failed (no device, launch error, ...) */
+  FM_ERR_TIMEOUT = 3,     /* a bounded device-side wait gave up (see fm_*_status words) */
+  FM_ERR_NONFINITE = 4,   /* a conserved-total check found NaN or Inf */
+  FM_ERR_UNSUPPORTED = 5, /* shape or option this build does not handle */
+  FM_ERR_NOMEM = 6        /* device allocation failed */
+} fm_status;
+
+/* ---- runtime helpers used by the emitted host code ----------------------- */
+
+/* Message for the last failing call on this thread ("" if none). */
+const char *fm_last_error(void);
+/* Static name of a status code. */
+const char *fm_status_name(int status);
+/* Library version string, e.g. "formura-gb300 0.1 sm_103a". */
+const char *fm_version(void);
+/* Number of visible CUDA devices (0 when there is none; never fails). */
+int fm_device_count(void);
+
+int fm_malloc(void **ptr, size_t bytes);
+int fm_free(void *ptr);
+int fm_memset(void *ptr, int value, size_t bytes, void *stream);
+int fm_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
+int fm_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int fm_memcpy_d2d(void *dst, const void *src, size_t bytes, void *stream);
+int fm_stream_sync(void *stream);
+/* Page-locks an existing host range (the generated globals) so that the
+ * copies above run at full link speed; fm_host_unregister undoes it. */
+int fm_host_register(void *ptr, size_t bytes);
+int fm_host_unregister(void *ptr);
+
+/* ---- Gray-Scott reaction-diffusion ---------------------------------------- */
+
+/* Constants of the Gray-Scott .fmr forms (examples/pearson-2d.fmr:16-17,
+ * examples/pearson-3d.fmr:3-4 in the F,k parameterisation). */
+typedef struct {
+  double F, k, Du, Dv, dt, dx;
+} fm_gs_params;
+
+/*
+ * 3D Gray-Scott in the examples/pearson-3d.fmr form, FP64, bit-exact with the
+ * generated loop nest (Translate.hs:671-737 over the DAG of pearson-3d.fmr:13-24
+ * with the F,k reaction of pearson-2d.fmr:21-22):
+ *   lap_a(W) = ((W[+1]-W)/dx - (W-W[-1])/dx)/dx,  lap = (lap_x + lap_y) + lap_z
+ *   U' = U + dt*(((-(U*V*V)) + F*(1-U)) + Du*lap(U))
+ *   V' = V + dt*(((U*V*V) - (F+k)*V) + Dv*lap(V))
+ * Advances U,V ([nx][ny][nz] device arrays) by `steps` in place.  work_U,
+ * work_V are device arrays of the same size used as the other half of the
+ * ping-pong pair (contents on return unspecified).
+ * Replaces the Computation loop nests of Formura_Forward
+ * (Translate.hs:1121-1131, genComputation :671-737).
+ * Requires nz % 32 == 0, ny % 16 == 0, nx >= 1, and 2^-40 <= dx <= 2^40.
+ */
+int fm_gs3d_f64_forward(int nx, int ny, int nz, double *U, double *V,
+                        double *work_U, double *work_V, const fm_gs_params *p,
+                        int steps, void *stream);
+
+/*
+ * 3D Gray-Scott, same form, binary32 arithmetic with compensated (Kahan) time
+ * accumulation: per field y = dt*dW - cW; t = W + y; cW = (t - W) - y; W = t.
+ * U,V,cU,cV are [nx][ny][nz] float device arrays (cU,cV = running
+ * compensation, zero them before the first call); work must hold 4*nx*ny*nz
+ * floats.  `tb` = time steps fused per HBM pass (temporal blocking depth;
+ * 1 = one step per pass; 0 = library default).
+ * Bit-exact with the binary32 restatement of the same DAG without FMA
+ * contraction.  Requires nz % 32 == 0, ny % 8 == 0, 2^-20 <= (float)dx <= 2^20.
+ */
+int fm_gs3d_f32k_forward(int nx, int ny, int nz, float *U, float *V, float *cU,
+                         float *cV, float *work, int steps, int tb,
+                         const fm_gs_params *p, void *stream);
+
+/* ---- 2D diffusion --------------------------------------------------------- */
+
+/*
+ * 2D diffusion in the examples/diffusion.fmr form reduced to 2D, FP64, bit-exact:
+ *   dens' = dens + (Dt / pow(Dx,2)) * (lap_x + lap_y),
+ *   lap_a = ((d[+1]-d)/2 - (d-d[-1])/2)/2.
+ * `coef` is the node Dt / Dx**2, evaluated by the caller in double with the
+ * host libm pow exactly as the generated code does (diffusion.fmr:20,
+ * Translate.hs:594).  dens is [nx][ny]; work is another nx*ny doubles.
+ * Runs all `steps` in one persistent launch when the grid fits the device
+ * (grid barriers with bounded waits); else one launch per step.
+ * Requires ny % 32 == 0.
+ */
+int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
+                          double coef, int steps, void *stream);
+
+/* ---- conserved totals ------------------------------------------------------ */
+
+/*
+ * Sum of n doubles (mass/energy totals) into *out_device (one double in device
+ * memory).  Deterministic: a fixed two-level tree whose shape depends only on
+ * n.  `partials` is caller-provided scratch of fm_sum_f64_scratch_elems(n)
+ * doubles.  A NaN or Inf anywhere in the input propagates to the total; the
+ * emitted host code reads it back and returns FM_ERR_NONFINITE.
+ */
+size_t fm_sum_f64_scratch_elems(int64_t n);
+int fm_sum_f64(int64_t n, const double *a, double *partials, double *out_device,
+               void *stream);
+/* Same tree over binary32 input, accumulated in double (FP32 state totals). */
+int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
+                      double *out_device, void *stream);
+
+/* ---- measurement ------------------------------------------------------------ */
+
+/*
+ * FMA-pipe probe used to measure the arithmetic roofline of this GPU:
+ * blocks x threads threads each run `iters` rounds of 8 independent FMA
+ * chains (fp64 != 0: double, else float), i.e. 16*iters flops per thread.
+ * `sink` is a device buffer of `blocks` elements of that type (never written
+ * in practice).  The caller times the launch on `stream`.
+ */
+int fm_probe_fma(int fp64, int blocks, int threads, int iters, void *sink,
+                 void *stream);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FORMURA_GB300_H */

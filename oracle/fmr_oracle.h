@@ -1,0 +1,71 @@
+/*
+ * fmr_oracle.h — CPU restatement of the per-cell arithmetic that Formura's
+ * generated C performs for the stencil programs this repository runs on the GPU.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, loads or
+ * calls this code; only the tests, the smoke check and the CPU-baseline leg of
+ * the benchmark do, as the checker and the timed CPU baseline.
+ *
+ * Every update follows the expression order that Formura's C back end emits
+ * (src/Formura/MPICxx/Translate.hs:481-629: one SSA temporary per DAG node,
+ * `**` -> pow, immediates -> double literals) for the named .fmr form, with
+ * periodic boundaries (the self-exchange of src/Formura/MPICxx/Translate.hs:1062-1068
+ * when mpi_grid_shape is all ones).  Built with -ffp-contract=off, each
+ * function is bit-for-bit the generated loop nest; the 2D Gray-Scott step is
+ * pinned against the reference's own examples-generated/pearson.c.
+ *
+ * Layout: row-major, last axis fastest (U[x][y][z]), no margin.
+ */
+#ifndef FMR_ORACLE_H
+#define FMR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Gray-Scott constants as the .fmr files name them. */
+typedef struct {
+  double F, k, Du, Dv, dt, dx;
+} fo_gs_params;
+
+/* 2D Gray-Scott, pearson-2d.fmr / examples-generated/pearson.fmr form
+ * (dU_dt and dV_dt manifested, then U_next = U + dt*dU_dt).  U,V are [nx][ny];
+ * advanced in place by `steps`.  Follows examples-generated/pearson.c:138-208. */
+void fo_gs2d_run_f64(int nx, int ny, double *U, double *V, int steps,
+                     const fo_gs_params *p);
+
+/* Same form in binary32 arithmetic (constants rounded to float, derived
+ * constants computed in float in DAG order): the oracle of the FP32 ensemble. */
+void fo_gs2d_run_f32(int nx, int ny, float *U, float *V, int steps,
+                     float F, float k, float Du, float Dv, float dt, float dx);
+
+/* 2D diffusion, examples/diffusion.fmr form reduced to 2D:
+ *   dens_next = dens + Dt / Dx**2 * sum_i ddx_i(ddx_i dens),
+ *   ddx a = (a[i+1/2] - a[i-1/2]) / 2.                       */
+void fo_diff2d_run_f64(int nx, int ny, double *dens, int steps, double Dt,
+                       double Dx);
+
+/* 3D Gray-Scott, examples/pearson-3d.fmr form (ddx a = (a[i+1/2]-a[i-1/2])/dx,
+ * reaction of pearson-2d.fmr:21-22, no manifest annotations).  [nx][ny][nz]. */
+void fo_gs3d_run_f64(int nx, int ny, int nz, double *U, double *V, int steps,
+                     const fo_gs_params *p);
+
+/* Same form in binary32 with compensated (Kahan) time accumulation:
+ *   y = dt*dU - cU;  t = U + y;  cU = (t - U) - y;  U = t.
+ * cU, cV carry the compensation between steps (start them at zero). */
+void fo_gs3d_run_f32_kahan(int nx, int ny, int nz, float *U, float *V,
+                           float *cU, float *cV, int steps, float F, float k,
+                           float Du, float Dv, float dt, float dx);
+
+/* Plain left-to-right double sum (conserved-total check). */
+double fo_sum_f64(int64_t n, const double *a);
+
+/* Number of OpenMP threads the oracle uses (1 without OpenMP). */
+int fo_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,124 @@
+"""The C ABI library: loads, exports what include/*.h declares, validates
+arguments before touching the device, and fails loudly without a GPU."""
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from formura_gb300 import _lib, backend
+from formura_gb300.build import INCLUDE, LIB
+
+DECL = re.compile(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(fm_\w+)\s*\(", re.M)
+
+
+def declared_symbols():
+    names = set()
+    for h in INCLUDE.glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names.update(DECL.findall(text))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(core_lib):
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    out = subprocess.run(["nm", "-D", "--defined-only", str(LIB)], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    missing = [s for s in syms if s not in exported]
+    assert not missing, missing
+    for s in syms:
+        assert hasattr(core_lib, s)
+    # ctypes signatures cover the whole header
+    assert set(syms) <= set(_lib.SIGNATURES), set(syms) - set(_lib.SIGNATURES)
+
+
+def test_version_and_status_names(core_lib):
+    assert b"sm_103a" in core_lib.fm_version()
+    assert core_lib.fm_status_name(0) == b"FM_OK"
+    assert core_lib.fm_status_name(3) == b"FM_ERR_TIMEOUT"
+    assert core_lib.fm_device_count() >= 0
+
+
+def test_argument_validation_precedes_device_work(core_lib):
+    p = _lib.GsParams(0.04, 0.06, 2e-5, 1e-5, 0.5, 0.01)
+    fake = ctypes.c_void_p(0x1000)
+    # nz not a multiple of 32
+    st = core_lib.fm_gs3d_f64_forward(8, 16, 30, fake, fake, fake, fake, ctypes.byref(p), 1, None)
+    assert st == 1 and b"nz" in core_lib.fm_last_error()
+    # NULL pointer
+    st = core_lib.fm_gs3d_f64_forward(8, 16, 32, None, fake, fake, fake, ctypes.byref(p), 1, None)
+    assert st == 1
+    # dx outside the exact-division range
+    bad = _lib.GsParams(0.04, 0.06, 2e-5, 1e-5, 0.5, 1e-30)
+    st = core_lib.fm_gs3d_f64_forward(8, 16, 32, fake, fake, fake, fake, ctypes.byref(bad), 1, None)
+    assert st == 1 and b"dx" in core_lib.fm_last_error()
+    st = core_lib.fm_diff2d_f64_forward(8, 30, fake, fake, 0.1, 1, None)
+    assert st == 1
+    st = core_lib.fm_gs3d_f32k_forward(8, 12, 32, fake, fake, fake, fake, fake, 1, 1,
+                                       ctypes.byref(p), None)
+    assert st == 1
+    # zero steps is a no-op that touches nothing
+    st = core_lib.fm_gs3d_f64_forward(8, 16, 32, fake, fake, fake, fake, ctypes.byref(p), 0, None)
+    assert st == 0
+
+
+def test_no_cpu_fallback_without_gpu(core_lib):
+    if core_lib.fm_device_count() > 0:
+        pytest.skip("a GPU is present")
+    p = _lib.GsParams(0.04, 0.06, 2e-5, 1e-5, 0.5, 0.01)
+    fake = ctypes.c_void_p(0x1000)
+    st = core_lib.fm_gs3d_f64_forward(8, 16, 32, fake, fake, fake, fake, ctypes.byref(p), 1, None)
+    assert st == 2  # FM_ERR_CUDA: no device, nothing computed on the host
+    ptr = ctypes.c_void_p()
+    assert core_lib.fm_malloc(ctypes.byref(ptr), 64) in (2, 6)
+
+
+def test_emitted_header_compiles_with_a_reference_style_driver(tmp_path):
+    """A driver written like examples/diffusion-main.cpp compiles and links
+    against an emitted program library."""
+    p = backend.Program(name="drv_diff", form="diff2d_f64", intra_node_shape=(32, 64),
+                        constants=dict(Dt=0.4, Dx=1.0), monitor_interval=20)
+    so = backend.build_program(p, outdir=tmp_path)
+    drv = tmp_path / "main.c"
+    drv.write_text(
+        '#include <stdio.h>\n#include "drv_diff.h"\n'
+        "int main(void){ struct Formura_Navigator nv; Formura_Init(&nv, MPI_COMM_WORLD);\n"
+        "  for(int x=nv.lower_x;x<nv.upper_x;++x) for(int y=nv.lower_y;y<nv.upper_y;++y) dens[x][y]=x+y;\n"
+        "  int st = Formura_Forward(&nv);\n"
+        '  printf("%d %d %d\\n", st, nv.time_step, NX*NY); return 0; }\n')
+    exe = tmp_path / "drv"
+    subprocess.run(["gcc", "-std=c11", "-I", str(tmp_path), "-I", str(INCLUDE), str(drv), "-o",
+                    str(exe), "-L", str(tmp_path), "-ldrv_diff", "-Wl,-rpath," + str(tmp_path)],
+                   check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    st, ts, n = map(int, r.stdout.split())
+    assert n == 32 * 64
+    if _lib.lib().fm_device_count() == 0:
+        assert st == 2 and ts == 0   # fails loudly, advances nothing
+    else:
+        assert st == 0 and ts == 20
+
+
+def test_navigator_layout_matches_header(tmp_path):
+    from formura_gb300.runtime import navigator_type
+
+    p = backend.Program(name="lay3", form="gs3d_f64", intra_node_shape=(16, 16, 32),
+                        constants=dict(F=0.04, k=0.06, Du=2e-5, Dv=1e-5, dt=0.5, dx=0.01),
+                        monitor_interval=4)
+    (tmp_path / "lay3.h").write_text(backend.emit_header(p))
+    nav = navigator_type(p)
+    fields = [f for f, _ in nav._fields_]
+    src = tmp_path / "off.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lay3.h"\nint main(void){'
+                   'printf("%zu", sizeof(struct Formura_Navigator));'
+                   + "".join('printf(" %%zu", offsetof(struct Formura_Navigator, %s));' % f
+                             for f in fields) + "return 0;}\n")
+    exe = tmp_path / "off"
+    subprocess.run(["gcc", "-I", str(tmp_path), "-I", str(INCLUDE), str(src), "-o", str(exe)],
+                   check=True)
+    vals = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()))
+    assert vals[0] == ctypes.sizeof(nav)
+    assert vals[1:] == [getattr(nav, f).offset for f in fields]
