@@ -308,6 +308,37 @@ def run_engine(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile_case(args):
+    """A few launches of one kernel on a small resident case, for ncu captures
+    (nothing is timed or printed as a bench value)."""
+    import torch
+
+    from formura_gb300 import inits, kernels
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda:0")
+    n = args.profile_n
+    if args.profile in ("gs3d_f64", "gs3d_f32k"):
+        U0, V0 = inits.gray_scott_3d(n, n, n, seed=1)
+        if args.profile == "gs3d_f64":
+            U, V = torch.from_numpy(U0).to(dev), torch.from_numpy(V0).to(dev)
+            kernels.gs3d_f64_forward(U, V, torch.empty_like(U), torch.empty_like(V),
+                                     kernels.gs_params(**GS), args.profile_steps)
+        else:
+            U = torch.from_numpy(U0.astype("float32")).to(dev)
+            V = torch.from_numpy(V0.astype("float32")).to(dev)
+            cU, cV = torch.zeros_like(U), torch.zeros_like(V)
+            w = torch.empty(4 * U.numel(), dtype=torch.float32, device=dev)
+            kernels.gs3d_f32k_forward(U, V, cU, cV, w, kernels.gs_params(**GS),
+                                      args.profile_steps, args.profile_tb)
+    elif args.profile == "diff2d":
+        d0 = inits.diffusion_2d(n, n, seed=1)
+        d = torch.from_numpy(d0).to(dev)
+        kernels.diff2d_f64_forward(d, torch.empty_like(d), 0.4, args.profile_steps)
+    torch.cuda.synchronize()
+    print("profile case %s n=%d steps=%d done" % (args.profile, n, args.profile_steps))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -315,8 +346,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "diff2d"], default=None,
+                    help="run a small case of one kernel for an ncu capture, then exit")
+    ap.add_argument("--profile-n", type=int, default=256)
+    ap.add_argument("--profile-steps", type=int, default=4)
+    ap.add_argument("--profile-tb", type=int, default=0)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_engine(args)
