@@ -186,3 +186,107 @@ extern "C" int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
     FM_TRY_CUDA(cudaMemcpyAsync(dens, src, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   return FM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// No-allocation variant.
+//
+// Some callers cannot call cudaMalloc: a host application that reserved its
+// whole device-memory budget up front and hands the library only its own
+// arrays, or a latency-critical loop that must not hit cudaMalloc's implicit
+// device-wide synchronization.  For them fm_diff2d_f64_forward_noalloc takes
+// only the state array; its ping-pong buffer and grid-barrier word live in
+// the file-scope device arrays below (8 MB + 256 B, held by every GPU that
+// loads this library until the process exits).
+namespace {
+
+constexpr size_t kNoAllocMaxCells = (size_t)FM_DIFF2D_NOALLOC_MAX_CELLS;
+static __device__ __align__(256) double g_noalloc_work[kNoAllocMaxCells];
+static __device__ __align__(256) GridSync g_noalloc_sync[1];
+
+struct NoAllocScratch {
+  double *work;
+  GridSync *sync;
+};
+
+std::mutex g_noalloc_mu;
+bool g_noalloc_ready[64] = {false};
+NoAllocScratch g_noalloc[64];
+
+// Device addresses of the scratch arrays for the current device.  In host
+// code g_noalloc_work names a host-side stand-in, not device memory, so the
+// address a kernel may use is looked up once per device (first call on that
+// device) with cudaGetSymbolAddress and cached.
+int noalloc_scratch(NoAllocScratch *out) {
+  int dev = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    fm::set_error("fm_diff2d_f64_forward_noalloc: device index %d not supported", dev);
+    return FM_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ready[dev]) {
+    NoAllocScratch s;
+    FM_TRY_CUDA(cudaGetSymbolAddress((void **)&s.work, g_noalloc_work));
+    FM_TRY_CUDA(cudaGetSymbolAddress((void **)&s.sync, g_noalloc_sync));
+    g_noalloc[dev] = s;
+    g_noalloc_ready[dev] = true;
+  }
+  *out = g_noalloc[dev];
+  return FM_OK;
+}
+
+}  // namespace
+
+extern "C" int fm_diff2d_f64_forward_noalloc(int nx, int ny, double *dens, double coef,
+                                             int steps, void *stream) {
+  FM_CHECK_ARG(dens, "fm_diff2d_f64_forward_noalloc: dens is NULL");
+  FM_CHECK_ARG(nx >= 1 && ny >= 32 && ny % 32 == 0,
+               "fm_diff2d_f64_forward_noalloc: need ny %% 32 == 0 (got %d x %d)", nx, ny);
+  FM_CHECK_ARG((size_t)nx * (size_t)ny <= kNoAllocMaxCells,
+               "fm_diff2d_f64_forward_noalloc: %d x %d = %zu cells exceeds the %zu-cell "
+               "static scratch (FM_DIFF2D_NOALLOC_MAX_CELLS); use fm_diff2d_f64_forward",
+               nx, ny, (size_t)nx * (size_t)ny, kNoAllocMaxCells);
+  FM_CHECK_ARG(steps >= 0, "fm_diff2d_f64_forward_noalloc: steps < 0");
+  if (steps == 0) return FM_OK;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  NoAllocScratch sc;
+  int st = noalloc_scratch(&sc);
+  if (st) return st;
+  int dev = 0, coop = 0, sms = 0, per_sm = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  FM_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) {
+    fm::set_error("fm_diff2d_f64_forward_noalloc: device has no cooperative launch");
+    return FM_ERR_UNSUPPORTED;
+  }
+  st = fm::device_sm_count(&sms);
+  if (st) return st;
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, diff2d_persistent, 256, 0));
+  if (per_sm < 1) {
+    fm::set_error("fm_diff2d_f64_forward_noalloc: kernel does not fit on an SM");
+    return FM_ERR_UNSUPPORTED;
+  }
+  const long long nseg = (long long)nx * (ny / 32);
+  const int grid = (int)std::max<long long>(
+      1, std::min<long long>((nseg + 7) / 8, (long long)sms * std::min(per_sm, 2)));
+  // The barrier word keeps the previous call's contents: it must start at zero.
+  FM_TRY_CUDA(cudaMemsetAsync(sc.sync, 0, sizeof(GridSync), s));
+  double *a = dens, *b = sc.work;
+  int nxv = nx, nyv = ny, stv = steps;
+  double cf = coef;
+  GridSync *gs = sc.sync;
+  void *args[] = {&a, &b, &nxv, &nyv, &cf, &stv, &gs};
+  FM_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)diff2d_persistent, dim3(grid), dim3(256),
+                                          args, 0, s));
+  GridSync host;
+  FM_TRY_CUDA(cudaMemcpyAsync(&host, sc.sync, sizeof(GridSync), cudaMemcpyDeviceToHost, s));
+  FM_TRY_CUDA(cudaStreamSynchronize(s));
+  if (host.err) {
+    fm::set_error("fm_diff2d_f64_forward_noalloc: grid barrier wait gave up");
+    return FM_ERR_TIMEOUT;
+  }
+  if (steps & 1)
+    FM_TRY_CUDA(cudaMemcpyAsync(dens, sc.work, (size_t)nx * ny * sizeof(double),
+                                cudaMemcpyDeviceToDevice, s));
+  return FM_OK;
+}

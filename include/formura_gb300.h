@@ -128,6 +128,31 @@ int fm_gs3d_f32k_forward(int nx, int ny, int nz, float *U, float *V, float *cU,
 int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
                           double coef, int steps, void *stream);
 
+/*
+ * fm_diff2d_f64_forward without any device allocation.  No counterpart in the
+ * reference (its generated C allocates nothing on a GPU).
+ *
+ * For callers that cannot call cudaMalloc: a host application that reserved
+ * its device-memory budget up front and passes only its own arrays, or a
+ * latency-critical loop that must not trigger cudaMalloc's implicit
+ * device-wide synchronization.  The caller passes only the state array; the
+ * ping-pong buffer and the grid-barrier word are a static device array of
+ * FM_DIFF2D_NOALLOC_MAX_CELLS doubles (8 MB) plus 256 bytes inside the
+ * library, which every GPU that loads the library holds until the process
+ * exits.  nx*ny above FM_DIFF2D_NOALLOC_MAX_CELLS returns FM_ERR_ARG.
+ *
+ * Same results, bit for bit, as fm_diff2d_f64_forward.  The first call on a
+ * device looks up the scratch's device address (cudaGetSymbolAddress), which
+ * may load the library's device code on that device; make that first call
+ * before any stream capture.  Every call shares the one scratch area, so
+ * calls whose work overlaps on the GPU (different streams, or different host
+ * threads, without ordering between them) race; the barrier word is cleared
+ * at the start of each call.  Synchronizes `stream` before returning.
+ */
+#define FM_DIFF2D_NOALLOC_MAX_CELLS (1 << 20)
+int fm_diff2d_f64_forward_noalloc(int nx, int ny, double *dens, double coef,
+                                  int steps, void *stream);
+
 /* ---- conserved totals ------------------------------------------------------ */
 
 /*
