@@ -317,6 +317,11 @@ def run_profile_case(args):
 
     torch.cuda.set_device(0)
     dev = torch.device("cuda:0")
+    from formura_gb300 import _lib
+
+    for kv in args.tune or []:
+        k, v = kv.split("=")
+        _lib.check(_lib.lib().fm_tune_set(k.encode(), int(v)), "fm_tune_set")
     n = args.profile_n
     if args.profile in ("gs3d_f64", "gs3d_f32k"):
         U0, V0 = inits.gray_scott_3d(n, n, n, seed=1)
@@ -351,6 +356,7 @@ def main():
     ap.add_argument("--profile-n", type=int, default=256)
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--profile-tb", type=int, default=0)
+    ap.add_argument("--tune", action="append", help="KEY=VALUE tuning knob (fm_tune_set)")
     args = ap.parse_args()
     if args.profile:
         run_profile_case(args)

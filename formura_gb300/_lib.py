@@ -57,6 +57,9 @@ SIGNATURES = {
     "fm_sum_f64_scratch_elems": (c_size_t, [c_int64]),
     "fm_sum_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f32_as_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fm_tune_set": (c_int, [ctypes.c_char_p, c_int]),
+    "fm_tune_get": (c_int, [ctypes.c_char_p, c_int]),
+    "fm_tune_clear": (c_int, []),
     "fm_probe_fma": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p]),
 }
 

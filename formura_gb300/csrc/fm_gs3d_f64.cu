@@ -4,44 +4,204 @@
 // The generated C evaluates, per cell, the whole U_next / V_next DAG with the
 // half-point differences recomputed at every use (Manifestation inlines the
 // delayed ddx node, src/Formura/OrthotopeMachine/Manifestation.hs:115-143).
-// A recomputed IEEE expression has the same value, so this kernel computes
-// each face flux (W[i+1]-W[i])/dx once and hands it to both cells that use it:
+// A recomputed IEEE expression has the same value, so these kernels compute
+// each face flux (W[i+1]-W[i])/dx once and hand it to both cells that use it:
 //   x (slowest axis): the CTA marches along x; the flux at x-1/2 is carried in
 //                     registers from the previous plane.
 //   y:                each thread owns RY consecutive y cells of one z column;
 //                     RY+1 fluxes serve RY cells.
 //   z (fastest axis): lanes of a warp are consecutive z; the flux at z+1/2 is
-//                     the next lane's z-1/2 flux (warp shuffle), lane 31
-//                     computes its own.
-// Divisions by dx use fm::div_const (correctly rounded, 1 DMUL + 2 DFMA).
-// On GB300 the FP64 pipe, not HBM, bounds this kernel (~70 FP64 instructions
-// per cell update against 32 B of compulsory traffic).
+//                     the next lane's z-1/2 flux (warp shuffle).  Lane 31 takes
+//                     it from the next warp through shared memory when the CTA
+//                     spans the whole periodic z row (gs3d_f64_row), or
+//                     computes it itself (gs3d_f64_tile, any nz).
+//
+// On GB300 the FP64 pipe (~1.7 lanes/clk/SM), not HBM, bounds these kernels:
+// the ~70 FP64 operations of one cell update take ~40x longer than moving its
+// 32 bytes.  Divisions by dx are the bulk of it; two exact methods exist:
+//   DIV = 0  fm::div_const   — Markstein: 1 DMUL + 2 DFMA
+//   DIV = 1  fm::div_const_i — 1 DMUL, then the rounding decided with 128-bit
+//                              integer products on the integer pipe (default:
+//                              10.9 GLUP/s at 256^3 against 6.2 for DIV = 0)
+//   DIV = 2  fm::div_const_r — 1 DMUL + 1 DFMA (exact residual), rounding
+//                              decided by integer compares of bit patterns.
+// The integer parts read doubles only through __double2hiint/__double2loint:
+// a 64-bit mask of a double's bit pattern is otherwise turned back into an
+// FP64 abs by the compiler, which costs as much as the DFMA it replaced.
 #include <algorithm>
+#include <cstdlib>
 
 #include "fm_common.cuh"
+#include "fm_tune.h"
 
 namespace {
 
-using fm::div_const;
-
 struct Gs64 {
-  double F, Fk, Du, Dv, dt, dx, rdx;
+  double F, Fk, Du, Dv, dt;
+  fm::DivConst dx;
 };
 
-constexpr int kWarps = 4;  // warps per CTA, stacked along y
-constexpr int kRY = 4;     // y cells per thread
-constexpr int kTY = kWarps * kRY;
+template <int DIV>
+__device__ __forceinline__ double ddx(double x, const Gs64 &c) {
+  if (DIV == 0) return fm::div_const(x, c.dx.d, c.dx.r);
+  if (DIV == 2) return fm::div_const_r(x, c.dx.d, c.dx.r);
+  return fm::div_const_i(x, c.dx);
+}
 
-__global__ void __launch_bounds__(kWarps * 32)
-    gs3d_f64_step(const double *__restrict__ U, const double *__restrict__ V,
-                  double *__restrict__ Un, double *__restrict__ Vn, int nx,
-                  int ny, int nz, int xchunk, int ntiles_yz, int ntiles,
-                  Gs64 c) {
+constexpr int kRY = 4;  // y cells per thread
+
+// One cell's update from its fluxes (the U_next and V_next nodes).
+template <int DIV>
+__device__ __forceinline__ void gs_cell(double u, double v, double fxu_m, double fxu_p,
+                                        double fyu_m, double fyu_p, double fzu_m,
+                                        double fzu_p, double fxv_m, double fxv_p,
+                                        double fyv_m, double fyv_p, double fzv_m,
+                                        double fzv_p, const Gs64 &c, double &un,
+                                        double &vn) {
+  // U_next: U + dt*(((-(U*V*V)) + F*(1-U)) + Du*((lx + ly) + lz))
+  const double a_1 = u * v;
+  const double a_2 = a_1 * v;
+  const double a_3 = -a_2;
+  const double a_5 = 1.0 - u;
+  const double a_6 = c.F * a_5;
+  const double a_7 = a_3 + a_6;
+  const double lx = ddx<DIV>(fxu_p - fxu_m, c);
+  const double ly = ddx<DIV>(fyu_p - fyu_m, c);
+  const double lz = ddx<DIV>(fzu_p - fzu_m, c);
+  const double a_l = (lx + ly) + lz;
+  const double dU = a_7 + c.Du * a_l;
+  un = u + c.dt * dU;
+  // V_next: V + dt*(((U*V*V) - (F+k)*V) + Dv*((mx + my) + mz))
+  const double b_6 = a_2 - c.Fk * v;
+  const double mx = ddx<DIV>(fxv_p - fxv_m, c);
+  const double my = ddx<DIV>(fyv_p - fyv_m, c);
+  const double mz = ddx<DIV>(fzv_p - fzv_m, c);
+  const double b_l = (mx + my) + mz;
+  const double dV = b_6 + c.Dv * b_l;
+  vn = v + c.dt * dV;
+}
+
+// ---------------------------------------------------------------------------
+// gs3d_f64_row: CTA = nz threads (nz/32 warps along z, nz <= 256), each thread
+// kRY y cells; the CTA covers a full periodic z row, so no flux is computed
+// twice along z.  Tiles: (ny/kRY) y blocks x ceil(nx/xchunk) x chunks.
+template <int DIV>
+__global__ void __launch_bounds__(256)
+    gs3d_f64_row(const double *__restrict__ U, const double *__restrict__ V,
+                 double *__restrict__ Un, double *__restrict__ Vn, int nx, int ny, int nz,
+                 int xchunk, int ntiles, Gs64 c) {
+  // [buffer][field][j][warp] lane-0 z fluxes, double-buffered by plane parity
+  __shared__ double s_fz[2][2][kRY][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int wz = blockDim.x >> 5;
+  const int wn = (w + 1 == wz) ? 0 : w + 1;
+  const int z = threadIdx.x;
+  const int zm = fm::wrap_dn(z, nz);
+  const int nyt = ny / kRY;
+  const size_t sx = (size_t)ny * nz;
+  int buf = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int y0 = (t % nyt) * kRY;
+    const int x0 = (t / nyt) * xchunk;
+    const int x1 = min(x0 + xchunk, nx);
+    int off[kRY];
+#pragma unroll
+    for (int j = 0; j < kRY; ++j) off[j] = (y0 + j) * nz + z;
+    const int off_ym = fm::wrap_dn(y0, ny) * nz + z;
+    const int off_yp = fm::wrap_up(y0 + kRY - 1, ny) * nz + z;
+    double uc[kRY], vc[kRY], fxu[kRY], fxv[kRY];
+    {
+      const size_t pm = (size_t)fm::wrap_dn(x0, nx) * sx, pc = (size_t)x0 * sx;
+#pragma unroll
+      for (int j = 0; j < kRY; ++j) {
+        const double um = __ldg(U + pm + off[j]), vm = __ldg(V + pm + off[j]);
+        uc[j] = __ldg(U + pc + off[j]);
+        vc[j] = __ldg(V + pc + off[j]);
+        fxu[j] = ddx<DIV>(uc[j] - um, c);
+        fxv[j] = ddx<DIV>(vc[j] - vm, c);
+      }
+    }
+    for (int x = x0; x < x1; ++x) {
+      const size_t pc = (size_t)x * sx;
+      const size_t pp = (size_t)fm::wrap_up(x, nx) * sx;
+      double up[kRY], vp[kRY];
+#pragma unroll
+      for (int j = 0; j < kRY; ++j) {
+        up[j] = __ldg(U + pp + off[j]);
+        vp[j] = __ldg(V + pp + off[j]);
+      }
+      // z fluxes at z-1/2
+      double fzu[kRY], fzv[kRY];
+#pragma unroll
+      for (int j = 0; j < kRY; ++j) {
+        double uzm = __shfl_up_sync(0xffffffffu, uc[j], 1);
+        double vzm = __shfl_up_sync(0xffffffffu, vc[j], 1);
+        if (lane == 0) {
+          uzm = __ldg(U + pc + (size_t)(y0 + j) * nz + zm);
+          vzm = __ldg(V + pc + (size_t)(y0 + j) * nz + zm);
+        }
+        fzu[j] = ddx<DIV>(uc[j] - uzm, c);
+        fzv[j] = ddx<DIV>(vc[j] - vzm, c);
+        if (lane == 0) {
+          s_fz[buf][0][j][w] = fzu[j];
+          s_fz[buf][1][j][w] = fzv[j];
+        }
+      }
+      // y fluxes: fy[j] at y0+j-1/2, j = 0..RY
+      double fyu[kRY + 1], fyv[kRY + 1];
+      {
+        const double um = __ldg(U + pc + off_ym), vm = __ldg(V + pc + off_ym);
+        const double upp = __ldg(U + pc + off_yp), vpp = __ldg(V + pc + off_yp);
+        fyu[0] = ddx<DIV>(uc[0] - um, c);
+        fyv[0] = ddx<DIV>(vc[0] - vm, c);
+#pragma unroll
+        for (int j = 1; j < kRY; ++j) {
+          fyu[j] = ddx<DIV>(uc[j] - uc[j - 1], c);
+          fyv[j] = ddx<DIV>(vc[j] - vc[j - 1], c);
+        }
+        fyu[kRY] = ddx<DIV>(upp - uc[kRY - 1], c);
+        fyv[kRY] = ddx<DIV>(vpp - vc[kRY - 1], c);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < kRY; ++j) {
+        double fzu_p = __shfl_down_sync(0xffffffffu, fzu[j], 1);
+        double fzv_p = __shfl_down_sync(0xffffffffu, fzv[j], 1);
+        if (lane == 31) {
+          fzu_p = s_fz[buf][0][j][wn];
+          fzv_p = s_fz[buf][1][j][wn];
+        }
+        const double fxu_p = ddx<DIV>(up[j] - uc[j], c);
+        const double fxv_p = ddx<DIV>(vp[j] - vc[j], c);
+        double un, vn;
+        gs_cell<DIV>(uc[j], vc[j], fxu[j], fxu_p, fyu[j], fyu[j + 1], fzu[j], fzu_p, fxv[j],
+                     fxv_p, fyv[j], fyv[j + 1], fzv[j], fzv_p, c, un, vn);
+        Un[pc + off[j]] = un;
+        Vn[pc + off[j]] = vn;
+        fxu[j] = fxu_p;
+        fxv[j] = fxv_p;
+        uc[j] = up[j];
+        vc[j] = vp[j];
+      }
+      buf ^= 1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// gs3d_f64_tile: any nz % 32 == 0.  CTA = 4 warps stacked along y, lanes along
+// z; lane 31 computes its own z+1/2 flux.
+constexpr int kTileWarps = 4;
+constexpr int kTY = kTileWarps * kRY;
+
+template <int DIV>
+__global__ void __launch_bounds__(kTileWarps * 32)
+    gs3d_f64_tile(const double *__restrict__ U, const double *__restrict__ V,
+                  double *__restrict__ Un, double *__restrict__ Vn, int nx, int ny, int nz,
+                  int xchunk, int ntiles_yz, int ntiles, Gs64 c) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nzt = nz >> 5;
   const size_t sx = (size_t)ny * nz;
-  const double dx = c.dx, rdx = c.rdx;
-
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int tyz = t % ntiles_yz;
     const int tx = t / ntiles_yz;
@@ -55,7 +215,6 @@ __global__ void __launch_bounds__(kWarps * 32)
     for (int j = 0; j < kRY; ++j) off[j] = (y0 + j) * nz + z;
     const int off_ym = fm::wrap_dn(y0, ny) * nz + z;
     const int off_yp = fm::wrap_up(y0 + kRY - 1, ny) * nz + z;
-
     double uc[kRY], vc[kRY], fxu[kRY], fxv[kRY];
     {
       const size_t pm = (size_t)fm::wrap_dn(x0, nx) * sx, pc = (size_t)x0 * sx;
@@ -64,11 +223,10 @@ __global__ void __launch_bounds__(kWarps * 32)
         const double um = __ldg(U + pm + off[j]), vm = __ldg(V + pm + off[j]);
         uc[j] = __ldg(U + pc + off[j]);
         vc[j] = __ldg(V + pc + off[j]);
-        fxu[j] = div_const(uc[j] - um, dx, rdx);
-        fxv[j] = div_const(vc[j] - vm, dx, rdx);
+        fxu[j] = ddx<DIV>(uc[j] - um, c);
+        fxv[j] = ddx<DIV>(vc[j] - vm, c);
       }
     }
-
     for (int x = x0; x < x1; ++x) {
       const size_t pc = (size_t)x * sx;
       const size_t pp = (size_t)fm::wrap_up(x, nx) * sx;
@@ -78,67 +236,44 @@ __global__ void __launch_bounds__(kWarps * 32)
         up[j] = __ldg(U + pp + off[j]);
         vp[j] = __ldg(V + pp + off[j]);
       }
-      // y fluxes: fy[j] is the flux at y0+j-1/2, j = 0..RY.
       double fyu[kRY + 1], fyv[kRY + 1];
       {
         const double um = __ldg(U + pc + off_ym), vm = __ldg(V + pc + off_ym);
         const double upp = __ldg(U + pc + off_yp), vpp = __ldg(V + pc + off_yp);
-        fyu[0] = div_const(uc[0] - um, dx, rdx);
-        fyv[0] = div_const(vc[0] - vm, dx, rdx);
+        fyu[0] = ddx<DIV>(uc[0] - um, c);
+        fyv[0] = ddx<DIV>(vc[0] - vm, c);
 #pragma unroll
         for (int j = 1; j < kRY; ++j) {
-          fyu[j] = div_const(uc[j] - uc[j - 1], dx, rdx);
-          fyv[j] = div_const(vc[j] - vc[j - 1], dx, rdx);
+          fyu[j] = ddx<DIV>(uc[j] - uc[j - 1], c);
+          fyv[j] = ddx<DIV>(vc[j] - vc[j - 1], c);
         }
-        fyu[kRY] = div_const(upp - uc[kRY - 1], dx, rdx);
-        fyv[kRY] = div_const(vpp - vc[kRY - 1], dx, rdx);
+        fyu[kRY] = ddx<DIV>(upp - uc[kRY - 1], c);
+        fyv[kRY] = ddx<DIV>(vpp - vc[kRY - 1], c);
       }
 #pragma unroll
       for (int j = 0; j < kRY; ++j) {
         const double u = uc[j], v = vc[j];
-        // z fluxes at z-1/2 (this lane) and z+1/2 (next lane, or own for lane 31)
         double uzm = __shfl_up_sync(0xffffffffu, u, 1);
         double vzm = __shfl_up_sync(0xffffffffu, v, 1);
         if (lane == 0) {
           uzm = __ldg(U + pc + (size_t)(y0 + j) * nz + zm);
           vzm = __ldg(V + pc + (size_t)(y0 + j) * nz + zm);
         }
-        const double fzu_m = div_const(u - uzm, dx, rdx);
-        const double fzv_m = div_const(v - vzm, dx, rdx);
+        const double fzu_m = ddx<DIV>(u - uzm, c);
+        const double fzv_m = ddx<DIV>(v - vzm, c);
         double fzu_p = __shfl_down_sync(0xffffffffu, fzu_m, 1);
         double fzv_p = __shfl_down_sync(0xffffffffu, fzv_m, 1);
         if (lane == 31) {
-          const double uzp = __ldg(U + pc + (size_t)(y0 + j) * nz + zp);
-          const double vzp = __ldg(V + pc + (size_t)(y0 + j) * nz + zp);
-          fzu_p = div_const(uzp - u, dx, rdx);
-          fzv_p = div_const(vzp - v, dx, rdx);
+          fzu_p = ddx<DIV>(__ldg(U + pc + (size_t)(y0 + j) * nz + zp) - u, c);
+          fzv_p = ddx<DIV>(__ldg(V + pc + (size_t)(y0 + j) * nz + zp) - v, c);
         }
-        const double fxu_p = div_const(up[j] - u, dx, rdx);
-        const double fxv_p = div_const(vp[j] - v, dx, rdx);
-
-        // U_next: U + dt*(((-(U*V*V)) + F*(1-U)) + Du*((lx + ly) + lz))
-        const double a_1 = u * v;
-        const double a_2 = a_1 * v;
-        const double a_3 = -a_2;
-        const double a_5 = 1.0 - u;
-        const double a_6 = c.F * a_5;
-        const double a_7 = a_3 + a_6;
-        const double lx = div_const(fxu_p - fxu[j], dx, rdx);
-        const double ly = div_const(fyu[j + 1] - fyu[j], dx, rdx);
-        const double lz = div_const(fzu_p - fzu_m, dx, rdx);
-        const double a_l = (lx + ly) + lz;
-        const double dU = a_7 + c.Du * a_l;
-        Un[pc + off[j]] = u + c.dt * dU;
-
-        // V_next: V + dt*(((U*V*V) - (F+k)*V) + Dv*((mx + my) + mz))
-        const double b_6 = a_2 - c.Fk * v;
-        const double mx = div_const(fxv_p - fxv[j], dx, rdx);
-        const double my = div_const(fyv[j + 1] - fyv[j], dx, rdx);
-        const double mz = div_const(fzv_p - fzv_m, dx, rdx);
-        const double b_l = (mx + my) + mz;
-        const double dV = b_6 + c.Dv * b_l;
-        Vn[pc + off[j]] = v + c.dt * dV;
-
+        const double fxu_p = ddx<DIV>(up[j] - u, c);
+        const double fxv_p = ddx<DIV>(vp[j] - v, c);
+        double un, vn;
+        gs_cell<DIV>(u, v, fxu[j], fxu_p, fyu[j], fyu[j + 1], fzu_m, fzu_p, fxv[j], fxv_p,
+                     fyv[j], fyv[j + 1], fzv_m, fzv_p, c, un, vn);
+        Un[pc + off[j]] = un;
+        Vn[pc + off[j]] = vn;
         fxu[j] = fxu_p;
         fxv[j] = fxv_p;
         uc[j] = up[j];
@@ -149,25 +284,29 @@ __global__ void __launch_bounds__(kWarps * 32)
 }
 
 struct LaunchPlan {
-  int xchunk, ntiles_yz, ntiles, grid;
+  bool row;
+  int div, threads, xchunk, ntiles_yz, ntiles, grid;
 };
 
-int plan_launch(int nx, int ny, int nz, LaunchPlan *lp) {
+template <typename K>
+int resident_blocks(K kernel, int threads, int *out) {
   int sms = 0;
   int st = fm::device_sm_count(&sms);
   if (st) return st;
   int per_sm = 0;
-  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs3d_f64_step,
-                                                             kWarps * 32, 0));
-  if (per_sm < 1) per_sm = 1;
-  const int resident = sms * per_sm;
-  const int ntiles_yz = (nz / 32) * (ny / kTY);
-  // Pick the x chunk that minimises waves x (chunk + warm-up plane cost).
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0));
+  *out = sms * std::max(per_sm, 1);
+  return FM_OK;
+}
+
+// Smallest (waves x (chunk + warm-up cost)) over candidate x chunks.
+int pick_xchunk(int nx, long long tiles_per_chunk_row, int resident, int forced) {
+  if (forced > 0) return std::min(forced, nx);
   double best = 1e300;
   int best_xc = 1;
-  for (int xc : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32}) {
+  for (int xc : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64}) {
     if (xc > nx) break;
-    const long long nt = (long long)ntiles_yz * ((nx + xc - 1) / xc);
+    const long long nt = tiles_per_chunk_row * ((nx + xc - 1) / xc);
     const long long waves = (nt + resident - 1) / resident;
     const double cost = (double)waves * (xc + 0.35);
     if (cost < best - 1e-9) {
@@ -175,11 +314,63 @@ int plan_launch(int nx, int ny, int nz, LaunchPlan *lp) {
       best_xc = xc;
     }
   }
-  lp->xchunk = best_xc;
-  lp->ntiles_yz = ntiles_yz;
-  lp->ntiles = ntiles_yz * ((nx + best_xc - 1) / best_xc);
+  return best_xc;
+}
+
+int plan_launch(int nx, int ny, int nz, double dx, LaunchPlan *lp) {
+  const int kind = fm::tune_get("gs3d_f64.kernel", 0);  // 0 auto, 1 tile, 2 row
+  lp->div = fm::tune_get("gs3d_f64.div", 1);
+  if (lp->div < 0 || lp->div > 2) lp->div = 1;
+  if (lp->div == 2 && !(dx >= 0x1p-20 && dx <= 0x1p20)) lp->div = 0;
+  const bool row_ok = nz <= 256 && ny % kRY == 0;
+  lp->row = (kind == 2 || kind == 0) && row_ok;
+  if (kind == 1 || ny % kTY != 0) lp->row = false;
+  if (!lp->row && ny % kTY != 0) {
+    fm::set_error("fm_gs3d_f64_forward: ny must be a multiple of %d for nz > 256", kTY);
+    return FM_ERR_UNSUPPORTED;
+  }
+  int resident = 0, st;
+  const int forced = fm::tune_get("gs3d_f64.xchunk", 0);
+  if (lp->row) {
+    lp->threads = nz;
+    st = lp->div == 2 ? resident_blocks(gs3d_f64_row<2>, nz, &resident)
+         : lp->div == 1 ? resident_blocks(gs3d_f64_row<1>, nz, &resident)
+                        : resident_blocks(gs3d_f64_row<0>, nz, &resident);
+    if (st) return st;
+    lp->ntiles_yz = ny / kRY;
+  } else {
+    lp->threads = kTileWarps * 32;
+    st = lp->div == 2 ? resident_blocks(gs3d_f64_tile<2>, lp->threads, &resident)
+         : lp->div == 1 ? resident_blocks(gs3d_f64_tile<1>, lp->threads, &resident)
+                        : resident_blocks(gs3d_f64_tile<0>, lp->threads, &resident);
+    if (st) return st;
+    lp->ntiles_yz = (nz / 32) * (ny / kTY);
+  }
+  lp->xchunk = pick_xchunk(nx, lp->ntiles_yz, resident, forced);
+  lp->ntiles = lp->ntiles_yz * ((nx + lp->xchunk - 1) / lp->xchunk);
   lp->grid = std::min(lp->ntiles, resident);
   return FM_OK;
+}
+
+template <int DIV>
+void launch_div(const LaunchPlan &lp, cudaStream_t s, const double *u, const double *v,
+                double *un, double *vn, int nx, int ny, int nz, const Gs64 &c) {
+  if (lp.row)
+    gs3d_f64_row<DIV><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz, lp.xchunk,
+                                                     lp.ntiles, c);
+  else
+    gs3d_f64_tile<DIV><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz, lp.xchunk,
+                                                      lp.ntiles_yz, lp.ntiles, c);
+}
+
+void launch(const LaunchPlan &lp, cudaStream_t s, const double *u, const double *v, double *un,
+            double *vn, int nx, int ny, int nz, const Gs64 &c) {
+  if (lp.div == 2)
+    launch_div<2>(lp, s, u, v, un, vn, nx, ny, nz, c);
+  else if (lp.div == 1)
+    launch_div<1>(lp, s, u, v, un, vn, nx, ny, nz, c);
+  else
+    launch_div<0>(lp, s, u, v, un, vn, nx, ny, nz, c);
 }
 
 }  // namespace
@@ -199,7 +390,7 @@ extern "C" int fm_gs3d_f64_forward(int nx, int ny, int nz, double *U, double *V,
   if (steps == 0) return FM_OK;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   LaunchPlan lp;
-  int st = plan_launch(nx, ny, nz, &lp);
+  int st = plan_launch(nx, ny, nz, p->dx, &lp);
   if (st) return st;
   Gs64 c;
   c.F = p->F;
@@ -207,12 +398,10 @@ extern "C" int fm_gs3d_f64_forward(int nx, int ny, int nz, double *U, double *V,
   c.Du = p->Du;
   c.Dv = p->Dv;
   c.dt = p->dt;
-  c.dx = p->dx;
-  c.rdx = 1.0 / p->dx;
+  c.dx = fm::make_div_const(p->dx);
   double *cu = U, *cv = V, *nu = work_U, *nv = work_V;
   for (int i = 0; i < steps; ++i) {
-    gs3d_f64_step<<<lp.grid, kWarps * 32, 0, s>>>(cu, cv, nu, nv, nx, ny, nz, lp.xchunk,
-                                                 lp.ntiles_yz, lp.ntiles, c);
+    launch(lp, s, cu, cv, nu, nv, nx, ny, nz, c);
     std::swap(cu, nu);
     std::swap(cv, nv);
   }

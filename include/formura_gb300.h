@@ -169,6 +169,24 @@ int fm_sum_f64(int64_t n, const double *a, double *partials, double *out_device,
 int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
                       double *out_device, void *stream);
 
+/* ---- tuning ------------------------------------------------------------------ */
+
+/*
+ * Process-wide tuning knobs.  Every knob has an automatic default; a set value
+ * overrides it for later calls.  No knob changes results (all variants of a
+ * kernel are bit-exact with each other).  Known keys:
+ *   "gs3d_f64.kernel"  0 auto, 1 tile kernel (any nz), 2 full-z-row kernel (nz <= 256)
+ *   "gs3d_f64.div"     0 Markstein division (3 FP64 ops), 1 integer-corrected (1 FP64 op +
+ *                      128-bit integer products; default), 2 residual + integer compare
+ *                      (2 FP64 ops)
+ *   "gs3d_f64.xchunk"  x planes per CTA tile (0 = automatic)
+ *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_forward
+ * fm_tune_clear() restores every default.
+ */
+int fm_tune_set(const char *key, int value);
+int fm_tune_get(const char *key, int fallback);
+int fm_tune_clear(void);
+
 /* ---- measurement ------------------------------------------------------------ */
 
 /*

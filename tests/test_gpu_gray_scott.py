@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 import torch
 
-from formura_gb300 import backend, inits, kernels
+from formura_gb300 import _lib, backend, inits, kernels
 from formura_gb300.runtime import FormuraProgram
 from oracle import oracle
 
@@ -34,6 +34,23 @@ def test_gs3d_f64_bit_exact(cuda_device, shape, steps):
     U, V = run_f64(U0, V0, steps, cuda_device)
     Uo, Vo = oracle.gs3d_f64(U0, V0, steps, **GS)
     assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
+
+
+@pytest.mark.parametrize("kernel,div,xchunk", [(1, 0, 0), (1, 1, 0), (1, 2, 0), (2, 0, 0),
+                                               (2, 1, 0), (2, 2, 0), (2, 2, 3), (1, 2, 5)])
+def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, xchunk):
+    lib = _lib.lib()
+    try:
+        lib.fm_tune_set(b"gs3d_f64.kernel", kernel)
+        lib.fm_tune_set(b"gs3d_f64.div", div)
+        lib.fm_tune_set(b"gs3d_f64.xchunk", xchunk)
+        for shape, steps in (((24, 32, 64), 9), ((9, 16, 256), 4), ((5, 48, 32), 3)):
+            U0, V0 = inits.gray_scott_3d(*shape, seed=31, ncubes=3, side=8)
+            U, V = run_f64(U0, V0, steps, cuda_device)
+            Uo, Vo = oracle.gs3d_f64(U0, V0, steps, **GS)
+            assert np.array_equal(U, Uo) and np.array_equal(V, Vo), (shape, kernel, div)
+    finally:
+        lib.fm_tune_clear()
 
 
 def test_gs3d_f64_bit_exact_other_constants(cuda_device):
