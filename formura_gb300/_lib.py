@@ -51,7 +51,10 @@ SIGNATURES = {
     "fm_gs3d_f64_forward": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                     ctypes.POINTER(GsParams), c_int, c_void_p]),
     "fm_gs3d_f32k_forward": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
-                                     c_void_p, c_int, c_int, ctypes.POINTER(GsParams), c_void_p]),
+                                     c_void_p, c_int, ctypes.POINTER(GsParams), c_void_p]),
+    "fm_gs3d_f32k_tb_forward": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p, c_int, c_int,
+                                        ctypes.POINTER(GsParams), c_void_p]),
     "fm_diff2d_f64_forward": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, c_int, c_void_p]),
     "fm_diff2d_f64_forward_noalloc": (c_int, [c_int, c_int, c_void_p, c_double, c_int, c_void_p]),
     "fm_sum_f64_scratch_elems": (c_size_t, [c_int64]),

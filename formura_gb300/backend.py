@@ -52,7 +52,9 @@ class Program:
 
     ``form`` names the kernel family that evaluates the program's ``step``:
       * ``gs3d_f64``   — examples/pearson-3d.fmr form, double
-      * ``gs3d_f32k``  — the same form in float with Kahan time accumulation
+      * ``gs3d_f32k``  — the same DAG in float with Kahan time accumulation
+      * ``gs3d_f32k_tb`` — the float fast form with Kahan accumulation,
+        temporally blocked (``temporal_blocking_interval`` > 1 -> depth <= 4)
       * ``diff2d_f64`` — examples/diffusion.fmr form in 2D, double
     ``constants`` are the .fmr constants of ``step`` (F, k, Du, Dv, dt, dx /
     Dt, Dx).  ``intra_node_shape``, ``mpi_grid_shape``, ``monitor_interval``
@@ -91,7 +93,7 @@ class Program:
 
     @property
     def elem(self) -> str:
-        return "float" if self.form.endswith("f32k") else "double"
+        return "float" if "f32" in self.form else "double"
 
     @property
     def state_names(self) -> List[str]:
@@ -100,7 +102,7 @@ class Program:
     @property
     def extra_state_names(self) -> List[str]:
         # Kahan compensation arrays carried between calls.
-        return ["U_compensation", "V_compensation"] if self.form.endswith("f32k") else []
+        return ["U_compensation", "V_compensation"] if "f32k" in self.form else []
 
     def validate(self) -> None:
         if self.mpi_grid_shape and any(int(m) != 1 for m in self.mpi_grid_shape):
@@ -123,6 +125,7 @@ class Program:
 FORMS = {
     "gs3d_f64": {"dim": 3, "constants": ("F", "k", "Du", "Dv", "dt", "dx")},
     "gs3d_f32k": {"dim": 3, "constants": ("F", "k", "Du", "Dv", "dt", "dx")},
+    "gs3d_f32k_tb": {"dim": 3, "constants": ("F", "k", "Du", "Dv", "dt", "dx")},
     "diff2d_f64": {"dim": 2, "constants": ("Dt", "Dx")},
 }
 
@@ -202,10 +205,20 @@ def _forward_call(p: Program) -> str:
         return (
             "fm_gs_params prm = {%s, %s, %s, %s, %s, %s};\n"
             "  return fm_gs3d_f32k_forward(%d, %d, %d, (float*)g_dev[0], (float*)g_dev[1],"
+            " (float*)g_dev[2], (float*)g_dev[3], (float*)g_work, steps, &prm, g_stream);"
+            % (_c_double(c["F"]), _c_double(c["k"]), _c_double(c["Du"]), _c_double(c["Dv"]),
+               _c_double(c["dt"]), _c_double(c["dx"]), nx[0], nx[1], nx[2]))
+    if p.form == "gs3d_f32k_tb":
+        # depth per HBM pass: the kernel's tuned default (0) unless the YAML asks
+        # for something smaller than the on-chip maximum of 4
+        tb = int(p.temporal_blocking_interval)
+        tb = tb if 1 <= tb < 4 else 0
+        return (
+            "fm_gs_params prm = {%s, %s, %s, %s, %s, %s};\n"
+            "  return fm_gs3d_f32k_tb_forward(%d, %d, %d, (float*)g_dev[0], (float*)g_dev[1],"
             " (float*)g_dev[2], (float*)g_dev[3], (float*)g_work, steps, %d, &prm, g_stream);"
             % (_c_double(c["F"]), _c_double(c["k"]), _c_double(c["Du"]), _c_double(c["Dv"]),
-               _c_double(c["dt"]), _c_double(c["dx"]), nx[0], nx[1], nx[2],
-               int(p.temporal_blocking_interval)))
+               _c_double(c["dt"]), _c_double(c["dx"]), nx[0], nx[1], nx[2], tb))
     if p.form == "diff2d_f64":
         # node pair pow(Dx,2) then Dt/that, evaluated in double by host libm as the
         # generated C does (`**` -> pow, Translate.hs:594)
@@ -219,7 +232,7 @@ def _forward_call(p: Program) -> str:
 def _work_elems(p: Program) -> str:
     if p.form == "gs3d_f64":
         return "2 * NCELLS"
-    if p.form == "gs3d_f32k":
+    if p.form in ("gs3d_f32k", "gs3d_f32k_tb"):
         return "4 * NCELLS"
     return "NCELLS"
 

@@ -7,17 +7,9 @@
 // so that the O(1e-7) rounding of each increment does not pile up over
 // thousands of steps.  State per cell: U, V, cU, cV (16 B).
 //
-// Two kernels:
-//  * gs3d_f32k_step: one step per launch (tb = 1), x-marching with register
-//    blocking along y and shuffles along z, like the FP64 kernel.
-//  * gs3d_f32k_tb:   temporal blocking — TB steps per HBM round trip.  A CTA
-//    owns a (y,z) tile plus a TB-cell halo and streams it along x.  Each
-//    time level s = 1..TB is a pipeline stage that lags the previous one by
-//    one plane; the three most recent planes of every level stay in shared
-//    memory (a ring), so a plane is read from HBM once and written once per
-//    TB steps.  The valid region shrinks by one cell per level (the trapezoid
-//    of Formura's skewed regions, src/Formura/MPICxx/Cut.hs:240-281, turned
-//    into a per-CTA overlapped tile).
+// One step per launch, x-marching with register blocking along y and
+// shuffles along z, like the FP64 kernel.  The temporally blocked kernel of
+// the binary32 fast form is in fm_gs3d_f32k_tb.cu.
 #include <algorithm>
 
 #include "fm_common.cuh"
@@ -178,18 +170,17 @@ int plan_step(int nx, int ny, int nz, int *xchunk, int *ntiles_yz, int *ntiles, 
 }  // namespace
 
 extern "C" int fm_gs3d_f32k_forward(int nx, int ny, int nz, float *U, float *V, float *cU,
-                                    float *cV, float *work, int steps, int tb,
-                                    const fm_gs_params *p, void *stream) {
+                                    float *cV, float *work, int steps, const fm_gs_params *p,
+                                    void *stream) {
   FM_CHECK_ARG(p && U && V && cU && cV && work, "fm_gs3d_f32k_forward: NULL argument");
   FM_CHECK_ARG(nx >= 1 && nz >= 32 && nz % 32 == 0 && ny >= kTY && ny % kTY == 0,
                "fm_gs3d_f32k_forward: need nz %% 32 == 0 and ny %% %d == 0 (got %d,%d,%d)",
                kTY, nx, ny, nz);
   FM_CHECK_ARG((long long)ny * nz < (1ll << 31), "fm_gs3d_f32k_forward: plane too large");
-  FM_CHECK_ARG(steps >= 0 && tb >= 0, "fm_gs3d_f32k_forward: negative steps or tb");
+  FM_CHECK_ARG(steps >= 0, "fm_gs3d_f32k_forward: steps < 0");
   const float dxf = (float)p->dx;
   FM_CHECK_ARG(dxf >= 0x1p-20f && dxf <= 0x1p20f,
                "fm_gs3d_f32k_forward: dx outside [2^-20, 2^20]");
-  (void)tb;
   if (steps == 0) return FM_OK;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   Gs32 c;

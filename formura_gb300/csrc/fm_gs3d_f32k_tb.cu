@@ -1,0 +1,290 @@
+// fm_gs3d_f32k_tb.cu — 3D Gray-Scott, binary32 + Kahan time accumulation,
+// temporally blocked: T time steps per HBM round trip.
+//
+// Formura's temporal blocking unrolls the step graph T times
+// (src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134) and runs it over
+// skewed space-time regions whose walls move with the stencil reach
+// (src/Formura/MPICxx/Cut.hs:240-281) so that a region's intermediate time
+// levels stay in cache.  Here the same idea is an overlapped tile streamed
+// along x:
+//
+//  * A CTA of 32x32 threads owns an input column tile of 32 (y) x 32 (z)
+//    cells (periodic wrap) whose inner (32-2T)^2 cells are written back.
+//  * It marches along x.  At iteration i it loads plane i (level 0) and each
+//    level s = 1..T advances plane i-s by one step, from level s-1's planes
+//    i-s-1, i-s, i-s+1.  The x neighbours come from a 3-plane register
+//    window per level, the z neighbours from the neighbouring lanes
+//    (shuffles; a warp is one y row), the y neighbours from a shared-memory
+//    copy of level s-1's plane i-s written by the rows above and below in the
+//    previous iteration (double-buffered by parity: ONE __syncthreads per
+//    plane for all T levels).  Level s is valid on rows/lanes [s, 32-s); the
+//    rows outside skip the level.
+//  * The Kahan compensation of each level lives in registers of the thread
+//    that owns the cell (a cell's compensation is never read by a neighbour).
+//
+// HBM traffic per cell and pass: U,V,cU,cV in (16 B, plus the halo re-read
+// when it misses L2) and out (16 B), i.e. ~32/T B per lattice update.
+//
+// Arithmetic: the binary32 fast form of the Gray-Scott step (oracle
+// fo_gs3d_run_f32k_fast) — differences summed per axis, explicit FMAs — so
+// every T gives bit-identical results.
+#include <algorithm>
+
+#include "fm_common.cuh"
+#include "fm_tune.h"
+
+namespace {
+
+constexpr int kE = 32;  // tile edge (threads per row = rows per CTA)
+
+struct Gs32f {
+  float F, Fk, cu, cv, dt;
+};
+
+__device__ __forceinline__ int wrap_any(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// One fast-form step of a cell.
+__device__ __forceinline__ void cell_step(float u, float v, float lu, float lv, float cu_in,
+                                          float cv_in, const Gs32f &c, float &un, float &vn,
+                                          float &cun, float &cvn) {
+  const float uvv = (u * v) * v;
+  const float dU = fmaf(c.cu, lu, fmaf(c.F, 1.0f - u, -uvv));
+  const float dV = fmaf(c.cv, lv, fmaf(-c.Fk, v, uvv));
+  const float yu = fmaf(c.dt, dU, -cu_in);
+  const float tu = u + yu;
+  cun = (tu - u) - yu;
+  un = tu;
+  const float yv = fmaf(c.dt, dV, -cv_in);
+  const float tv = v + yv;
+  cvn = (tv - v) - yv;
+  vn = tv;
+}
+
+template <int T>
+__global__ void __launch_bounds__(kE *kE, 1)
+    gs3d_f32k_tb(const float *__restrict__ U, const float *__restrict__ V,
+                 const float *__restrict__ cU, const float *__restrict__ cV,
+                 float *__restrict__ Un, float *__restrict__ Vn, float *__restrict__ cUn,
+                 float *__restrict__ cVn, int nx, int ny, int nz, int xchunk, int nty,
+                 int ntz, int ntiles, Gs32f c) {
+  constexpr int O = kE - 2 * T;  // output tile edge
+  // s_u[level][parity][row][lane], same for s_v; levels 0..T-1 feed levels 1..T
+  extern __shared__ float smem[];
+  float *s_u = smem;
+  float *s_v = smem + T * 2 * kE * kE;
+  const int lane = threadIdx.x & 31;
+  const int row = threadIdx.x >> 5;
+  const size_t sx = (size_t)ny * nz;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tz = t % ntz;
+    const int ty = (t / ntz) % nty;
+    const int tx = t / (ntz * nty);
+    const int x0 = tx * xchunk;
+    const int x1 = min(x0 + xchunk, nx);
+    const int gy_out = ty * O + row - T;  // global y of this thread's column
+    const int gz_out = tz * O + lane - T;
+    const size_t col = (size_t)wrap_any(gy_out, ny) * nz + wrap_any(gz_out, nz);
+    const bool writer = row >= T && row < T + O && lane >= T && lane < T + O &&
+                        gy_out < ny && gz_out < nz;
+    float wu[T][3], wv[T][3];  // level s window: planes (newest-2, newest-1, newest)
+    float clu[T], clv[T];      // level s compensation at its newest plane
+#pragma unroll
+    for (int s = 0; s < T; ++s) {
+      wu[s][0] = wu[s][1] = wu[s][2] = 0.0f;
+      wv[s][0] = wv[s][1] = wv[s][2] = 0.0f;
+      clu[s] = clv[s] = 0.0f;
+    }
+    // Input planes are prefetched kPF iterations ahead so that their load
+    // latency overlaps the T levels of work of the planes before them.
+    constexpr int kPF = 2;
+    float pu[kPF], pv[kPF], pcu[kPF], pcv[kPF];
+#pragma unroll
+    for (int k = 0; k < kPF; ++k) {
+      const int ip = x0 - T + k;
+      const size_t g = (size_t)wrap_any(ip, nx) * sx + col;
+      pu[k] = __ldg(U + g);
+      pv[k] = __ldg(V + g);
+      pcu[k] = __ldg(cU + g);
+      pcv[k] = __ldg(cV + g);
+    }
+    for (int i = x0 - T; i < x1 + T; ++i) {
+      const int par = i & 1;
+      // ---- level 0: plane i from the prefetch queue; queue plane i+kPF
+      const float in_u = pu[0], in_v = pv[0], in_cu = pcu[0], in_cv = pcv[0];
+#pragma unroll
+      for (int k = 0; k + 1 < kPF; ++k) {
+        pu[k] = pu[k + 1];
+        pv[k] = pv[k + 1];
+        pcu[k] = pcu[k + 1];
+        pcv[k] = pcv[k + 1];
+      }
+      if (i + kPF < x1 + T) {
+        const size_t g = (size_t)wrap_any(i + kPF, nx) * sx + col;
+        pu[kPF - 1] = __ldg(U + g);
+        pv[kPF - 1] = __ldg(V + g);
+        pcu[kPF - 1] = __ldg(cU + g);
+        pcv[kPF - 1] = __ldg(cV + g);
+      }
+      {
+        wu[0][0] = wu[0][1];
+        wu[0][1] = wu[0][2];
+        wu[0][2] = in_u;
+        wv[0][0] = wv[0][1];
+        wv[0][1] = wv[0][2];
+        wv[0][2] = in_v;
+        s_u[((0 * 2 + par) * kE + row) * kE + lane] = in_u;
+        s_v[((0 * 2 + par) * kE + row) * kE + lane] = in_v;
+      }
+      float carry_u = clu[0], carry_v = clv[0];  // level 0's c at plane i-1
+      clu[0] = in_cu;
+      clv[0] = in_cv;
+      // ---- levels 1..T: level s advances plane i-s
+#pragma unroll
+      for (int s = 1; s <= T; ++s) {
+        const float u = wu[s - 1][1], v = wv[s - 1][1];
+        // z neighbours from lanes +-1 (lanes 0/31 are never valid at s >= 1)
+        const float uzm = __shfl_up_sync(0xffffffffu, u, 1);
+        const float uzp = __shfl_down_sync(0xffffffffu, u, 1);
+        const float vzm = __shfl_up_sync(0xffffffffu, v, 1);
+        const float vzp = __shfl_down_sync(0xffffffffu, v, 1);
+        const float cin_u = carry_u, cin_v = carry_v;
+        if (row >= s && row < kE - s) {  // warp-uniform
+          const int base = ((s - 1) * 2 + (par ^ 1)) * kE;
+          const float uym = s_u[(base + row - 1) * kE + lane];
+          const float uyp = s_u[(base + row + 1) * kE + lane];
+          const float vym = s_v[(base + row - 1) * kE + lane];
+          const float vyp = s_v[(base + row + 1) * kE + lane];
+          const float lu = (((wu[s - 1][2] - u) + (wu[s - 1][0] - u)) + ((uyp - u) + (uym - u))) +
+                           ((uzp - u) + (uzm - u));
+          const float lv = (((wv[s - 1][2] - v) + (wv[s - 1][0] - v)) + ((vyp - v) + (vym - v))) +
+                           ((vzp - v) + (vzm - v));
+          float un, vn, cun, cvn;
+          cell_step(u, v, lu, lv, cin_u, cin_v, c, un, vn, cun, cvn);
+          if (s < T) {
+            carry_u = clu[s];
+            carry_v = clv[s];
+            clu[s] = cun;
+            clv[s] = cvn;
+            wu[s][0] = wu[s][1];
+            wu[s][1] = wu[s][2];
+            wu[s][2] = un;
+            wv[s][0] = wv[s][1];
+            wv[s][1] = wv[s][2];
+            wv[s][2] = vn;
+            s_u[((s * 2 + par) * kE + row) * kE + lane] = un;
+            s_v[((s * 2 + par) * kE + row) * kE + lane] = vn;
+          } else {
+            const int p = i - T;
+            if (writer && p >= x0) {
+              const size_t g = (size_t)p * sx + col;
+              Un[g] = un;
+              Vn[g] = vn;
+              cUn[g] = cun;
+              cVn[g] = cvn;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <int T>
+int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const float *cu,
+              const float *cv, float *un, float *vn, float *cun, float *cvn, const Gs32f &c,
+              cudaStream_t s) {
+  constexpr int O = kE - 2 * T;
+  const size_t smem = (size_t)2 * T * 2 * kE * kE * sizeof(float);
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && !attr_set[dev]) {
+    FM_TRY_CUDA(cudaFuncSetAttribute(gs3d_f32k_tb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    attr_set[dev] = true;
+  }
+  int sms = 0;
+  int st = fm::device_sm_count(&sms);
+  if (st) return st;
+  int per_sm = 0;
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs3d_f32k_tb<T>, kE * kE,
+                                                             smem));
+  const int resident = sms * std::max(per_sm, 1);
+  const int nty = (ny + O - 1) / O, ntz = (nz + O - 1) / O;
+  const long long nyz = (long long)nty * ntz;
+  int xc = fm::tune_get("gs3d_f32k.xchunk", 0);
+  if (xc <= 0) {
+    // minimise waves x (chunk + 2T pipeline fill)
+    double best = 1e300;
+    for (int cand = 4; cand <= nx; cand += 4) {
+      const long long tiles = nyz * ((nx + cand - 1) / cand);
+      const double cost = (double)((tiles + resident - 1) / resident) * (cand + 2 * T);
+      if (cost < best - 1e-9) {
+        best = cost;
+        xc = cand;
+      }
+    }
+    if (xc <= 0) xc = nx;
+  }
+  xc = std::min(xc, nx);
+  const long long ntiles = nyz * ((nx + xc - 1) / xc);
+  if (ntiles > (1ll << 30)) {
+    fm::set_error("fm_gs3d_f32k_tb_forward: grid too large");
+    return FM_ERR_UNSUPPORTED;
+  }
+  const int grid = (int)std::min<long long>(ntiles, resident);
+  gs3d_f32k_tb<T><<<grid, kE * kE, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz, xc,
+                                               nty, ntz, (int)ntiles, c);
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+
+}  // namespace
+
+extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *V, float *cU,
+                                       float *cV, float *work, int steps, int tb,
+                                       const fm_gs_params *p, void *stream) {
+  FM_CHECK_ARG(p && U && V && cU && cV && work, "fm_gs3d_f32k_tb_forward: NULL argument");
+  FM_CHECK_ARG(nx >= 1 && ny >= 1 && nz >= 1, "fm_gs3d_f32k_tb_forward: empty grid");
+  FM_CHECK_ARG((long long)ny * nz < (1ll << 31), "fm_gs3d_f32k_tb_forward: plane too large");
+  FM_CHECK_ARG(steps >= 0 && tb >= 0 && tb <= 4,
+               "fm_gs3d_f32k_tb_forward: need steps >= 0 and 0 <= tb <= 4 (got %d, %d)", steps,
+               tb);
+  if (steps == 0) return FM_OK;
+  if (tb == 0) tb = fm::tune_get("gs3d_f32k.tb", 3);  // 3: fastest at 256^3 on GB300
+  tb = std::max(1, std::min(tb, 4));
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  Gs32f c;
+  c.F = (float)p->F;
+  c.Fk = (float)(p->F + p->k);
+  c.cu = (float)(p->Du / (p->dx * p->dx));
+  c.cv = (float)(p->Dv / (p->dx * p->dx));
+  c.dt = (float)p->dt;
+  const size_t n = (size_t)nx * ny * nz;
+  float *cur[4] = {U, V, cU, cV};
+  float *nxt[4] = {work, work + n, work + 2 * n, work + 3 * n};
+  int done = 0;
+  while (done < steps) {
+    const int t = std::min(tb, steps - done);
+    int st;
+    switch (t) {
+      case 1: st = launch_tb<1>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
+      case 2: st = launch_tb<2>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
+      case 3: st = launch_tb<3>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
+      default: st = launch_tb<4>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
+    }
+    if (st) return st;
+    for (int k = 0; k < 4; ++k) std::swap(cur[k], nxt[k]);
+    done += t;
+  }
+  if (cur[0] != U) {
+    float *dst[4] = {U, V, cU, cV};
+    for (int k = 0; k < 4; ++k)
+      FM_TRY_CUDA(cudaMemcpyAsync(dst[k], cur[k], n * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  }
+  return FM_OK;
+}

@@ -47,17 +47,30 @@ def gs3d_f64_forward(U, V, work_U, work_V, params: GsParams, steps: int, stream=
     check(st, "fm_gs3d_f64_forward")
 
 
-def gs3d_f32k_forward(U, V, cU, cV, work, params: GsParams, steps: int, tb: int = 0, stream=None):
-    """Advance FP32 U,V with Kahan compensations cU,cV by `steps` in place."""
+def _f32k_args(U, V, cU, cV, work):
     shp = tuple(U.shape)
     if len(shp) != 3:
         raise ValueError("U must be 3D")
     args = [_need(t, torch.float32, shp, n) for t, n in ((U, "U"), (V, "V"), (cU, "cU"), (cV, "cV"))]
     n = shp[0] * shp[1] * shp[2]
-    w = _need(work, torch.float32, (4 * n,), "work")
-    st = lib().fm_gs3d_f32k_forward(shp[0], shp[1], shp[2], *args, w, int(steps), int(tb),
+    return shp, args, _need(work, torch.float32, (4 * n,), "work")
+
+
+def gs3d_f32k_forward(U, V, cU, cV, work, params: GsParams, steps: int, stream=None):
+    """Advance FP32 U,V (generated DAG in float) with Kahan compensations cU,cV."""
+    shp, args, w = _f32k_args(U, V, cU, cV, work)
+    st = lib().fm_gs3d_f32k_forward(shp[0], shp[1], shp[2], *args, w, int(steps),
                                     ctypes.byref(params), ctypes.c_void_p(_stream_ptr(stream)))
     check(st, "fm_gs3d_f32k_forward")
+
+
+def gs3d_f32k_tb_forward(U, V, cU, cV, work, params: GsParams, steps: int, tb: int = 0,
+                         stream=None):
+    """Advance FP32 U,V (fast form, Kahan) by `steps`, `tb` steps per HBM pass."""
+    shp, args, w = _f32k_args(U, V, cU, cV, work)
+    st = lib().fm_gs3d_f32k_tb_forward(shp[0], shp[1], shp[2], *args, w, int(steps), int(tb),
+                                       ctypes.byref(params), ctypes.c_void_p(_stream_ptr(stream)))
+    check(st, "fm_gs3d_f32k_tb_forward")
 
 
 def diff2d_f64_forward(dens, work, coef: float, steps: int, stream=None):

@@ -23,9 +23,10 @@ PROGRAMS = {
         constants=GS3D_CONSTANTS, monitor_interval=2000,
         temporal_blocking_interval=1, mpi_grid_shape=(1, 1, 1)),
     # The same program in binary32 with Kahan time accumulation, temporally
-    # blocked 8 steps per HBM pass (M = 2000 is a multiple of 2*8).
+    # blocked (temporal_blocking_interval 8: M = 2000 is a multiple of 2*8; the
+    # kernel runs its tuned on-chip depth per HBM pass).
     "gray_scott_3d_f32k": Program(
-        name="gray_scott_3d_f32k", form="gs3d_f32k", intra_node_shape=(256, 256, 256),
+        name="gray_scott_3d_f32k", form="gs3d_f32k_tb", intra_node_shape=(256, 256, 256),
         constants=GS3D_CONSTANTS, monitor_interval=2000,
         temporal_blocking_interval=8, mpi_grid_shape=(1, 1, 1)),
 }

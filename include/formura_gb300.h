@@ -99,18 +99,33 @@ int fm_gs3d_f64_forward(int nx, int ny, int nz, double *U, double *V,
                         int steps, void *stream);
 
 /*
- * 3D Gray-Scott, same form, binary32 arithmetic with compensated (Kahan) time
- * accumulation: per field y = dt*dW - cW; t = W + y; cW = (t - W) - y; W = t.
+ * 3D Gray-Scott, the same generated DAG evaluated in binary32 (the .fmr
+ * program with `float` state), with compensated (Kahan) time accumulation:
+ * per field y = dt*dW - cW; t = W + y; cW = (t - W) - y; W = t.
  * U,V,cU,cV are [nx][ny][nz] float device arrays (cU,cV = running
  * compensation, zero them before the first call); work must hold 4*nx*ny*nz
- * floats.  `tb` = time steps fused per HBM pass (temporal blocking depth;
- * 1 = one step per pass; 0 = library default).
- * Bit-exact with the binary32 restatement of the same DAG without FMA
- * contraction.  Requires nz % 32 == 0, ny % 8 == 0, 2^-20 <= (float)dx <= 2^20.
+ * floats.  One step per launch.  Bit-exact with the binary32 restatement of
+ * the DAG without FMA contraction.
+ * Requires nz % 32 == 0, ny % 8 == 0, 2^-20 <= (float)dx <= 2^20.
  */
 int fm_gs3d_f32k_forward(int nx, int ny, int nz, float *U, float *V, float *cU,
-                         float *cV, float *work, int steps, int tb,
+                         float *cV, float *work, int steps,
                          const fm_gs_params *p, void *stream);
+
+/*
+ * 3D Gray-Scott in binary32 with Kahan time accumulation, temporally blocked:
+ * `tb` steps (1..4; 0 = tuned default) run per HBM round trip, streaming
+ * overlapped 32x32 (y,z) tiles along x (Formura's temporal blocking,
+ * src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134 and the skewed
+ * regions of src/Formura/MPICxx/Cut.hs:240-281, as on-chip pipelines).
+ * Arithmetic is the binary32 "fast form" (per-axis sums of differences,
+ * explicit FMAs, constants Du/dx^2, Dv/dx^2, F+k rounded once to float):
+ * results are bit-identical for every tb and are judged by their error against
+ * the FP64 run.  Same arrays as fm_gs3d_f32k_forward; any nx, ny, nz >= 1.
+ */
+int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *V,
+                            float *cU, float *cV, float *work, int steps,
+                            int tb, const fm_gs_params *p, void *stream);
 
 /* ---- 2D diffusion --------------------------------------------------------- */
 
@@ -180,7 +195,8 @@ int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
  *                      128-bit integer products; default), 2 residual + integer compare
  *                      (2 FP64 ops)
  *   "gs3d_f64.xchunk"  x planes per CTA tile (0 = automatic)
- *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_forward
+ *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_tb_forward (1..4)
+ *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)
  * fm_tune_clear() restores every default.
  */
 int fm_tune_set(const char *key, int value);

@@ -368,6 +368,72 @@ void fo_gs3d_run_f32_kahan(int nx, int ny, int nz, float *U, float *V,
   free(buf);
 }
 
+/* Fast binary32 form (see fmr_oracle.h). */
+static void gs3d_step_f32k_fast(int nx, int ny, int nz, const float *restrict U,
+                                const float *restrict V, const float *restrict cU,
+                                const float *restrict cV, float *restrict Un,
+                                float *restrict Vn, float *restrict cUn,
+                                float *restrict cVn, float F, float Fk, float cu,
+                                float cv, float dt) {
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int x = 0; x < nx; ++x) {
+    for (int y = 0; y < ny; ++y) {
+      const int xp = wrap_up(x, nx), xm = wrap_dn(x, nx);
+      const int yp = wrap_up(y, ny), ym = wrap_dn(y, ny);
+      for (int z = 0; z < nz; ++z) {
+        const int zp = wrap_up(z, nz), zm = wrap_dn(z, nz);
+        const size_t i = IDX3(x, y, z);
+        const float u = U[i], v = V[i];
+        const float sxu = (U[IDX3(xp, y, z)] - u) + (U[IDX3(xm, y, z)] - u);
+        const float syu = (U[IDX3(x, yp, z)] - u) + (U[IDX3(x, ym, z)] - u);
+        const float szu = (U[IDX3(x, y, zp)] - u) + (U[IDX3(x, y, zm)] - u);
+        const float lu = (sxu + syu) + szu;
+        const float sxv = (V[IDX3(xp, y, z)] - v) + (V[IDX3(xm, y, z)] - v);
+        const float syv = (V[IDX3(x, yp, z)] - v) + (V[IDX3(x, ym, z)] - v);
+        const float szv = (V[IDX3(x, y, zp)] - v) + (V[IDX3(x, y, zm)] - v);
+        const float lv = (sxv + syv) + szv;
+        const float uvv = (u * v) * v;
+        const float dU = fmaf(cu, lu, fmaf(F, 1.0f - u, -uvv));
+        const float dV = fmaf(cv, lv, fmaf(-Fk, v, uvv));
+        const float yu = fmaf(dt, dU, -cU[i]);
+        const float tu = u + yu;
+        cUn[i] = (tu - u) - yu;
+        Un[i] = tu;
+        const float yv = fmaf(dt, dV, -cV[i]);
+        const float tv = v + yv;
+        cVn[i] = (tv - v) - yv;
+        Vn[i] = tv;
+      }
+    }
+  }
+}
+
+void fo_gs3d_run_f32k_fast(int nx, int ny, int nz, float *U, float *V,
+                           float *cU, float *cV, int steps, double F, double k,
+                           double Du, double Dv, double dt, double dx) {
+  const size_t n = (size_t)nx * ny * nz;
+  const float Ff = (float)F, Fk = (float)(F + k), cu = (float)(Du / (dx * dx)),
+              cv = (float)(Dv / (dx * dx)), dtf = (float)dt;
+  float *buf = (float *)malloc(4 * n * sizeof(float));
+  float *cu_ = U, *cv_ = V, *ccu = cU, *ccv = cV;
+  float *nu = buf, *nv = buf + n, *ncu = buf + 2 * n, *ncv = buf + 3 * n;
+  for (int s = 0; s < steps; ++s) {
+    gs3d_step_f32k_fast(nx, ny, nz, cu_, cv_, ccu, ccv, nu, nv, ncu, ncv, Ff, Fk, cu, cv, dtf);
+    float *t;
+    t = cu_; cu_ = nu; nu = t;
+    t = cv_; cv_ = nv; nv = t;
+    t = ccu; ccu = ncu; ncu = t;
+    t = ccv; ccv = ncv; ncv = t;
+  }
+  if (cu_ != U) {
+    memcpy(U, cu_, n * sizeof(float));
+    memcpy(V, cv_, n * sizeof(float));
+    memcpy(cU, ccu, n * sizeof(float));
+    memcpy(cV, ccv, n * sizeof(float));
+  }
+  free(buf);
+}
+
 double fo_sum_f64(int64_t n, const double *a) {
   double s = 0.0;
   for (int64_t i = 0; i < n; ++i) s += a[i];

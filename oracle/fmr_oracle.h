@@ -59,6 +59,19 @@ void fo_gs3d_run_f32_kahan(int nx, int ny, int nz, float *U, float *V,
                            float *cU, float *cV, int steps, float F, float k,
                            float Du, float Dv, float dt, float dx);
 
+/* The binary32 "fast form" of the same 3D Gray-Scott step that the
+ * temporally blocked GPU kernel evaluates (FMAs explicit, no divisions):
+ *   s_a = (W[a+1]-W) + (W[a-1]-W);  lap = (s_x + s_y) + s_z
+ *   uvv = (U*V)*V
+ *   dU = fmaf(cu, lapU, fmaf(F, 1-U, -uvv))     cu = (float)(Du/(dx*dx))
+ *   dV = fmaf(cv, lapV, fmaf(-Fk, V, uvv))      cv = (float)(Dv/(dx*dx)), Fk = (float)(F+k)
+ *   Kahan per field: y = fmaf(dt, dW, -cW); t = W + y; cW = (t - W) - y; W = t
+ * It is not the generated DAG (that is fo_gs3d_run_f32_kahan); its accuracy is
+ * judged against fo_gs3d_run_f64. */
+void fo_gs3d_run_f32k_fast(int nx, int ny, int nz, float *U, float *V,
+                           float *cU, float *cV, int steps, double F, double k,
+                           double Du, double Dv, double dt, double dx);
+
 /* Plain left-to-right double sum (conserved-total check). */
 double fo_sum_f64(int64_t n, const double *a);
 

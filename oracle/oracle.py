@@ -49,6 +49,7 @@ def _load(name: str) -> ctypes.CDLL:
     h.fo_diff2d_run_f64.argtypes = [i, i, P, i, d, d]
     h.fo_gs3d_run_f64.argtypes = [i, i, i, P, P, i, ctypes.POINTER(GsParams)]
     h.fo_gs3d_run_f32_kahan.argtypes = [i, i, i, P, P, P, P, i, f, f, f, f, f, f]
+    h.fo_gs3d_run_f32k_fast.argtypes = [i, i, i, P, P, P, P, i, d, d, d, d, d, d]
     h.fo_sum_f64.argtypes = [ctypes.c_int64, P]
     h.fo_sum_f64.restype = d
     h.fo_num_threads.restype = i
@@ -101,6 +102,15 @@ def gs3d_f32_kahan(U, V, cU, cV, steps, F, k, Du, Dv, dt, dx, fast=False):
     nx, ny, nz = arrs[0].shape
     lib(fast).fo_gs3d_run_f32_kahan(nx, ny, nz, *[_ptr(a) for a in arrs], int(steps),
                                     *[ctypes.c_float(x) for x in (F, k, Du, Dv, dt, dx)])
+    return tuple(arrs)
+
+
+def gs3d_f32k_fast(U, V, cU, cV, steps, F, k, Du, Dv, dt, dx, fast=False):
+    """The binary32 fast form with Kahan accumulation (the TB kernel's math)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float32).copy() for a in (U, V, cU, cV)]
+    nx, ny, nz = arrs[0].shape
+    lib(fast).fo_gs3d_run_f32k_fast(nx, ny, nz, *[_ptr(a) for a in arrs], int(steps),
+                                    float(F), float(k), float(Du), float(Dv), float(dt), float(dx))
     return tuple(arrs)
 
 

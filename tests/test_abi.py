@@ -57,9 +57,12 @@ def test_argument_validation_precedes_device_work(core_lib):
     assert st == 1 and b"dx" in core_lib.fm_last_error()
     st = core_lib.fm_diff2d_f64_forward(8, 30, fake, fake, 0.1, 1, None)
     assert st == 1
-    st = core_lib.fm_gs3d_f32k_forward(8, 12, 32, fake, fake, fake, fake, fake, 1, 1,
+    st = core_lib.fm_gs3d_f32k_forward(8, 12, 32, fake, fake, fake, fake, fake, 1,
                                        ctypes.byref(p), None)
     assert st == 1
+    st = core_lib.fm_gs3d_f32k_tb_forward(8, 16, 32, fake, fake, fake, fake, fake, 4, 5,
+                                          ctypes.byref(p), None)
+    assert st == 1 and b"tb" in core_lib.fm_last_error()
     # zero steps is a no-op that touches nothing
     st = core_lib.fm_gs3d_f64_forward(8, 16, 32, fake, fake, fake, fake, ctypes.byref(p), 0, None)
     assert st == 0

@@ -122,31 +122,68 @@ def test_gs3d_program_forward_matches_oracle(cuda_device, tmp_path):
     prog.finalize()
 
 
-def run_f32k(U0, V0, steps, tb, dev):
+def run_f32k(U0, V0, steps, tb, dev, cU0=None, cV0=None):
+    """tb None: the generated-DAG float kernel; else the temporally blocked fast form."""
     n = U0.size
     U = torch.from_numpy(U0.astype(np.float32)).to(dev)
     V = torch.from_numpy(V0.astype(np.float32)).to(dev)
-    cU, cV = torch.zeros_like(U), torch.zeros_like(V)
+    cU = torch.zeros_like(U) if cU0 is None else torch.from_numpy(cU0).to(dev)
+    cV = torch.zeros_like(V) if cV0 is None else torch.from_numpy(cV0).to(dev)
     work = torch.empty(4 * n, dtype=torch.float32, device=dev)
-    kernels.gs3d_f32k_forward(U, V, cU, cV, work, kernels.gs_params(**GS), steps, tb)
+    if tb is None:
+        kernels.gs3d_f32k_forward(U, V, cU, cV, work, kernels.gs_params(**GS), steps)
+    else:
+        kernels.gs3d_f32k_tb_forward(U, V, cU, cV, work, kernels.gs_params(**GS), steps, tb)
     torch.cuda.synchronize()
     return [t.cpu().numpy() for t in (U, V, cU, cV)]
 
 
-@pytest.mark.parametrize("tb", [1, 4, 8])
 @pytest.mark.parametrize("shape,steps", [((32, 32, 32), 24), ((20, 24, 64), 16)])
-def test_gs3d_f32k_bit_exact(cuda_device, shape, steps, tb):
+def test_gs3d_f32k_dag_bit_exact(cuda_device, shape, steps):
     U0, V0 = inits.gray_scott_3d(*shape, seed=4, ncubes=3, side=8)
-    got = run_f32k(U0, V0, steps, tb, cuda_device)
+    got = run_f32k(U0, V0, steps, None, cuda_device)
     Z = np.zeros(shape, np.float32)
     want = oracle.gs3d_f32_kahan(U0.astype(np.float32), V0.astype(np.float32), Z, Z, steps, **GS)
     for g, w in zip(got, want):
         assert np.array_equal(g, w)
 
 
+@pytest.mark.parametrize("tb", [1, 2, 3, 4])
+@pytest.mark.parametrize("shape,steps", [((32, 32, 32), 13), ((20, 24, 64), 8), ((7, 45, 33), 5),
+                                         ((64, 64, 64), 12)])
+def test_gs3d_f32k_tb_bit_exact(cuda_device, shape, steps, tb):
+    """Every blocking depth gives the fast form's step-by-step result bit for bit,
+    including ragged tiles (sizes not multiples of the output tile) and a
+    nonzero incoming compensation."""
+    U0, V0 = inits.gray_scott_3d(*shape, seed=4, ncubes=3, side=4)
+    rng = np.random.default_rng(1)
+    cU0 = (rng.standard_normal(shape) * 1e-9).astype(np.float32)
+    cV0 = (rng.standard_normal(shape) * 1e-9).astype(np.float32)
+    got = run_f32k(U0, V0, steps, tb, cuda_device, cU0, cV0)
+    want = oracle.gs3d_f32k_fast(U0.astype(np.float32), V0.astype(np.float32), cU0, cV0, steps,
+                                 **GS)
+    for g, w in zip(got, want):
+        assert np.array_equal(g, w)
+
+
+def test_gs3d_f32k_tb_xchunk_variants(cuda_device):
+    lib = _lib.lib()
+    U0, V0 = inits.gray_scott_3d(40, 32, 32, seed=9, ncubes=2, side=8)
+    Z = np.zeros(U0.shape, np.float32)
+    want = oracle.gs3d_f32k_fast(U0.astype(np.float32), V0.astype(np.float32), Z, Z, 8, **GS)
+    try:
+        for xc in (1, 3, 8, 40, 100):
+            lib.fm_tune_set(b"gs3d_f32k.xchunk", xc)
+            got = run_f32k(U0, V0, 8, 4, cuda_device)
+            assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), xc
+    finally:
+        lib.fm_tune_clear()
+
+
 def test_gs3d_f32k_error_against_f64(cuda_device):
     U0, V0 = inits.gray_scott_3d(32, 32, 64, seed=2, ncubes=2, side=8)
-    U, V, _, _ = run_f32k(U0, V0, 400, 8, cuda_device)
     Uo, Vo = oracle.gs3d_f64(U0, V0, 400, **GS)
-    assert np.linalg.norm(U - Uo) / np.linalg.norm(Uo) < 1e-5
-    assert np.linalg.norm(V - Vo) / np.linalg.norm(Vo) < 1e-4
+    for tb in (None, 4):
+        U, V, _, _ = run_f32k(U0, V0, 400, tb, cuda_device)
+        assert np.linalg.norm(U - Uo) / np.linalg.norm(Uo) < 1e-6
+        assert np.linalg.norm(V - Vo) / np.linalg.norm(Vo) < 1e-5
