@@ -57,6 +57,17 @@ SIGNATURES = {
                                         ctypes.POINTER(GsParams), c_void_p]),
     "fm_diff2d_f64_forward": (c_int, [c_int, c_int, c_void_p, c_void_p, c_double, c_int, c_void_p]),
     "fm_diff2d_f64_forward_noalloc": (c_int, [c_int, c_int, c_void_p, c_double, c_int, c_void_p]),
+    "fm_gs2d_f32_forward": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    ctypes.POINTER(GsParams), c_int, c_void_p]),
+    "fm_gs2d_ensemble_create": (c_int, [ctypes.POINTER(c_void_p), c_int, ctypes.POINTER(c_int),
+                                        ctypes.POINTER(c_double), ctypes.POINTER(c_double),
+                                        c_double, c_double, c_double, c_double, c_int, c_int]),
+    "fm_gs2d_ensemble_layout": (c_int, [c_void_p, ctypes.POINTER(c_int64),
+                                        ctypes.POINTER(c_int64), ctypes.POINTER(c_int)]),
+    "fm_gs2d_ensemble_forward": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                         c_int, c_void_p]),
+    "fm_gs2d_ensemble_status": (c_int, [c_void_p, c_void_p]),
+    "fm_gs2d_ensemble_destroy": (c_int, [c_void_p]),
     "fm_sum_f64_scratch_elems": (c_size_t, [c_int64]),
     "fm_sum_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f32_as_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),

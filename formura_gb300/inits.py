@@ -72,3 +72,28 @@ def gray_scott_2d_square(nx: int, ny: int, seed: int = 1, dtype=np.float64, frac
     U[np.ix_(ix, iy)] = 0.5 + 0.01 * r[0]
     V[np.ix_(ix, iy)] = 0.25 + 0.01 * r[1]
     return U.astype(dtype), V.astype(dtype)
+
+
+ENSEMBLE_SIZES = (64, 128, 256, 512, 1024)
+
+
+def gs2d_ensemble(n_inst: int = 512, seed: int = 1, sizes=ENSEMBLE_SIZES,
+                  F_range=(0.02, 0.06), k_range=(0.05, 0.07)):
+    """The batched 2D Gray-Scott workload: instance sizes drawn uniformly from
+    `sizes`, F ~ U[F_range], k ~ U[k_range] (seeded).  Returns (sizes, F, k)."""
+    r = uniform(seed, 3 * n_inst).reshape(3, n_inst)
+    sz = [int(sizes[min(int(x * len(sizes)), len(sizes) - 1)]) for x in r[0]]
+    F = F_range[0] + (F_range[1] - F_range[0]) * r[1]
+    k = k_range[0] + (k_range[1] - k_range[0]) * r[2]
+    return sz, F, k
+
+
+def gs2d_ensemble_state(sizes, seed: int = 1, dtype=np.float32):
+    """Flat U, V of an ensemble: instance i is gray_scott_2d_square(n_i, n_i,
+    seed + i) laid out back to back."""
+    us, vs = [], []
+    for i, n in enumerate(sizes):
+        u, v = gray_scott_2d_square(n, n, seed=seed * 100003 + i)
+        us.append(u.reshape(-1))
+        vs.append(v.reshape(-1))
+    return np.concatenate(us).astype(dtype), np.concatenate(vs).astype(dtype)

@@ -114,3 +114,75 @@ def probe_fma(fp64: bool, blocks: int, threads: int, iters: int, sink: torch.Ten
     st = lib().fm_probe_fma(1 if fp64 else 0, blocks, threads, iters,
                             ctypes.c_void_p(sink.data_ptr()), ctypes.c_void_p(_stream_ptr(stream)))
     check(st, "fm_probe_fma")
+
+
+def gs2d_f32_forward(U, V, work_U, work_V, params: GsParams, steps: int, stream=None):
+    """One 2D Gray-Scott instance (pearson-2d form, float), one launch per step."""
+    shp = tuple(U.shape)
+    if len(shp) != 2:
+        raise ValueError("U must be 2D")
+    args = [_need(t, torch.float32, shp, n) for t, n in
+            ((U, "U"), (V, "V"), (work_U, "work_U"), (work_V, "work_V"))]
+    st = lib().fm_gs2d_f32_forward(shp[0], shp[1], *args, ctypes.byref(params), int(steps),
+                                   ctypes.c_void_p(_stream_ptr(stream)))
+    check(st, "fm_gs2d_f32_forward")
+
+
+class Ensemble:
+    """An uneven ensemble of periodic 2D Gray-Scott instances (fm_gs2d_ensemble_*).
+
+    ``sizes[i]`` x ``sizes[i]`` cells with their own ``F[i]``, ``k[i]``; all
+    instances' U (and V) back to back in one float32 CUDA buffer, instance i
+    starting at ``offsets[i]``.
+    """
+
+    def __init__(self, sizes, F, k, Du=2e-5, Dv=1e-5, dt=1.0, dx=0.01, tile=0, tb=0):
+        import numpy as np
+
+        n = len(sizes)
+        if not (len(F) == len(k) == n) or n == 0:
+            raise ValueError("sizes, F, k must have the same nonzero length")
+        self.sizes = [int(s) for s in sizes]
+        sz = (ctypes.c_int * n)(*self.sizes)
+        f = (ctypes.c_double * n)(*map(float, F))
+        kk = (ctypes.c_double * n)(*map(float, k))
+        h = ctypes.c_void_p()
+        check(lib().fm_gs2d_ensemble_create(ctypes.byref(h), n, sz, f, kk, float(Du), float(Dv),
+                                            float(dt), float(dx), int(tile), int(tb)),
+              "fm_gs2d_ensemble_create")
+        self._h = h
+        total = ctypes.c_int64()
+        offs = (ctypes.c_int64 * n)()
+        nt = ctypes.c_int()
+        check(lib().fm_gs2d_ensemble_layout(h, ctypes.byref(total), offs, ctypes.byref(nt)),
+              "fm_gs2d_ensemble_layout")
+        self.total_cells = int(total.value)
+        self.offsets = np.array(offs[:], dtype=np.int64)
+        self.ntiles = int(nt.value)
+
+    def view(self, flat, i):
+        o, s = int(self.offsets[i]), self.sizes[i]
+        return flat[o:o + s * s].view(s, s)
+
+    def forward(self, U, V, work_U, work_V, steps: int, use_graph: bool = True, stream=None):
+        shp = (self.total_cells,)
+        args = [_need(t, torch.float32, shp, n) for t, n in
+                ((U, "U"), (V, "V"), (work_U, "work_U"), (work_V, "work_V"))]
+        check(lib().fm_gs2d_ensemble_forward(self._h, *args, int(steps), 1 if use_graph else 0,
+                                             ctypes.c_void_p(_stream_ptr(stream))),
+              "fm_gs2d_ensemble_forward")
+
+    def status(self, stream=None):
+        check(lib().fm_gs2d_ensemble_status(self._h, ctypes.c_void_p(_stream_ptr(stream))),
+              "fm_gs2d_ensemble_status")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fm_gs2d_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

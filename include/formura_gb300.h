@@ -127,6 +127,50 @@ int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *V,
                             float *cU, float *cV, float *work, int steps,
                             int tb, const fm_gs_params *p, void *stream);
 
+/* ---- 2D Gray-Scott and uneven ensembles ------------------------------------- */
+
+/*
+ * 2D Gray-Scott in the examples/pearson-2d.fmr form, binary32, one instance:
+ * the float evaluation of the DAG of examples-generated/pearson.c:138-208
+ * (no FMA contraction; Du/(dx*dx), Dv/(dx*dx), F+k evaluated in float in DAG
+ * order).  U,V are [nx][ny]; work_U, work_V the ping-pong pair.  One launch
+ * per step (the "sequential per-instance launches" baseline of ensembles).
+ */
+int fm_gs2d_f32_forward(int nx, int ny, float *U, float *V, float *work_U,
+                        float *work_V, const fm_gs_params *p, int steps,
+                        void *stream);
+
+/*
+ * An ensemble of independent periodic 2D Gray-Scott instances of uneven sizes
+ * (n_i x n_i) and their own F_i, k_i, sharing Du, Dv, dt, dx — the batched
+ * form of the pearson-2d program.  All instances' U (and V) are stored back to
+ * back in one float buffer; fm_gs2d_ensemble_layout gives each instance's
+ * first cell.  Per cell the arithmetic is that of fm_gs2d_f32_forward
+ * (bit-identical results).
+ *
+ * fm_gs2d_ensemble_create builds the plan (device instance and tile tables):
+ * `tile` = output tile edge (32 or 64; 0 = tuned default), `tb` = time steps
+ * per shared-memory pass (1..8; 0 = tuned default).
+ * fm_gs2d_ensemble_forward advances every instance `steps` steps in ONE
+ * cooperative persistent launch (grid barrier between passes, bounded
+ * waits); with use_graph != 0 the launch is captured once into a CUDA graph
+ * (re-captured when the buffers, stream or step count change) and replayed.
+ * work_U, work_V: ping-pong buffers of total_cells floats.
+ * fm_gs2d_ensemble_status synchronizes `stream` and returns FM_ERR_TIMEOUT if
+ * the last run's grid barrier gave up.
+ */
+typedef struct fm_ensemble fm_ensemble;
+int fm_gs2d_ensemble_create(fm_ensemble **out, int n_inst, const int *sizes,
+                            const double *F, const double *k, double Du,
+                            double Dv, double dt, double dx, int tile, int tb);
+int fm_gs2d_ensemble_layout(const fm_ensemble *e, int64_t *total_cells,
+                            int64_t *offsets, int *ntiles);
+int fm_gs2d_ensemble_forward(fm_ensemble *e, float *U, float *V, float *work_U,
+                             float *work_V, int steps, int use_graph,
+                             void *stream);
+int fm_gs2d_ensemble_status(fm_ensemble *e, void *stream);
+int fm_gs2d_ensemble_destroy(fm_ensemble *e);
+
 /* ---- 2D diffusion --------------------------------------------------------- */
 
 /*
@@ -197,6 +241,8 @@ int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
  *   "gs3d_f64.xchunk"  x planes per CTA tile (0 = automatic)
  *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_tb_forward (1..4)
  *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)
+ *   "gs2d_ens.tile"    default output tile edge of ensembles (32 or 64)
+ *   "gs2d_ens.tb"      default steps per shared-memory pass of ensembles
  * fm_tune_clear() restores every default.
  */
 int fm_tune_set(const char *key, int value);
