@@ -1,0 +1,389 @@
+// fm_mhd.cu — 3D ideal MHD with Dedner divergence cleaning and artificial
+// viscosity: the time step of the reference program examples/3d-mhd-rk4.fmr.
+//
+// Fields (SoA, [n][n][n] each): dens (perturbation of dens0 = 1), vx, vy, vz,
+// Bx, By, Bz, s, Psi.  One step (3d-mhd-rk4.fmr:104-145):
+//   q4 = S + dt/4 f(S);  q3 = S + dt/3 f(q4);  q2 = S + dt/2 f(q3);
+//   nx = S + dt f(q2)                                  (mhd_stage, 4 launches)
+//   then, per field, the artificial-viscosity fluxes of nx along x, y, z
+//   applied in turn, dens floored at -0.9, and s += numerical heat
+//                                                      (mhd_finish, 1 launch)
+// f = ddt_sys (3d-mhd-rk4.fmr:83-101) uses the 4th-order difference
+// (a[i-2] + 8a[i+1] - 8a[i-1] - a[i+2])/(12 dx) of 33 quantities per cell;
+// composite arguments (dens*v_i, pressure, B_j*B_i, v_i*B_j - v_j*B_i) are
+// re-evaluated at each of the four neighbours, as the generated code does.
+//
+// Precision: template parameter R is the bulk type.  R = double reproduces
+// the all-FP64 program bit for bit (IEEE divisions: fm::div_const_i for the
+// constant 12*dx, __ddiv_rn for /dens and num/den).  R = float is the
+// production path: the bulk in binary32, the numerical-heat (energy) update
+// of s in FP64 — the difference of kinetic and magnetic energies before and
+// after the viscosity step is a cancellation-prone small difference — and the
+// conserved totals in FP64 (fm_mhd_totals).
+#include <algorithm>
+
+#include "fm_common.cuh"
+
+namespace {
+
+constexpr int NF = 9;
+
+struct Fields {
+  void *p[NF];
+};
+
+template <typename R>
+struct MhdC {
+  R dt_c;  // stage coefficient (dt/4, dt/3, dt/2, dt)
+  R h12;   // 12*dx
+  R c_h2;  // c_h*c_h
+  R ch2_cp2, c8, c4, dp_ddens, dp_ds, dens0;
+  fm::DivConst h12d;  // for the double path's exact division
+  float h12f, rh12f;  // for the float path's exact division
+};
+
+template <typename R>
+__device__ __forceinline__ R div_h(R x, const MhdC<R> &k);
+template <>
+__device__ __forceinline__ double div_h<double>(double x, const MhdC<double> &k) {
+  return fm::div_const_i(x, k.h12d);
+}
+template <>
+__device__ __forceinline__ float div_h<float>(float x, const MhdC<float> &k) {
+  return fm::div_const_f(x, k.h12f, k.rh12f);
+}
+
+__device__ __forceinline__ double vdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float vdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double vmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float vmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double vmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float vmin(float a, float b) { return fminf(a, b); }
+
+template <typename R>
+__device__ __forceinline__ R ld(const void *f, size_t i) {
+  return __ldg(reinterpret_cast<const R *>(f) + i);
+}
+
+// (((a[-2] + 8*a[+1]) - 8*a[-1]) - a[+2]) / (12*dx)
+template <typename R>
+__device__ __forceinline__ R d4(R am2, R am1, R ap1, R ap2, const MhdC<R> &k) {
+  const R t1 = R(8) * ap1;
+  const R t2 = am2 + t1;
+  const R t3 = R(8) * am1;
+  const R t4 = t2 - t3;
+  const R t5 = t4 - ap2;
+  return div_h<R>(t5, k);
+}
+
+// The quantities whose derivative along axis a is needed, at one point.
+template <typename R>
+struct AxisQ {
+  R m, v, P, BB[3], E[3], s, B;
+};
+
+template <typename R>
+__device__ __forceinline__ AxisQ<R> axis_q(const Fields &Q, size_t i, int a, const MhdC<R> &k) {
+  const R dn = ld<R>(Q.p[0], i);
+  const R v0 = ld<R>(Q.p[1], i), v1 = ld<R>(Q.p[2], i), v2 = ld<R>(Q.p[3], i);
+  const R B0 = ld<R>(Q.p[4], i), B1 = ld<R>(Q.p[5], i), B2 = ld<R>(Q.p[6], i);
+  const R s = ld<R>(Q.p[7], i), Psi = ld<R>(Q.p[8], i);
+  const R v[3] = {v0, v1, v2}, B[3] = {B0, B1, B2};
+  AxisQ<R> q;
+  const R d = k.dens0 + dn;
+  q.m = d * v[a];
+  q.v = v[a];
+  const R b2 = ((B0 * B0) + (B1 * B1)) + (B2 * B2);
+  q.P = ((k.dp_ddens * d) + (k.dp_ds * s)) + (k.c8 * b2);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    q.BB[c] = B[a] * B[c];  // B_j * B_i with j = a
+    // E_ij = -(0*del_ij*Psi) + v_i*B_j - v_j*B_i with j = a, i = c
+    const R z = R(0) * (c == a ? R(1) : R(0));
+    const R t = -(z * Psi);
+    q.E[c] = (t + (v[c] * B[a])) - (v[a] * B[c]);
+  }
+  q.s = s;
+  q.B = B[a];
+  return q;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128)
+    mhd_stage(Fields Q, Fields S, Fields O, int n, MhdC<R> k) {
+  const int z = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+  const int x = blockIdx.z;
+  if (z >= n || y >= n) return;
+  const size_t sx = (size_t)n * n, sy = (size_t)n;
+  const size_t c = (size_t)x * sx + (size_t)y * sy + z;
+  const int co[3] = {x, y, z};
+  const size_t st[3] = {sx, sy, 1};
+  // derivative results
+  R dm[3], dv[3], dP[3], dBB[3][3], dE[3][3], ds[3], dB[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const size_t base = c - (size_t)co[a] * st[a];
+    const int im2 = co[a] - 2 < 0 ? co[a] - 2 + n : co[a] - 2;
+    const int im1 = co[a] - 1 < 0 ? co[a] - 1 + n : co[a] - 1;
+    const int ip1 = co[a] + 1 >= n ? co[a] + 1 - n : co[a] + 1;
+    const int ip2 = co[a] + 2 >= n ? co[a] + 2 - n : co[a] + 2;
+    const AxisQ<R> qm2 = axis_q<R>(Q, base + (size_t)im2 * st[a], a, k);
+    const AxisQ<R> qm1 = axis_q<R>(Q, base + (size_t)im1 * st[a], a, k);
+    const AxisQ<R> qp1 = axis_q<R>(Q, base + (size_t)ip1 * st[a], a, k);
+    const AxisQ<R> qp2 = axis_q<R>(Q, base + (size_t)ip2 * st[a], a, k);
+    dm[a] = d4<R>(qm2.m, qm1.m, qp1.m, qp2.m, k);
+    dv[a] = d4<R>(qm2.v, qm1.v, qp1.v, qp2.v, k);
+    dP[a] = d4<R>(qm2.P, qm1.P, qp1.P, qp2.P, k);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dBB[a][i] = d4<R>(qm2.BB[i], qm1.BB[i], qp1.BB[i], qp2.BB[i], k);
+      dE[i][a] = d4<R>(qm2.E[i], qm1.E[i], qp1.E[i], qp2.E[i], k);
+    }
+    ds[a] = d4<R>(qm2.s, qm1.s, qp1.s, qp2.s, k);
+    dB[a] = d4<R>(qm2.B, qm1.B, qp1.B, qp2.B, k);
+  }
+  const R dn = ld<R>(Q.p[0], c);
+  const R v[3] = {ld<R>(Q.p[1], c), ld<R>(Q.p[2], c), ld<R>(Q.p[3], c)};
+  const R Psi = ld<R>(Q.p[8], c);
+  const R dens = k.dens0 + dn;
+  R f[NF];
+  f[0] = -(((dm[0]) + (dm[1])) + (dm[2]));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const R A = ((v[0] * dv[i]) + (v[1] * dv[i])) + (v[2] * dv[i]);
+    const R Y = ((dBB[0][i]) + (dBB[1][i])) + (dBB[2][i]);
+    f[1 + i] = ((-A) - vdiv(dP[i], dens)) + vdiv(k.c4 * Y, dens);
+    f[4 + i] = ((dE[i][0]) + (dE[i][1])) + (dE[i][2]);
+  }
+  f[7] = ((v[0] * ds[0]) + (v[1] * ds[1])) + (v[2] * ds[2]);
+  const R divB = ((dB[0]) + (dB[1])) + (dB[2]);
+  f[8] = (-(k.c_h2 * divB)) - (k.ch2_cp2 * Psi);
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+    reinterpret_cast<R *>(O.p[q])[c] = ld<R>(S.p[q], c) + (k.dt_c * f[q]);
+}
+
+// `<%` of three: fmin(0, fmax(a, fmax(b, c))) + fmax(0, fmin(a, fmin(b, c)))
+template <typename R>
+__device__ __forceinline__ R minmod3(R a, R b, R c) {
+  return vmin(R(0), vmax(a, vmax(b, c))) + vmax(R(0), vmin(a, vmin(b, c)));
+}
+
+template <typename R>
+__device__ __forceinline__ R slope(R um, R u0, R up) {
+  return minmod3<R>((up - um) / R(2), R(1.4) * (up - u0), R(1.4) * (u0 - um));
+}
+
+template <typename R>
+__device__ __forceinline__ R av_flux(R num, R den) {
+  const R nd = num * den;
+  const R r = vdiv(num, den);
+  const R t = R(0.75) * (r - R(1));
+  const R phi1 = vmin(R(1), vmax(R(0), R(1) + t));
+  const R Phi = (nd <= R(0)) ? R(0) : phi1;
+  return -((R(0.15) * Phi) * num);
+}
+
+// flux at the face between u0 and u1, given u[-1], u0, u1, u[+2]
+template <typename R>
+__device__ __forceinline__ R face(R um, R u0, R u1, R u2) {
+  const R ul = u0 + (R(0.5) * slope<R>(um, u0, u1));
+  const R ur = u1 - (R(0.5) * slope<R>(u0, u1, u2));
+  return av_flux<R>(ur - ul, u1 - u0);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128)
+    mhd_finish(Fields N, Fields S, int n, MhdC<R> k) {
+  const int z = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int y = blockIdx.y * 4 + (threadIdx.x >> 5);
+  const int x = blockIdx.z;
+  if (z >= n || y >= n) return;
+  const size_t sx = (size_t)n * n, sy = (size_t)n;
+  const size_t c = (size_t)x * sx + (size_t)y * sy + z;
+  const int co[3] = {x, y, z};
+  const size_t st[3] = {sx, sy, 1};
+  size_t off[3][5];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const size_t base = c - (size_t)co[a] * st[a];
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      int q = co[a] + d;
+      q = q < 0 ? q + n : (q >= n ? q - n : q);
+      off[a][d + 2] = base + (size_t)q * st[a];
+    }
+  }
+  R nv[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    R w = ld<R>(N.p[f], c);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const R u[5] = {ld<R>(N.p[f], off[a][0]), ld<R>(N.p[f], off[a][1]), ld<R>(N.p[f], off[a][2]),
+                      ld<R>(N.p[f], off[a][3]), ld<R>(N.p[f], off[a][4])};
+      const R fm = face<R>(u[0], u[1], u[2], u[3]);  // avf[i-1/2]
+      const R fp = face<R>(u[1], u[2], u[3], u[4]);  // avf[i+1/2]
+      w = (w + fm) - fp;
+    }
+    nv[f] = w;
+  }
+  // numerical_heat (3d-mhd-rk4.fmr:141-143), always in FP64; dens = the
+  // step's input density perturbation.
+  const double r1 = ld<R>(N.p[1], c), r2 = ld<R>(N.p[2], c), r3 = ld<R>(N.p[3], c);
+  const double b1 = ld<R>(N.p[4], c), b2 = ld<R>(N.p[5], c), b3 = ld<R>(N.p[6], c);
+  const double n1 = nv[1], n2 = nv[2], n3 = nv[3], m1 = nv[4], m2 = nv[5], m3 = nv[6];
+  const double svr = ((r1 * r1) + (r2 * r2)) + (r3 * r3);
+  const double svn = ((n1 * n1) + (n2 * n2)) + (n3 * n3);
+  const double sbr = ((b1 * b1) + (b2 * b2)) + (b3 * b3);
+  const double sbn = ((m1 * m1) + (m2 * m2)) + (m3 * m3);
+  // S is written below, so it is read through the coherent path (not __ldg)
+  const double dens_in = reinterpret_cast<const R *>(S.p[0])[c];
+  const double den8 = (8.0 * 3.141592653589793) * (1.0 + dens_in);
+  const double heat = (0.5 * (svr - svn)) + (__ddiv_rn(1.0, den8) * (sbr - sbn));
+  reinterpret_cast<R *>(S.p[0])[c] = vmax(nv[0], R(-0.9));
+#pragma unroll
+  for (int f = 1; f < NF; ++f)
+    if (f != 7) reinterpret_cast<R *>(S.p[f])[c] = nv[f];
+  reinterpret_cast<R *>(S.p[7])[c] = (R)((double)nv[7] + heat);
+}
+
+// Conserved totals in FP64: mass perturbation, kinetic + magnetic energy,
+// s, and the x-momentum; fixed tree as in fm_reduce.cu.
+template <typename R>
+__global__ void __launch_bounds__(256)
+    mhd_totals_stage1(Fields S, long long ncell, long long chunk, double *partials) {
+  __shared__ double sh[4][256];
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(lo + chunk, ncell);
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const double c8 = 1.0 / (8.0 * 3.141592653589793);
+  for (long long i = lo + threadIdx.x; i < hi; i += 256) {
+    const double d = 1.0 + (double)ld<R>(S.p[0], i);
+    const double v0 = ld<R>(S.p[1], i), v1 = ld<R>(S.p[2], i), v2 = ld<R>(S.p[3], i);
+    const double B0 = ld<R>(S.p[4], i), B1 = ld<R>(S.p[5], i), B2 = ld<R>(S.p[6], i);
+    acc[0] = acc[0] + (double)ld<R>(S.p[0], i);
+    acc[1] = acc[1] + (0.5 * d * (v0 * v0 + v1 * v1 + v2 * v2) + c8 * (B0 * B0 + B1 * B1 + B2 * B2));
+    acc[2] = acc[2] + (double)ld<R>(S.p[7], i);
+    acc[3] = acc[3] + d * v0;
+  }
+  for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] = sh[q][threadIdx.x] + sh[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) partials[(size_t)blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(256) mhd_totals_stage2(int g, const double *partials, double *out) {
+  __shared__ double sh[4][256];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < g; i += 256)
+    for (int q = 0; q < 4; ++q) acc[q] = acc[q] + partials[(size_t)i * 4 + q];
+  for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] = sh[q][threadIdx.x] + sh[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+template <typename R>
+MhdC<R> make_consts(int n, double coef) {
+  // 3d-mhd-rk4.fmr:4-11 evaluated in double as the generated code does
+  const double NX = n;
+  const double pi = 3.141592653589793;
+  const double dt = 0.1 / fmax(NX, fmax(NX, NX));
+  const double dx = 1.0 / NX;
+  const double c_h = dx / dt;
+  MhdC<R> k;
+  k.dt_c = (R)coef;
+  k.h12 = (R)(12.0 * dx);
+  k.c_h2 = (R)(c_h * c_h);
+  k.ch2_cp2 = (R)(c_h / 0.18);
+  k.c8 = (R)(1.0 / (8.0 * pi));
+  k.c4 = (R)(1.0 / (4.0 * pi));
+  k.dp_ddens = (R)1.0;
+  k.dp_ds = (R)(2.0 / 5.0);
+  k.dens0 = (R)1.0;
+  k.h12d = fm::make_div_const(12.0 * dx);
+  k.h12f = (float)(12.0 * dx);
+  k.rh12f = 1.0f / k.h12f;
+  return k;
+}
+
+template <typename R>
+int mhd_forward(int n, R *const *fields, R *work, int steps, cudaStream_t s) {
+  const size_t cells = (size_t)n * n * n;
+  Fields S, A, B;
+  for (int f = 0; f < NF; ++f) {
+    S.p[f] = fields[f];
+    A.p[f] = work + (size_t)f * cells;
+    B.p[f] = work + (size_t)(NF + f) * cells;
+  }
+  const double NX = n;
+  const double dt = 0.1 / fmax(NX, fmax(NX, NX));
+  const MhdC<R> k4 = make_consts<R>(n, dt / 4.0), k3 = make_consts<R>(n, dt / 3.0),
+                k2 = make_consts<R>(n, dt / 2.0), k1 = make_consts<R>(n, dt);
+  const dim3 grid((n + 31) / 32, (n + 3) / 4, n);
+  for (int i = 0; i < steps; ++i) {
+    mhd_stage<R><<<grid, 128, 0, s>>>(S, S, A, n, k4);
+    mhd_stage<R><<<grid, 128, 0, s>>>(A, S, B, n, k3);
+    mhd_stage<R><<<grid, 128, 0, s>>>(B, S, A, n, k2);
+    mhd_stage<R><<<grid, 128, 0, s>>>(A, S, B, n, k1);
+    mhd_finish<R><<<grid, 128, 0, s>>>(B, S, n, k1);
+  }
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+
+template <typename R>
+int mhd_totals(int n, R *const *fields, double *partials, double *out, cudaStream_t s) {
+  Fields S;
+  for (int f = 0; f < NF; ++f) S.p[f] = fields[f];
+  const long long cells = (long long)n * n * n;
+  const int g = (int)std::max<long long>(1, std::min<long long>((cells + 4095) / 4096, 1024));
+  const long long chunk = (cells + g - 1) / g;
+  mhd_totals_stage1<R><<<g, 256, 0, s>>>(S, cells, chunk, partials);
+  mhd_totals_stage2<<<1, 256, 0, s>>>(g, partials, out);
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+
+}  // namespace
+
+extern "C" int fm_mhd_forward_f64(int n, double *const fields[9], double *work, int steps,
+                                  void *stream) {
+  FM_CHECK_ARG(fields && work && n >= 5 && steps >= 0,
+               "fm_mhd_forward_f64: need n >= 5, fields, work, steps >= 0");
+  for (int f = 0; f < NF; ++f) FM_CHECK_ARG(fields[f], "fm_mhd_forward_f64: field %d is NULL", f);
+  if (steps == 0) return FM_OK;
+  return mhd_forward<double>(n, fields, work, steps, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int fm_mhd_forward_f32(int n, float *const fields[9], float *work, int steps,
+                                  void *stream) {
+  FM_CHECK_ARG(fields && work && n >= 5 && steps >= 0,
+               "fm_mhd_forward_f32: need n >= 5, fields, work, steps >= 0");
+  for (int f = 0; f < NF; ++f) FM_CHECK_ARG(fields[f], "fm_mhd_forward_f32: field %d is NULL", f);
+  if (steps == 0) return FM_OK;
+  return mhd_forward<float>(n, fields, work, steps, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" size_t fm_mhd_totals_scratch_elems(int n) {
+  const long long cells = (long long)n * n * n;
+  return 4 * (size_t)std::max<long long>(1, std::min<long long>((cells + 4095) / 4096, 1024));
+}
+
+extern "C" int fm_mhd_totals(int n, int fp64, void *const fields[9], double *partials,
+                             double *out_device, void *stream) {
+  FM_CHECK_ARG(fields && partials && out_device && n >= 1, "fm_mhd_totals: bad arguments");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (fp64) return mhd_totals<double>(n, reinterpret_cast<double *const *>(fields), partials, out_device, s);
+  return mhd_totals<float>(n, reinterpret_cast<float *const *>(fields), partials, out_device, s);
+}

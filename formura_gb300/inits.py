@@ -97,3 +97,47 @@ def gs2d_ensemble_state(sizes, seed: int = 1, dtype=np.float32):
         us.append(u.reshape(-1))
         vs.append(v.reshape(-1))
     return np.concatenate(us).astype(dtype), np.concatenate(vs).astype(dtype)
+
+
+MHD_FIELDS = ("dens", "vx", "vy", "vz", "Bx", "By", "Bz", "s", "Psi")
+
+
+def _random_modes(n: int, seed: int, kmax: float, offset: int) -> np.ndarray:
+    """A real periodic field on [0,1)^3 (n^3 grid) made of all Fourier modes
+    with 0 < |k| <= kmax (integer wavenumbers), unit amplitude and seeded
+    random phases, normalised to unit rms."""
+    k = np.fft.fftfreq(n, 1.0 / n)
+    kx, ky, kz = np.meshgrid(k, k, k[: n // 2 + 1], indexing="ij")
+    kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    mask = (kk > 0) & (kk <= kmax)
+    spec = np.zeros(kk.shape, dtype=np.complex128)
+    m = int(mask.sum())
+    ph = uniform(seed, m, offset=offset) * 2.0 * np.pi
+    spec[mask] = np.exp(1j * ph)
+    f = np.fft.irfftn(spec, s=(n, n, n), axes=(0, 1, 2))
+    return f / np.sqrt(np.mean(f ** 2))
+
+
+def _d4(a: np.ndarray, axis: int, n: int) -> np.ndarray:
+    """The 4th-order central difference of 3d-mhd-rk4.fmr:13-15 (dx = 1/n)."""
+    r = lambda s: np.roll(a, -s, axis)  # noqa: E731  (value at i+s)
+    return (((r(-2) + 8.0 * r(1)) - 8.0 * r(-1)) - r(2)) / (12.0 * (1.0 / n))
+
+
+def mhd_3d(n: int, seed: int = 1, amp: float = 1e-2, kmax: float = 4.0):
+    """Initial state of the 3D MHD workload: rho = 1, p = 1 (dens = 0, s = 0
+    for the linearised EOS p = dens0 + dens + 0.4 s of 3d-mhd-rk4.fmr:94),
+    Psi = 0, velocity and magnetic perturbations of rms amplitude `amp` with
+    random phases over wavenumbers 0 < |k| <= kmax.  B is the discrete curl of
+    a random vector potential taken with the program's own 4th-order
+    difference, so its discrete divergence vanishes (up to rounding).
+    Returns the 9 fields as float64 arrays [n][n][n]."""
+    v = [amp * _random_modes(n, seed, kmax, offset=1000003 * c) for c in range(3)]
+    A = [_random_modes(n, seed + 7, kmax, offset=1000003 * (c + 3)) for c in range(3)]
+    B = [_d4(A[2], 1, n) - _d4(A[1], 2, n),
+         _d4(A[0], 2, n) - _d4(A[2], 0, n),
+         _d4(A[1], 0, n) - _d4(A[0], 1, n)]
+    rms = np.sqrt(np.mean(B[0] ** 2 + B[1] ** 2 + B[2] ** 2) / 3.0)
+    B = [amp * b / rms for b in B]
+    z = np.zeros((n, n, n))
+    return [z.copy(), v[0], v[1], v[2], B[0], B[1], B[2], z.copy(), z.copy()]

@@ -186,3 +186,41 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+MHD_NFIELDS = 9
+
+
+def _mhd_ptrs(fields, dtype, n):
+    if len(fields) != MHD_NFIELDS:
+        raise ValueError("9 MHD fields expected (dens, vx, vy, vz, Bx, By, Bz, s, Psi)")
+    return (ctypes.c_void_p * MHD_NFIELDS)(
+        *[_need(f, dtype, (n, n, n), "field %d" % i).value for i, f in enumerate(fields)])
+
+
+def mhd_forward(fields, work, steps: int, stream=None):
+    """Advance the 9 MHD fields (float64: all-FP64 path; float32: binary32 bulk
+    with the FP64 energy update) by `steps` time steps of 3d-mhd-rk4.fmr."""
+    n = int(fields[0].shape[0])
+    dtype = fields[0].dtype
+    if dtype not in (torch.float64, torch.float32):
+        raise ValueError("MHD fields must be float64 or float32")
+    ptrs = _mhd_ptrs(fields, dtype, n)
+    w = _need(work, dtype, (18 * n ** 3,), "work")
+    fn = lib().fm_mhd_forward_f64 if dtype == torch.float64 else lib().fm_mhd_forward_f32
+    check(fn(n, ptrs, w, int(steps), ctypes.c_void_p(_stream_ptr(stream))), "fm_mhd_forward")
+
+
+def mhd_totals(fields, stream=None):
+    """FP64 totals (mass, kinetic+magnetic energy, sum s, x-momentum) as a
+    4-element float64 CUDA tensor."""
+    n = int(fields[0].shape[0])
+    dtype = fields[0].dtype
+    ptrs = _mhd_ptrs(fields, dtype, n)
+    part = torch.empty(int(lib().fm_mhd_totals_scratch_elems(n)), dtype=torch.float64,
+                       device=fields[0].device)
+    out = torch.empty(4, dtype=torch.float64, device=fields[0].device)
+    check(lib().fm_mhd_totals(n, 1 if dtype == torch.float64 else 0, ptrs,
+                              ctypes.c_void_p(part.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                              ctypes.c_void_p(_stream_ptr(stream))), "fm_mhd_totals")
+    return out

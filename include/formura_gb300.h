@@ -171,6 +171,39 @@ int fm_gs2d_ensemble_forward(fm_ensemble *e, float *U, float *V, float *work_U,
 int fm_gs2d_ensemble_status(fm_ensemble *e, void *stream);
 int fm_gs2d_ensemble_destroy(fm_ensemble *e);
 
+/* ---- 3D MHD ----------------------------------------------------------------- */
+
+/*
+ * Time steps of the reference program examples/3d-mhd-rk4.fmr: 9 fields
+ * (dens = perturbation of dens0 = 1, vx, vy, vz, Bx, By, Bz, s, Psi), each
+ * an [n][n][n] device array, periodic, dx = 1/n, dt = 0.1/n as the program
+ * defines them.  Per step: four manifested low-storage Runge-Kutta stages
+ * (q4 = S + dt/4 f(S), q3 = S + dt/3 f(q4), q2 = S + dt/2 f(q3),
+ * next = S + dt f(q2); f = ddt_sys with 4th-order central differences,
+ * 3d-mhd-rk4.fmr:83-110), then the artificial-viscosity fluxes of `next`
+ * along x, y, z applied in turn, dens floored at -0.9, and
+ * s += numerical_heat (3d-mhd-rk4.fmr:112-145).  `work` holds 18*n^3
+ * elements.  Replaces the Computation loop nests of that program's
+ * Formura_Forward (src/Formura/MPICxx/Translate.hs:671-737).
+ *
+ * fm_mhd_forward_f64: all-FP64, bit-exact with the generated DAG.
+ * fm_mhd_forward_f32: the bulk in binary32; the numerical-heat (energy)
+ * update of s in FP64.  Requires n >= 5.
+ */
+int fm_mhd_forward_f64(int n, double *const fields[9], double *work, int steps,
+                       void *stream);
+int fm_mhd_forward_f32(int n, float *const fields[9], float *work, int steps,
+                       void *stream);
+/*
+ * FP64 conserved totals of an MHD state into out_device[0..3]: sum of dens,
+ * sum of (1/2 (1+dens)|v|^2 + |B|^2/(8 pi)), sum of s, sum of (1+dens) vx.
+ * fp64 != 0: fields are double, else float.  `partials` holds
+ * fm_mhd_totals_scratch_elems(n) doubles.  Deterministic for a given n.
+ */
+size_t fm_mhd_totals_scratch_elems(int n);
+int fm_mhd_totals(int n, int fp64, void *const fields[9], double *partials,
+                  double *out_device, void *stream);
+
 /* ---- 2D diffusion --------------------------------------------------------- */
 
 /*

@@ -72,6 +72,12 @@ void fo_gs3d_run_f32k_fast(int nx, int ny, int nz, float *U, float *V,
                            float *cU, float *cV, int steps, double F, double k,
                            double Du, double Dv, double dt, double dx);
 
+/* One-or-more time steps of examples/3d-mhd-rk4.fmr in double (fmr_mhd.c).
+ * fields[0..8] = dens, vx, vy, vz, Bx, By, Bz, s, Psi, each [nx][ny][nz],
+ * advanced in place.  dx = 1/nx and dt = 0.1/max(n) as the program defines
+ * them (a cubic grid, nx = ny = nz, is assumed for dx = dy = dz). */
+void fo_mhd_run_f64(int nx, int ny, int nz, double *const fields[9], int steps);
+
 /* Plain left-to-right double sum (conserved-total check). */
 double fo_sum_f64(int64_t n, const double *a);
 

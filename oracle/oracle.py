@@ -50,6 +50,7 @@ def _load(name: str) -> ctypes.CDLL:
     h.fo_gs3d_run_f64.argtypes = [i, i, i, P, P, i, ctypes.POINTER(GsParams)]
     h.fo_gs3d_run_f32_kahan.argtypes = [i, i, i, P, P, P, P, i, f, f, f, f, f, f]
     h.fo_gs3d_run_f32k_fast.argtypes = [i, i, i, P, P, P, P, i, d, d, d, d, d, d]
+    h.fo_mhd_run_f64.argtypes = [i, i, i, ctypes.POINTER(P), i]
     h.fo_sum_f64.argtypes = [ctypes.c_int64, P]
     h.fo_sum_f64.restype = d
     h.fo_num_threads.restype = i
@@ -112,6 +113,16 @@ def gs3d_f32k_fast(U, V, cU, cV, steps, F, k, Du, Dv, dt, dx, fast=False):
     lib(fast).fo_gs3d_run_f32k_fast(nx, ny, nz, *[_ptr(a) for a in arrs], int(steps),
                                     float(F), float(k), float(Du), float(Dv), float(dt), float(dx))
     return tuple(arrs)
+
+
+def mhd_f64(fields, steps, fast=False):
+    """examples/3d-mhd-rk4.fmr steps in double; fields = 9 arrays [n][n][n]
+    (dens, vx, vy, vz, Bx, By, Bz, s, Psi).  Returns new arrays."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64).copy() for a in fields]
+    nx, ny, nz = arrs[0].shape
+    ptrs = (ctypes.c_void_p * 9)(*[a.ctypes.data for a in arrs])
+    lib(fast).fo_mhd_run_f64(nx, ny, nz, ptrs, int(steps))
+    return arrs
 
 
 def num_threads(fast: bool = False) -> int:
