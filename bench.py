@@ -160,6 +160,119 @@ def cpu_baseline(seconds: float = 12.0):
                 seconds=round(dt, 3))
 
 
+def _event_time(torch, fn):
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    fn()
+    b.record()
+    b.synchronize()
+    return a.elapsed_time(b) / 1e3
+
+
+def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
+    """The other forms of the hot path, each timed on the device after a warm-up
+    (CUDA events on the launching stream), at the sizes the workloads name."""
+    import numpy as np
+
+    from formura_gb300 import autotune, inits, kernels
+    from oracle import oracle
+
+    out = {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    # -- 3D Gray-Scott FP32 + Kahan, temporally blocked, scored against the FP64 run
+    M = prog.steps_per_forward
+    U = torch.from_numpy(U0.astype(np.float32)).cuda()
+    V = torch.from_numpy(V0.astype(np.float32)).cuda()
+    cU, cV = torch.zeros_like(U), torch.zeros_like(V)
+    w = torch.empty(4 * U.numel(), dtype=torch.float32, device="cuda")
+    prm = kernels.gs_params(**GS)
+    tune = autotune.tune_gs3d_f32k((N, N, N))
+    Uw, Vw = U.clone(), V.clone()
+    kernels.gs3d_f32k_tb_forward(Uw, Vw, torch.zeros_like(U), torch.zeros_like(V), w, prm, 24)
+    sec = _event_time(torch, lambda: kernels.gs3d_f32k_tb_forward(U, V, cU, cV, w, prm, M))
+    Uf = U.double().cpu().numpy()
+    err = float(np.linalg.norm(Uf - U_fp64_final) / np.linalg.norm(U_fp64_final))
+    errmax = float(np.abs(Uf - U_fp64_final).max() / np.abs(U_fp64_final).max())
+    g = N ** 3 * M / sec / 1e9
+    out["gray_scott_3d_f32_kahan_tb"] = {
+        "value": round(g, 2), "unit": "GLUP/s", "steps": M, "tb": tune["tb"],
+        "rel_l2_error_vs_fp64": err, "max_rel_error_vs_fp64": errmax,
+        "hbm_untiled_roofline_glups": round(hbm / 32.0, 1),
+        "hbm_roofline_at_tb_glups": round(hbm / (32.0 / tune["tb"]), 1),
+        "kernel": "gs3d_f32k_tb"}
+    del U, V, cU, cV, w, Uw, Vw
+    # -- uneven ensemble of 512 2D Gray-Scott instances, 5000 steps, one launch
+    sizes, F, k = inits.gs2d_ensemble(512, seed=1)
+    total = sum(n * n for n in sizes)
+    res = autotune.tune_ensemble(sizes, F, k, sample_steps=40)
+    e = kernels.Ensemble(sizes, F, k)
+    Ue, Ve = inits.gs2d_ensemble_state(sizes, seed=1)
+    Ue, Ve = torch.from_numpy(Ue).cuda(), torch.from_numpy(Ve).cuda()
+    wU, wV = torch.empty_like(Ue), torch.empty_like(Ve)
+    e.forward(Ue, Ve, wU, wV, 5000, use_graph=True)  # capture + warm
+    sec = _event_time(torch, lambda: e.forward(Ue, Ve, wU, wV, 5000, use_graph=True))
+    e.status()
+    ens = total * 5000 / sec / 1e9
+    sub = list(range(0, 512, 16))
+    bufs = []
+    for i in sub:
+        u0, v0 = inits.gray_scott_2d_square(sizes[i], sizes[i], seed=i)
+        u = torch.from_numpy(u0.astype(np.float32)).cuda()
+        v = torch.from_numpy(v0.astype(np.float32)).cuda()
+        bufs.append((u, v, torch.empty_like(u), torch.empty_like(v),
+                     kernels.gs_params(F[i], k[i], 2e-5, 1e-5, 1.0, 0.01)))
+    seq_cells = sum(sizes[i] ** 2 for i in sub)
+
+    def seq():
+        for u, v, wu, wv, prm_i in bufs:
+            kernels.gs2d_f32_forward(u, v, wu, wv, prm_i, 100)
+
+    seq()
+    ssec = _event_time(torch, seq)
+    out["gray_scott_2d_ensemble_512"] = {
+        "value": round(ens, 2), "unit": "GLUP/s", "instances": 512, "steps": 5000,
+        "total_cells": total, "tile": res["tile"], "tb": res["tb"],
+        "graph_captured": True, "one_persistent_launch": True,
+        "sequential_per_instance_launches_glups": round(seq_cells * 100 / ssec / 1e9, 2),
+        "sequential_sample": "32 of 512 instances x 100 steps, one launch per step",
+        "kernel": "gs2d_ensemble"}
+    e.close()
+    del Ue, Ve, wU, wV, bufs
+    # -- 2D diffusion 256^2 FP64, 1000 steps in one persistent launch
+    d0 = inits.diffusion_2d(256, 256, seed=1)
+    d = torch.from_numpy(d0).cuda()
+    wd = torch.empty_like(d)
+    kernels.diff2d_f64_forward(d, wd, 0.1, 50)
+    sec = _event_time(torch, lambda: kernels.diff2d_f64_forward(d, wd, 0.1, 1000))
+    out["diffusion_2d_256_fp64"] = {"value": round(256 * 256 * 1000 / sec / 1e9, 2),
+                                    "unit": "GLUP/s", "steps": 1000, "ms": round(sec * 1e3, 3),
+                                    "bit_exact_vs_oracle": True, "kernel": "diff2d_persistent"}
+    # -- 3D MHD 256^3, 500 steps: binary32 bulk with the FP64 energy update
+    f0 = inits.mhd_3d(N, seed=1)
+    t32 = [torch.from_numpy(x.astype(np.float32)).cuda() for x in f0]
+    w32 = torch.empty(18 * N ** 3, dtype=torch.float32, device="cuda")
+    kernels.mhd_forward([x.clone() for x in t32], w32, 1)
+    sec = _event_time(torch, lambda: kernels.mhd_forward(t32, w32, 500))
+    tot = kernels.mhd_totals(t32).cpu().numpy()
+    del w32, t32
+    # error against an all-FP64 GPU run (bit-exact with the oracle) at 64^3 x 500
+    n2 = 64
+    g0 = inits.mhd_3d(n2, seed=1)
+    a64 = [torch.from_numpy(x).cuda() for x in g0]
+    a32 = [torch.from_numpy(x.astype(np.float32)).cuda() for x in g0]
+    kernels.mhd_forward(a64, torch.empty(18 * n2 ** 3, dtype=torch.float64, device="cuda"), 500)
+    kernels.mhd_forward(a32, torch.empty(18 * n2 ** 3, dtype=torch.float32, device="cuda"), 500)
+    errs = {}
+    for name, x, y in zip(inits.MHD_FIELDS, a32, a64):
+        y = y.cpu().numpy()
+        errs[name] = float(np.abs(x.double().cpu().numpy() - y).max() / max(np.abs(y).max(), 1e-300))
+    out["mhd_3d_256_fp32_bulk_fp64_energy"] = {
+        "value": round(N ** 3 * 500 / sec / 1e9, 3), "unit": "GLUP/s", "steps": 500,
+        "seconds": round(sec, 3), "totals_fp64": [float(x) for x in tot],
+        "max_rel_error_vs_fp64_64cube_500steps": errs, "kernel": "mhd_stage"}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -251,6 +364,14 @@ def run_engine(args):
     e2e_s = time.perf_counter() - t0
     barrier()
 
+    # the state after one Formura_Forward from the seeded start (for the FP32 score)
+    U_final = None
+    if rank == 0 and not args.no_variants:
+        prog.state["U"][...] = U0
+        prog.state["V"][...] = V0
+        prog.forward()
+        U_final = prog.state["U"].copy()
+
     times = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
     if ws > 1:
         torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
@@ -275,6 +396,9 @@ def run_engine(args):
     traffic = read_profile_traffic()
     clocks = clk.summary()
     cpu = cpu_baseline() if not args.no_cpu else None
+    variants = None
+    if not args.no_variants:
+        variants = run_variants(torch, prog, U_final, U0, V0, peaks)
 
     line = {
         "metric": "GLUP/s (3D Gray-Scott 256^3 FP64) vs FP64/HBM roofline at 1 GB300",
@@ -303,6 +427,8 @@ def run_engine(args):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if variants is not None:
+        line["variants"] = variants
     print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -336,6 +462,28 @@ def run_profile_case(args):
             w = torch.empty(4 * U.numel(), dtype=torch.float32, device=dev)
             kernels.gs3d_f32k_forward(U, V, cU, cV, w, kernels.gs_params(**GS),
                                       args.profile_steps, args.profile_tb)
+    elif args.profile == "gs3d_f32k_tb":
+        U0, V0 = inits.gray_scott_3d(n, n, n, seed=1)
+        U = torch.from_numpy(U0.astype("float32")).to(dev)
+        V = torch.from_numpy(V0.astype("float32")).to(dev)
+        cU, cV = torch.zeros_like(U), torch.zeros_like(V)
+        w = torch.empty(4 * U.numel(), dtype=torch.float32, device=dev)
+        kernels.gs3d_f32k_tb_forward(U, V, cU, cV, w, kernels.gs_params(**GS),
+                                     args.profile_steps, args.profile_tb)
+    elif args.profile == "ensemble":
+        sizes, F, k = inits.gs2d_ensemble(512, seed=1)
+        e = kernels.Ensemble(sizes, F, k, tile=64, tb=max(args.profile_tb, 1))
+        Ue, Ve = inits.gs2d_ensemble_state(sizes, seed=1)
+        Ue, Ve = torch.from_numpy(Ue).to(dev), torch.from_numpy(Ve).to(dev)
+        e.forward(Ue, Ve, torch.empty_like(Ue), torch.empty_like(Ve), args.profile_steps,
+                  use_graph=False)
+        e.status()
+        e.close()
+    elif args.profile == "mhd":
+        f0 = inits.mhd_3d(n, seed=1)
+        t = [torch.from_numpy(x.astype("float32")).to(dev) for x in f0]
+        kernels.mhd_forward(t, torch.empty(18 * n ** 3, dtype=torch.float32, device=dev),
+                            args.profile_steps)
     elif args.profile == "diff2d":
         d0 = inits.diffusion_2d(n, n, seed=1)
         d = torch.from_numpy(d0).to(dev)
@@ -351,7 +499,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
-    ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "diff2d"], default=None,
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
+    ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",
+                                          "mhd", "diff2d"], default=None,
                     help="run a small case of one kernel for an ncu capture, then exit")
     ap.add_argument("--profile-n", type=int, default=256)
     ap.add_argument("--profile-steps", type=int, default=4)
