@@ -419,7 +419,7 @@ def run_engine(args):
                              "frac": round(achieved_gbs / hbm_peak, 4),
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
                      "fp32_peak_tflops": round(fp32_peak, 2),
-                     "kernel": "gs3d_f64_step", "ms_per_launch": round(per_launch * 1e3, 4)},
+                     "kernel": "gs3d_f64_row", "ms_per_launch": round(per_launch * 1e3, 4)},
         "e2e": {"value": round(e2e, 4), "unit": "GLUP/s",
                 "h2d_bytes_per_step": 2 * 8 * N ** 3, "d2h_bytes_per_step": 2 * 8 * N ** 3},
         "gpu_launches": 2 * launches,
