@@ -73,6 +73,8 @@ SIGNATURES = {
     "fm_mhd_totals_scratch_elems": (c_size_t, [c_int]),
     "fm_mhd_totals": (c_int, [c_int, c_int, ctypes.POINTER(c_void_p), c_void_p, c_void_p,
                               c_void_p]),
+    "fm_tc_gemm_bf16": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_void_p]),
     "fm_sum_f64_scratch_elems": (c_size_t, [c_int64]),
     "fm_sum_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f32_as_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),

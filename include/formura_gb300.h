@@ -204,6 +204,19 @@ size_t fm_mhd_totals_scratch_elems(int n);
 int fm_mhd_totals(int n, int fp64, void *const fields[9], double *partials,
                   double *out_device, void *stream);
 
+/* ---- tensor-core building block ---------------------------------------------- */
+
+/*
+ * C[M x N] (fp32, row-major) = A[M x K] * B[N x K]^T with A, B row-major
+ * bf16 (16-byte aligned), on the tcgen05 tensor cores with FP32 accumulation
+ * in tensor memory.  No counterpart in the reference (it has no GPU code);
+ * the building block of the learned surrogate's convolutions.
+ * M % 128 == 0, N % 64 == 0, K % 64 == 0.  *err_device (an int the caller
+ * zeroes) becomes 1 if a bounded wait on the tensor core gave up.
+ */
+int fm_tc_gemm_bf16(int M, int N, int K, const void *A, const void *B, float *C,
+                    int *err_device, void *stream);
+
 /* ---- 2D diffusion --------------------------------------------------------- */
 
 /*
