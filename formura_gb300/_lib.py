@@ -75,6 +75,23 @@ SIGNATURES = {
                               c_void_p]),
     "fm_tc_gemm_bf16": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
                                 c_void_p]),
+    "fm_conv3x3_fwd_bf16": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p]),
+    "fm_conv3x3_wgrad_bf16": (c_int, [c_int, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p]),
+    "fm_sur_pack": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                            c_void_p]),
+    "fm_sur_unpack": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, ctypes.c_float,
+                              c_void_p]),
+    "fm_sur_loss_grad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p, ctypes.c_float, ctypes.c_float, c_void_p]),
+    "fm_sur_bias_grad": (c_int, [c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "fm_sur_flip": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "fm_sur_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                            c_void_p, c_void_p, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                            ctypes.c_float, c_int, c_int, c_void_p]),
+    "fm_sur_gelu_bwd": (c_int, [ctypes.c_longlong, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f64_scratch_elems": (c_size_t, [c_int64]),
     "fm_sum_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f32_as_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),

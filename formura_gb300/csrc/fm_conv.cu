@@ -1,0 +1,410 @@
+// fm_conv.cu — 3x3 periodic convolutions on the tcgen05 tensor cores (BF16
+// operands, FP32 accumulation in tensor memory): the layers of the learned
+// 16-step surrogate.
+//
+// Activation layout: NHWC bf16 with a one-pixel periodic halo,
+// [B][H+2][W+2][C]; the halo always holds the wrapped-around border, so a
+// 3x3 tap is a plain shifted read.  Weights: [Cout][9][Cin] bf16, tap
+// t = (dy+1)*3 + (dx+1).
+//
+// conv3x3_fwd<NT>: implicit GEMM.  M = 128 consecutive pixels (row-major over
+// B*H*W), N = Cout = NT (32 or 64), K = 9 taps x 64 input channels.  For each
+// tap the CTA gathers the 128 shifted pixel rows (128 B each) and the tap's
+// NT x 64 weight block into shared memory (K-major core-matrix layout, two
+// stages), thread 0 issues four K=16 MMAs and commits them to the stage's
+// mbarrier.  The fused epilogue reads the 128 x NT accumulator from TMEM:
+//   v = acc (+ bias) (* gelu'(gate)) (+ residual);  z_out <- v;
+//   y <- act(v) stored bf16 into the padded output (halo included) and/or
+//   fp32 unpadded.
+// One kernel thereby serves the forward layers and, with flipped/transposed
+// weights, the data gradients (see the host entry points).
+//
+// conv3x3_wgrad<NT>: dW[t][co][ci] = sum_p dY[p][co] * X[p + t][ci] as a
+// split-K GEMM: M = (tap, ci) rows (576, in 5 tiles of 128), N = co,
+// K = pixels; each CTA accumulates a pixel range in TMEM and adds its tile
+// to the fp32 gradient with atomics.
+#include <algorithm>
+
+#include "fm_common.cuh"
+#include "fm_tc.cuh"
+
+namespace {
+
+using namespace fm::tc;
+typedef __nv_bfloat16 bf16;
+
+constexpr int CIN = 64;
+constexpr int kTM = 128;
+
+__device__ __forceinline__ float gelu(float x) {
+  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+struct ConvArgs {
+  const bf16 *x;      // [B][H+2][W+2][64]
+  const bf16 *w;      // [NT][9][64]
+  const float *bias;  // [NT] or null
+  const bf16 *gate;   // padded [..][NT]: multiply by gelu'(gate) (or null)
+  const bf16 *resid;  // padded [..][NT]: add (or null)
+  bf16 *z_out;        // padded [..][NT] pre-activation (or null)
+  bf16 *y_out;        // padded [..][NT] (or null)
+  float *y_f32;       // [B][H][W][NT] (or null)
+  int B, H, W, act;   // act: 0 none, 1 GELU
+  int *err;
+};
+
+__device__ __forceinline__ size_t pad_index(int b, int py, int px, int H, int W) {
+  return ((size_t)b * (H + 2) + py) * (W + 2) + px;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(128) conv3x3_fwd(ConvArgs a) {
+  constexpr int kABytes = kTM * CIN * 2, kBBytes = NT * CIN * 2;
+  constexpr int kStage = kABytes + kBBytes;
+  extern __shared__ __align__(1024) uint8_t dsm[];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int H = a.H, W = a.W;
+  const int hw = H * W;
+  const long long p0 = (long long)blockIdx.x * kTM;
+  if (warp == 0) tmem_alloc(&s_tmem, NT < 32 ? 32 : NT);
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  const uint32_t idesc = idesc_bf16_f32(kTM, NT);
+  uint32_t ph0 = 0u, ph1 = 0u;
+  bool ok = true;
+  for (int t = 0; t < 9; ++t) {
+    const int st = t & 1;
+    if (t >= 2) {
+      if (!mbar_wait(&bar[st], st ? ph1 : ph0)) ok = false;
+      if (st) ph1 ^= 1u; else ph0 ^= 1u;
+    }
+    const int dy = t / 3 - 1, dx = t % 3 - 1;
+    uint8_t *sa = dsm + st * kStage;
+    uint8_t *sb = sa + kABytes;
+    // A: 128 shifted pixel rows x 64 channels
+    for (int v = tid; v < kTM * 8; v += 128) {
+      const int r = v >> 3, kk = (v & 7) * 8;
+      const long long p = p0 + r;
+      const int b = (int)(p / hw), rem = (int)(p % hw);
+      const int y = rem / W, xx = rem % W;
+      const bf16 *src = a.x + pad_index(b, y + 1 + dy, xx + 1 + dx, H, W) * CIN + kk;
+      *reinterpret_cast<uint4 *>(sa + kmajor_off(r, kk, CIN)) =
+          *reinterpret_cast<const uint4 *>(src);
+    }
+    // B: the tap's NT x 64 weights
+    for (int v = tid; v < NT * 8; v += 128) {
+      const int r = v >> 3, kk = (v & 7) * 8;
+      *reinterpret_cast<uint4 *>(sb + kmajor_off(r, kk, CIN)) =
+          *reinterpret_cast<const uint4 *>(a.w + ((size_t)r * 9 + t) * CIN + kk);
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after_sync();
+      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+#pragma unroll
+      for (int s = 0; s < CIN / 16; ++s)
+        mma_bf16(tmem, smem_desc(a0 + s * 256, 128, (CIN / 8) * 128),
+                 smem_desc(b0 + s * 256, 128, (CIN / 8) * 128), idesc, (t | s) != 0);
+      mma_commit(&bar[st]);
+    }
+  }
+  // the last two taps (7 -> stage 1, 8 -> stage 0)
+  if (!mbar_wait(&bar[1], ph1)) ok = false;
+  if (!mbar_wait(&bar[0], ph0)) ok = false;
+  fence_after_sync();
+  if (ok) {
+    const long long p = p0 + warp * 32 + (tid & 31);
+    const int b = (int)(p / hw), rem = (int)(p % hw);
+    const int y = rem / W, xx = rem % W;
+    // padded positions this pixel occupies: interior + periodic halo copies
+    int pys[2] = {y + 1, -1}, pxs[2] = {xx + 1, -1};
+    if (y == 0) pys[1] = H + 1;
+    if (y == H - 1) pys[1] = 0;
+    if (xx == 0) pxs[1] = W + 1;
+    if (xx == W - 1) pxs[1] = 0;
+    const size_t pin = pad_index(b, y + 1, xx + 1, H, W);
+#pragma unroll
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (a.bias) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += __ldg(a.bias + c0 + i);
+      }
+      if (a.gate) {
+        const bf16 *g = a.gate + pin * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] *= gelu_grad(__bfloat162float(g[i]));
+      }
+      if (a.resid) {
+        const bf16 *rr = a.resid + pin * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += __bfloat162float(rr[i]);
+      }
+      __align__(16) bf16 zb[16], yb[16];
+      if (a.z_out) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) zb[i] = __float2bfloat16_rn(v[i]);
+      }
+      if (a.act == 1) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) yb[i] = __float2bfloat16_rn(v[i]);
+#pragma unroll
+      for (int iy = 0; iy < 2; ++iy) {
+        if (pys[iy] < 0) continue;
+#pragma unroll
+        for (int ix = 0; ix < 2; ++ix) {
+          if (pxs[ix] < 0) continue;
+          const size_t q = pad_index(b, pys[iy], pxs[ix], H, W) * NT + c0;
+          if (a.z_out) {
+            reinterpret_cast<uint4 *>(a.z_out + q)[0] = reinterpret_cast<const uint4 *>(zb)[0];
+            reinterpret_cast<uint4 *>(a.z_out + q)[1] = reinterpret_cast<const uint4 *>(zb)[1];
+          }
+          if (a.y_out) {
+            reinterpret_cast<uint4 *>(a.y_out + q)[0] = reinterpret_cast<const uint4 *>(yb)[0];
+            reinterpret_cast<uint4 *>(a.y_out + q)[1] = reinterpret_cast<const uint4 *>(yb)[1];
+          }
+        }
+      }
+      if (a.y_f32) {
+        float *dst = a.y_f32 + (size_t)p * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[i] = v[i];
+      }
+    }
+  } else {
+    if (tid == 0) atomicExch(a.err, 1);
+    mbar_wait(&bar[0], ph0 ^ 1u);
+    mbar_wait(&bar[1], ph1 ^ 1u);
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, NT < 32 ? 32 : NT);
+}
+
+// ---------------------------------------------------------------------------
+struct WgradArgs {
+  const bf16 *x;   // [B][H+2][W+2][64]
+  const bf16 *dy;  // padded [B][H+2][W+2][NT]
+  float *dwt;      // [9][64][NT] fp32 accumulators (dW transposed)
+  int B, H, W;
+  int chunks_per_cta;  // 64-pixel K chunks per CTA
+  int *err;
+};
+
+template <int NT>
+__global__ void __launch_bounds__(128) conv3x3_wgrad(WgradArgs a) {
+  constexpr int kKC = 64;                        // pixels per K chunk
+  constexpr int kABytes = kTM * kKC * 2;         // (tap,ci) x pixels
+  constexpr int kBBytes = NT * kKC * 2;          // co x pixels
+  constexpr int kStage = kABytes + kBBytes;
+  extern __shared__ __align__(1024) uint8_t dsm[];
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int H = a.H, W = a.W, hw = H * W;
+  const long long npix = (long long)a.B * hw;
+  const int mt = blockIdx.y;  // rows 128*mt .. : taps 2mt, 2mt+1
+  const long long k_begin = (long long)blockIdx.x * a.chunks_per_cta * kKC;
+  const long long k_lim = k_begin + (long long)a.chunks_per_cta * kKC;
+  const long long k_end = npix < k_lim ? npix : k_lim;
+  const int nchunks = (int)((k_end - k_begin + kKC - 1) / kKC);
+  if (warp == 0) tmem_alloc(&s_tmem, NT < 32 ? 32 : NT);
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  const uint32_t idesc = idesc_bf16_f32(kTM, NT);
+  uint32_t ph0 = 0u, ph1 = 0u;
+  bool ok = true;
+  for (int c = 0; c < nchunks; ++c) {
+    const int st = c & 1;
+    if (c >= 2) {
+      if (!mbar_wait(&bar[st], st ? ph1 : ph0)) ok = false;
+      if (st) ph1 ^= 1u; else ph0 ^= 1u;
+    }
+    uint8_t *sa = dsm + st * kStage;
+    uint8_t *sb = sa + kABytes;
+    const long long kb = k_begin + (long long)c * kKC;
+    // A[(tl, ci)][k] = X[p_k + tap(2mt+tl)][ci]: each thread reads 8 channels of
+    // one pixel and scatters them down the column k of rows ci..ci+7.
+    for (int v = tid; v < 2 * kKC * 8; v += 128) {
+      const int tl = v / (kKC * 8);
+      const int rem = v % (kKC * 8);
+      const int k = rem >> 3, ci0 = (rem & 7) * 8;
+      const int tap = 2 * mt + tl;
+      const long long p = kb + k;
+      __align__(16) bf16 vals[8];
+      if (tap < 9 && p < k_end) {
+        const int b = (int)(p / hw), r2 = (int)(p % hw);
+        const int y = r2 / W, xx = r2 % W;
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        *reinterpret_cast<uint4 *>(vals) = *reinterpret_cast<const uint4 *>(
+            a.x + pad_index(b, y + 1 + dy, xx + 1 + dx, H, W) * CIN + ci0);
+      } else {
+        *reinterpret_cast<uint4 *>(vals) = make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        *reinterpret_cast<bf16 *>(sa + kmajor_off(tl * 64 + ci0 + i, k, kKC)) = vals[i];
+    }
+    // B[co][k] = dY[p_k][co]
+    for (int v = tid; v < kKC * (NT / 8); v += 128) {
+      const int k = v / (NT / 8), co0 = (v % (NT / 8)) * 8;
+      const long long p = kb + k;
+      __align__(16) bf16 vals[8];
+      if (p < k_end) {
+        const int b = (int)(p / hw), r2 = (int)(p % hw);
+        const int y = r2 / W, xx = r2 % W;
+        *reinterpret_cast<uint4 *>(vals) = *reinterpret_cast<const uint4 *>(
+            a.dy + pad_index(b, y + 1, xx + 1, H, W) * NT + co0);
+      } else {
+        *reinterpret_cast<uint4 *>(vals) = make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        *reinterpret_cast<bf16 *>(sb + kmajor_off(co0 + i, k, kKC)) = vals[i];
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      fence_after_sync();
+      const uint32_t a0 = smem_u32(sa), b0 = smem_u32(sb);
+#pragma unroll
+      for (int s = 0; s < kKC / 16; ++s)
+        mma_bf16(tmem, smem_desc(a0 + s * 256, 128, (kKC / 8) * 128),
+                 smem_desc(b0 + s * 256, 128, (kKC / 8) * 128), idesc, (c | s) != 0);
+      mma_commit(&bar[st]);
+    }
+  }
+  // wait for the outstanding chunks
+  if (nchunks >= 2) {
+    const int s_last = (nchunks - 1) & 1, s_prev = (nchunks - 2) & 1;
+    if (!mbar_wait(&bar[s_prev], s_prev ? ph1 : ph0)) ok = false;
+    if (s_prev) ph1 ^= 1u; else ph0 ^= 1u;
+    if (!mbar_wait(&bar[s_last], s_last ? ph1 : ph0)) ok = false;
+  } else if (nchunks == 1) {
+    if (!mbar_wait(&bar[0], ph0)) ok = false;
+  }
+  fence_after_sync();
+  if (ok && nchunks > 0) {
+    const int row = warp * 32 + (tid & 31);  // (tl, ci)
+    const int tap = 2 * mt + (row >> 6), ci = row & 63;
+#pragma unroll
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (tap < 9) {
+        float *dst = a.dwt + ((size_t)tap * 64 + ci) * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) atomicAdd(dst + i, v[i]);
+      }
+    }
+  } else if (!ok) {
+    if (tid == 0) atomicExch(a.err, 1);
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, NT < 32 ? 32 : NT);
+}
+
+template <int NT>
+int launch_fwd(const ConvArgs &a, cudaStream_t s) {
+  const int smem = 2 * (kTM * CIN * 2 + NT * CIN * 2);
+  FM_TRY_CUDA(cudaFuncSetAttribute(conv3x3_fwd<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   smem));
+  const long long npix = (long long)a.B * a.H * a.W;
+  conv3x3_fwd<NT><<<(unsigned)(npix / kTM), 128, smem, s>>>(a);
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+
+template <int NT>
+int launch_wgrad(WgradArgs a, cudaStream_t s) {
+  const int smem = 2 * (kTM * 64 * 2 + NT * 64 * 2);
+  FM_TRY_CUDA(cudaFuncSetAttribute(conv3x3_wgrad<NT>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int sms = 0;
+  int st = fm::device_sm_count(&sms);
+  if (st) return st;
+  const long long npix = (long long)a.B * a.H * a.W;
+  const long long nch = (npix + 63) / 64;
+  // about 4 CTAs per SM over the 5 row tiles
+  const long long want = std::max<long long>(1, (long long)sms * 4 / 5);
+  a.chunks_per_cta = (int)std::max<long long>(1, (nch + want - 1) / want);
+  const long long gx = (nch + a.chunks_per_cta - 1) / a.chunks_per_cta;
+  conv3x3_wgrad<NT><<<dim3((unsigned)gx, 5), 128, smem, s>>>(a);
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+
+}  // namespace
+
+extern "C" int fm_conv3x3_fwd_bf16(int B, int H, int W, int cout, const void *x_pad,
+                                   const void *w, const float *bias, const void *gate_pad,
+                                   const void *resid_pad, int act, void *z_pad_out,
+                                   void *y_pad_out, float *y_f32_out, int *err_device,
+                                   void *stream) {
+  FM_CHECK_ARG(x_pad && w && err_device, "fm_conv3x3_fwd_bf16: NULL input");
+  FM_CHECK_ARG(B >= 1 && H >= 2 && W >= 2 && ((long long)B * H * W) % kTM == 0,
+               "fm_conv3x3_fwd_bf16: B*H*W must be a multiple of 128 (got %d*%d*%d)", B, H, W);
+  FM_CHECK_ARG(cout == 32 || cout == 64, "fm_conv3x3_fwd_bf16: cout must be 32 or 64");
+  FM_CHECK_ARG(act == 0 || act == 1, "fm_conv3x3_fwd_bf16: act must be 0 or 1");
+  FM_CHECK_ARG(z_pad_out || y_pad_out || y_f32_out, "fm_conv3x3_fwd_bf16: no output");
+  ConvArgs a;
+  a.x = (const bf16 *)x_pad;
+  a.w = (const bf16 *)w;
+  a.bias = bias;
+  a.gate = (const bf16 *)gate_pad;
+  a.resid = (const bf16 *)resid_pad;
+  a.z_out = (bf16 *)z_pad_out;
+  a.y_out = (bf16 *)y_pad_out;
+  a.y_f32 = y_f32_out;
+  a.B = B;
+  a.H = H;
+  a.W = W;
+  a.act = act;
+  a.err = err_device;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return cout == 64 ? launch_fwd<64>(a, s) : launch_fwd<32>(a, s);
+}
+
+extern "C" int fm_conv3x3_wgrad_bf16(int B, int H, int W, int cout, const void *x_pad,
+                                     const void *dy_pad, float *dwt, int *err_device,
+                                     void *stream) {
+  FM_CHECK_ARG(x_pad && dy_pad && dwt && err_device, "fm_conv3x3_wgrad_bf16: NULL input");
+  FM_CHECK_ARG(B >= 1 && H >= 2 && W >= 2, "fm_conv3x3_wgrad_bf16: need H, W >= 2");
+  FM_CHECK_ARG(cout == 32 || cout == 64, "fm_conv3x3_wgrad_bf16: cout must be 32 or 64");
+  WgradArgs a;
+  a.x = (const bf16 *)x_pad;
+  a.dy = (const bf16 *)dy_pad;
+  a.dwt = dwt;
+  a.B = B;
+  a.H = H;
+  a.W = W;
+  a.chunks_per_cta = 1;
+  a.err = err_device;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  return cout == 64 ? launch_wgrad<64>(a, s) : launch_wgrad<32>(a, s);
+}

@@ -217,6 +217,63 @@ int fm_mhd_totals(int n, int fp64, void *const fields[9], double *partials,
 int fm_tc_gemm_bf16(int M, int N, int K, const void *A, const void *B, float *C,
                     int *err_device, void *stream);
 
+/* ---- learned 16-step surrogate (BF16 tcgen05 convolutions) ------------------- */
+
+/*
+ * No counterpart in the reference (a new form: a convolutional neural operator
+ * that jumps 16 steps of the pearson-2d Gray-Scott program, with the plain
+ * stencil as its fallback and judge).
+ *
+ * Latent tensors are NHWC bf16 with a one-pixel periodic halo,
+ * [B][H+2][W+2][64]; weights [cout][9][64] bf16 (tap t = (dy+1)*3 + dx+1).
+ *
+ * fm_conv3x3_fwd_bf16: y = act(conv3x3(x, w) (+ bias) (* gelu'(gate)) (+ resid))
+ * on the tcgen05 tensor cores (implicit GEMM, FP32 accumulation in tensor
+ * memory).  cout 32 or 64; B*H*W % 128 == 0; act 0 = none, 1 = GELU (erf).
+ * Outputs (any subset): z_pad_out = value before act (bf16, padded),
+ * y_pad_out (bf16, padded, halo written), y_f32_out ([B][H][W][cout] fp32).
+ * fm_conv3x3_wgrad_bf16: dwt[t][ci][co] += sum_p dy[p][co] * x[p+t][ci]
+ * (split-K over pixels, fp32 atomics; zero dwt first).
+ * *err_device becomes 1 if a bounded tensor-core wait gave up.
+ */
+int fm_conv3x3_fwd_bf16(int B, int H, int W, int cout, const void *x_pad,
+                        const void *w, const float *bias, const void *gate_pad,
+                        const void *resid_pad, int act, void *z_pad_out,
+                        void *y_pad_out, float *y_f32_out, int *err_device,
+                        void *stream);
+int fm_conv3x3_wgrad_bf16(int B, int H, int W, int cout, const void *x_pad,
+                          const void *dy_pad, float *dwt, int *err_device,
+                          void *stream);
+
+/* Latent packing: (U, V, F, k) of B periodic N x N fields -> [B][N/4+2][N/4+2][64]
+ * (4x4 space-to-depth, channel q*16 + sy*4 + sx, q = U, V, (F-0.04)*50,
+ * (k-0.06)*100; halo filled).  Unpacking: U += scale*y[..][sub],
+ * V += scale*y[..][16+sub] from an fp32 latent [B][N/4][N/4][64]. */
+int fm_sur_pack(int B, int N, const float *U, const float *V, const float *F,
+                const float *K, void *xpad, void *stream);
+int fm_sur_unpack(int B, int N, const float *y, float *U, float *V, float scale,
+                  void *stream);
+/* Training: MSE of the latent prediction y against (S1 - S0)/scale; writes
+ * grad_scale * dL/dy as a padded bf16 latent and adds the loss to *loss. */
+int fm_sur_loss_grad(int B, int N, const float *y, const float *U0,
+                     const float *V0, const float *U1, const float *V1,
+                     void *dy_pad, float *loss, float scale, float grad_scale,
+                     void *stream);
+/* db[c] += sum over interior pixels of dy_pad[..][c] (n = latent edge). */
+int fm_sur_bias_grad(int B, int n, const void *dy_pad, float *db, void *stream);
+/* wf[ci][t][co] = w[co][8-t][ci]: data-gradient weights as a forward conv. */
+int fm_sur_flip(const void *w, void *wf, void *stream);
+/* One Adam step on fp32 master weights w [64][9][64] (gradient dwt[9][ci][co])
+ * and bias b [64]; writes the bf16 copy wb.  mask_co >= 0 pins output
+ * channels >= mask_co to zero.  step counts from 1. */
+int fm_sur_adam(float *w, const float *gwt, float *mw, float *vw, void *wb,
+                float *b, const float *gb, float *mb, float *vb, float lr,
+                float b1, float b2, float eps, int step, int mask_co,
+                void *stream);
+/* dz = dh * gelu'(z) over padded bf16 latents of `count` elements. */
+int fm_sur_gelu_bwd(long long count, const void *dh, const void *z, void *dz,
+                    void *stream);
+
 /* ---- 2D diffusion --------------------------------------------------------- */
 
 /*

@@ -1,0 +1,147 @@
+"""The surrogate's tcgen05 convolution kernels and training gradients against
+the CPU float64 reference (oracle/surrogate_ref.py).
+
+Inputs and weights are rounded to bf16 before both paths see them, so the
+single-convolution checks isolate accumulation order (fp32 on the tensor
+cores): tolerance 1e-4 of the magnitude scale.  Whole-network gradients also
+differ by the bf16 rounding of every intermediate activation on the GPU:
+checked by relative norm error < 5e-2 and cosine similarity > 0.995 per layer.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from formura_gb300 import _lib, inits
+from formura_gb300.surrogate import C, Surrogate
+from oracle import surrogate_ref as ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def pad_periodic(x):
+    """[B][n][n][C] -> [B][n+2][n+2][C] with the periodic halo."""
+    rows = torch.cat([x[:, -1:], x, x[:, :1]], 1)
+    return torch.cat([rows[:, :, -1:], rows, rows[:, :, :1]], 2)
+
+
+def bf16r(t):
+    return t.to(torch.bfloat16).to(torch.float64)
+
+
+@pytest.mark.parametrize("B,n", [(2, 16), (1, 32), (4, 8)])
+def test_conv_fwd_matches_cpu(cuda_device, B, n):
+    g = torch.Generator().manual_seed(B * 100 + n)
+    x = bf16r(torch.randn(B, n, n, C, generator=g, dtype=torch.float64))
+    w = bf16r(torch.randn(C, 9, C, generator=g, dtype=torch.float64) * 0.05)
+    b = torch.randn(C, generator=g, dtype=torch.float64) * 0.1
+    want = ref.conv(x, w, b)
+    xg = pad_periodic(x).to(torch.bfloat16).cuda().contiguous()
+    wg = w.to(torch.bfloat16).cuda().contiguous()
+    bg = b.float().cuda()
+    y = torch.empty(B, n, n, C, device="cuda")
+    ypad = torch.zeros(B, n + 2, n + 2, C, dtype=torch.bfloat16, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = _lib.lib().fm_conv3x3_fwd_bf16(B, n, n, C, _p(xg), _p(wg), _p(bg), None, None, 0, None,
+                                        _p(ypad), _p(y), _p(err),
+                                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(st, "fm_conv3x3_fwd_bf16")
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    scale = ref.conv(x.abs(), w.abs()).abs() + 1e-3
+    assert ((y.double().cpu() - want).abs() <= 1e-4 * scale).all()
+    # the padded bf16 output carries the periodic halo
+    assert torch.equal(ypad.cpu(), pad_periodic(y.cpu().to(torch.bfloat16).double()).to(torch.bfloat16))
+
+
+def test_conv_wgrad_and_dgrad_match_autograd(cuda_device):
+    B, n = 2, 16
+    g = torch.Generator().manual_seed(7)
+    x = bf16r(torch.randn(B, n, n, C, generator=g, dtype=torch.float64))
+    w = bf16r(torch.randn(C, 9, C, generator=g, dtype=torch.float64) * 0.05)
+    dy = bf16r(torch.randn(B, n, n, C, generator=g, dtype=torch.float64))
+    xr, wr = x.clone().requires_grad_(True), w.clone().requires_grad_(True)
+    ref.conv(xr, wr).backward(dy)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    xg = pad_periodic(x).to(torch.bfloat16).cuda().contiguous()
+    dyg = pad_periodic(dy).to(torch.bfloat16).cuda().contiguous()
+    dwt = torch.zeros(9, C, C, device="cuda")
+    L = _lib.lib()
+    _lib.check(L.fm_conv3x3_wgrad_bf16(B, n, n, C, _p(xg), _p(dyg), _p(dwt), _p(err), s), "wgrad")
+    wb = w.to(torch.bfloat16).cuda().contiguous()
+    wf = torch.empty_like(wb)
+    _lib.check(L.fm_sur_flip(_p(wb), _p(wf), s), "flip")
+    dx = torch.empty(B, n, n, C, device="cuda")
+    _lib.check(L.fm_conv3x3_fwd_bf16(B, n, n, C, _p(dyg), _p(wf), None, None, None, 0, None, None,
+                                     _p(dx), _p(err), s), "dgrad")
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    gw = dwt.double().cpu().permute(2, 0, 1)          # [t][ci][co] -> [co][t][ci]
+    assert torch.allclose(gw, wr.grad, rtol=1e-4, atol=1e-4 * wr.grad.abs().max().item())
+    assert torch.allclose(dx.double().cpu(), xr.grad, rtol=1e-4,
+                          atol=1e-4 * xr.grad.abs().max().item())
+
+
+def test_network_gradients_match_cpu_oracle(cuda_device):
+    B, N = 2, 32
+    sizes = [N] * B
+    U0, V0 = inits.gs2d_ensemble_state(sizes, seed=4)
+    U0 = U0.reshape(B, N, N)
+    V0 = V0.reshape(B, N, N)
+    rng = np.random.default_rng(0)
+    U1 = U0 + 0.01 * rng.standard_normal(U0.shape).astype(np.float32)
+    V1 = V0 + 0.01 * rng.standard_normal(V0.shape).astype(np.float32)
+    F = np.array([0.03, 0.05], np.float32)
+    K = np.array([0.055, 0.065], np.float32)
+    net = Surrogate(seed=3)
+    for L in net.layers:   # non-trivial biases
+        L.b.copy_(torch.randn(C, generator=torch.Generator().manual_seed(1)).cuda() * 0.05)
+        if L.mask_co > 0:
+            L.b[L.mask_co:] = 0
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    loss = net.loss_and_grads(t(U0), t(V0), t(F), t(K), t(U1), t(V1))
+    torch.cuda.synchronize()
+    net.check_errors()
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).double()  # noqa: E731
+    ws = [L.wb.double().cpu() for L in net.layers]
+    bs = [L.b.double().cpu() for L in net.layers]
+    lref, gws, gbs = ref.loss_and_grads(bf16r(d(U0)), bf16r(d(V0)), d(F), d(K), d(U1), d(V1), ws,
+                                         bs)
+    assert abs(loss.item() - lref) < 2e-2 * lref
+    for i, (L, gw, gb) in enumerate(zip(net.layers, gws, gbs)):
+        got = L.gw.double().cpu().permute(2, 0, 1)
+        rel = ((got - gw).norm() / gw.norm()).item()
+        cos = (torch.dot(got.flatten(), gw.flatten()) / (got.norm() * gw.norm())).item()
+        assert rel < 5e-2 and cos > 0.995, (i, rel, cos)
+        relb = ((L.gb.double().cpu() - gb).norm() / (gb.norm() + 1e-30)).item()
+        assert relb < 5e-2, (i, relb)
+
+
+def test_training_reduces_loss(cuda_device):
+    """A few Adam steps on a fixed batch of true 16-step pairs reduce the loss."""
+    from formura_gb300 import kernels
+
+    B, N = 8, 64
+    sizes, F, K = inits.gs2d_ensemble(B, seed=11, sizes=(N,))
+    e = kernels.Ensemble(sizes, F, K)
+    U, V = inits.gs2d_ensemble_state(sizes, seed=2)
+    U, V = torch.from_numpy(U).cuda(), torch.from_numpy(V).cuda()
+    wU, wV = torch.empty_like(U), torch.empty_like(V)
+    e.forward(U, V, wU, wV, 200, use_graph=False)  # develop some structure
+    U0, V0 = U.clone().view(B, N, N), V.clone().view(B, N, N)
+    e.forward(U, V, wU, wV, 16, use_graph=False)
+    U1, V1 = U.view(B, N, N), V.view(B, N, N)
+    Ft = torch.tensor(F, dtype=torch.float32, device="cuda")
+    Kt = torch.tensor(K, dtype=torch.float32, device="cuda")
+    net = Surrogate(seed=0)
+    first = net.train_step(U0, V0, Ft, Kt, U1, V1, lr=1e-3).item()
+    for _ in range(60):
+        last = net.train_step(U0, V0, Ft, Kt, U1, V1, lr=1e-3).item()
+    net.check_errors()
+    assert last < 0.2 * first, (first, last)
