@@ -105,6 +105,23 @@ class Surrogate:
         return {"w": [L.w.cpu() for L in self.layers], "b": [L.b.cpu() for L in self.layers],
                 "step": self.step_count}
 
+    def save_npz(self, path) -> None:
+        """Weights and biases as float32 arrays (w0..w13 [64][9][64], b0..b13)."""
+        arrs = {}
+        for i, L in enumerate(self.layers):
+            arrs["w%d" % i] = L.w.cpu().numpy()
+            arrs["b%d" % i] = L.b.cpu().numpy()
+        arrs["step"] = np.array(self.step_count)
+        np.savez_compressed(path, **arrs)
+
+    def load_npz(self, path) -> None:
+        with np.load(path) as z:
+            for i, L in enumerate(self.layers):
+                L.w.copy_(torch.from_numpy(z["w%d" % i]).to(self.dev))
+                L.b.copy_(torch.from_numpy(z["b%d" % i]).to(self.dev))
+                L.wb.copy_(L.w.to(torch.bfloat16))
+            self.step_count = int(z["step"])
+
     def load_state_dict(self, sd):
         for L, w, b in zip(self.layers, sd["w"], sd["b"]):
             L.w.copy_(w.to(self.dev))
