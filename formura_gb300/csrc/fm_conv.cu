@@ -27,6 +27,7 @@
 
 #include "fm_common.cuh"
 #include "fm_tc.cuh"
+#include "fm_tune.h"
 
 namespace {
 
@@ -200,6 +201,197 @@ __global__ void __launch_bounds__(128) conv3x3_fwd(ConvArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// conv3x3_fwd_res: the persistent, weight-resident form for cout = 64.
+//
+// Output positions are indexed in the FLATTENED PADDED image,
+// j = py*(W+2) + px; the 3x3 tap (dy,dx) of position j reads position
+// j + dy*(W+2) + dx.  A tile of 128 consecutive positions therefore reads one
+// contiguous region [j0 - (W+3), j0 + 128 + (W+3)).  That region is staged
+// into shared memory as eight "channel-group planes" (8 channels = 16 B per
+// position, positions consecutive, plane stride PL): in the K-major
+// no-swizzle descriptor this is SBO = 128 B between 8-row groups and
+// LBO = PL between K-adjacent core matrices, so the A operand of every tap is
+// the SAME region at start offset ((W+3) + dy*(W+2) + dx)*16 — no per-tap
+// gather.  Halo positions of the tile are computed and discarded.
+//   * the 9 taps' weights (72 KB) are loaded once per CTA and stay resident;
+//   * regions are double-buffered with cp.async (prefetch of tile i+1 while the
+//     tensor core works on tile i);
+//   * two TMEM accumulators (2 x 64 columns): the epilogue of tile i-1 runs
+//     while the MMAs of tile i are in flight.
+constexpr int kResThreads = 128;
+
+__host__ __device__ __forceinline__ int res_region_len(int Wp) { return kTM + 2 * (Wp + 1); }
+
+__global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, int ntile_img,
+                                                                  int ntiles, int plane) {
+  constexpr int NT = 64;
+  constexpr int kWBytes = 9 * NT * CIN * 2;  // 72 KB, tap tiles of 8 KB
+  extern __shared__ __align__(1024) uint8_t dsm[];
+  uint8_t *sw = dsm;                          // weights
+  uint8_t *sreg = dsm + kWBytes;              // 2 region buffers of 8*plane bytes
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t s_tmem;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int H = a.H, W = a.W, Wp = W + 2;
+  const int rlen = res_region_len(Wp);
+  const long long img = (long long)(H + 2) * Wp;  // positions per padded image
+  if (warp == 0) tmem_alloc(&s_tmem, 128);
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+  }
+  // weights -> resident K-major tiles (one cp.async group)
+  for (int v = tid; v < 9 * NT * 8; v += kResThreads) {
+    const int tap = v / (NT * 8), rem = v % (NT * 8);
+    const int r = rem >> 3, kk = (rem & 7) * 8;
+    cp_async16(sw + tap * (NT * CIN * 2) + kmajor_off(r, kk, CIN),
+               a.w + ((size_t)r * 9 + tap) * CIN + kk, true);
+  }
+  cp_async_commit();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  const uint32_t idesc = idesc_bf16_f32(kTM, NT);
+
+  auto stage = [&](int it, int buf) {
+    const int tile = blockIdx.x + it * gridDim.x;
+    const int b = tile / ntile_img, tl = tile % ntile_img;
+    const long long j0 = (long long)(Wp + 1) + (long long)tl * kTM;
+    const long long r0 = j0 - (Wp + 1);
+    const bf16 *base = a.x + (size_t)b * img * CIN;
+    uint8_t *dst = sreg + (size_t)buf * 8 * plane;
+    for (int v = tid; v < rlen * 8; v += kResThreads) {
+      const int pos = v >> 3, kg = v & 7;
+      const long long j = r0 + pos;
+      const bool ok = j < img;
+      cp_async16(dst + kg * plane + pos * 16, base + (size_t)(ok ? j : 0) * CIN + kg * 8, ok);
+    }
+    cp_async_commit();
+  };
+
+  auto epilogue = [&](int it, int acc) {
+    const int tile = blockIdx.x + it * gridDim.x;
+    const int b = tile / ntile_img, tl = tile % ntile_img;
+    const long long j = (long long)(Wp + 1) + (long long)tl * kTM + warp * 32 + (tid & 31);
+    const int py = (int)(j / Wp), px = (int)(j % Wp);
+    const bool interior = py >= 1 && py <= H && px >= 1 && px <= W;
+    const int y = py - 1, xx = px - 1;
+    int pys[2] = {py, -1}, pxs[2] = {px, -1};
+    if (y == 0) pys[1] = H + 1;
+    if (y == H - 1) pys[1] = 0;
+    if (xx == 0) pxs[1] = W + 1;
+    if (xx == W - 1) pxs[1] = 0;
+    const size_t pin = (size_t)b * img + (size_t)j;
+#pragma unroll
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem + (uint32_t)(acc * 64) + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      if (!interior) continue;
+      if (a.bias) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += __ldg(a.bias + c0 + i);
+      }
+      if (a.gate) {
+        const bf16 *g = a.gate + pin * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] *= gelu_grad(__bfloat162float(g[i]));
+      }
+      if (a.resid) {
+        const bf16 *rr = a.resid + pin * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += __bfloat162float(rr[i]);
+      }
+      __align__(16) bf16 zb[16], yb[16];
+      if (a.z_out) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) zb[i] = __float2bfloat16_rn(v[i]);
+      }
+      if (a.act == 1) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) yb[i] = __float2bfloat16_rn(v[i]);
+#pragma unroll
+      for (int iy = 0; iy < 2; ++iy) {
+        if (pys[iy] < 0) continue;
+#pragma unroll
+        for (int ix = 0; ix < 2; ++ix) {
+          if (pxs[ix] < 0) continue;
+          const size_t q = (((size_t)b * (H + 2) + pys[iy]) * Wp + pxs[ix]) * NT + c0;
+          if (a.z_out) {
+            reinterpret_cast<uint4 *>(a.z_out + q)[0] = reinterpret_cast<const uint4 *>(zb)[0];
+            reinterpret_cast<uint4 *>(a.z_out + q)[1] = reinterpret_cast<const uint4 *>(zb)[1];
+          }
+          if (a.y_out) {
+            reinterpret_cast<uint4 *>(a.y_out + q)[0] = reinterpret_cast<const uint4 *>(yb)[0];
+            reinterpret_cast<uint4 *>(a.y_out + q)[1] = reinterpret_cast<const uint4 *>(yb)[1];
+          }
+        }
+      }
+      if (a.y_f32) {
+        float *dst = a.y_f32 + (((size_t)b * H + y) * W + xx) * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[i] = v[i];
+      }
+    }
+  };
+
+  const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / gridDim.x + 1 : 0;
+  uint32_t ph[2] = {0u, 0u};
+  bool ok = true;
+  if (my_tiles > 0) stage(0, 0);
+  for (int it = 0; it < my_tiles; ++it) {
+    const int buf = it & 1;
+    if (it >= 1) {
+      // MMAs of tile it-1 read region buffer buf^1 and write accumulator buf^1
+      if (!mbar_wait(&bar[buf ^ 1], ph[buf ^ 1])) ok = false;
+      ph[buf ^ 1] ^= 1u;
+    }
+    if (it + 1 < my_tiles) {
+      stage(it + 1, buf ^ 1);
+      cp_async_wait<1>();  // weights and region `it` have landed
+    } else {
+      cp_async_wait<0>();
+    }
+    fence_proxy_async_smem();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (tid == 0) {
+      const uint32_t reg = smem_u32(sreg + (size_t)buf * 8 * plane);
+      const uint32_t wbase = smem_u32(sw);
+#pragma unroll 1
+      for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+        const uint32_t a_off = (uint32_t)((Wp + 1) + dy * Wp + dx) * 16u;
+#pragma unroll
+        for (int s = 0; s < CIN / 16; ++s) {
+          const uint64_t ad = smem_desc(reg + a_off + (uint32_t)(2 * s) * (uint32_t)plane,
+                                        (uint32_t)plane, 128);
+          const uint64_t bd = smem_desc(wbase + tap * (NT * CIN * 2) + s * 256, 128,
+                                        (CIN / 8) * 128);
+          mma_bf16(tmem + (uint32_t)(buf * 64), ad, bd, idesc, (tap | s) != 0);
+        }
+      }
+      mma_commit(&bar[buf]);
+    }
+    if (it >= 1 && ok) epilogue(it - 1, buf ^ 1);
+  }
+  if (my_tiles > 0) {
+    const int last = (my_tiles - 1) & 1;
+    if (!mbar_wait(&bar[last], ph[last])) ok = false;
+    fence_after_sync();
+    if (ok) epilogue(my_tiles - 1, last);
+  }
+  if (!ok && tid == 0) atomicExch(a.err, 1);
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// ---------------------------------------------------------------------------
 struct WgradArgs {
   const bf16 *x;   // [B][H+2][W+2][64]
   const bf16 *dy;  // padded [B][H+2][W+2][NT]
@@ -361,14 +553,40 @@ int launch_wgrad(WgradArgs a, cudaStream_t s) {
 
 }  // namespace
 
+namespace {
+int launch_fwd_res(const ConvArgs &a, cudaStream_t s) {
+  const int Wp = a.W + 2;
+  const int rlen = res_region_len(Wp);
+  const int plane = ((rlen * 16 + 127) / 128) * 128;
+  const size_t smem = (size_t)9 * 64 * CIN * 2 + 2 * 8 * (size_t)plane;
+  int dev = 0, optin = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  FM_TRY_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem > (size_t)optin || plane / 16 >= (1 << 14)) return FM_ERR_UNSUPPORTED;
+  FM_TRY_CUDA(cudaFuncSetAttribute(conv3x3_fwd_res, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  int sms = 0;
+  int st = fm::device_sm_count(&sms);
+  if (st) return st;
+  // positions Wp+1 .. (H+1)*Wp - 2 of each padded image hold every interior cell
+  const long long span = (long long)a.H * Wp - 2;
+  const int ntile_img = (int)((span + kTM - 1) / kTM);
+  const long long ntiles = (long long)ntile_img * a.B;
+  if (ntiles > (1ll << 30)) return FM_ERR_UNSUPPORTED;
+  const int grid = (int)std::min<long long>(ntiles, sms);
+  conv3x3_fwd_res<<<grid, kResThreads, smem, s>>>(a, ntile_img, (int)ntiles, plane);
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+}  // namespace
+
 extern "C" int fm_conv3x3_fwd_bf16(int B, int H, int W, int cout, const void *x_pad,
                                    const void *w, const float *bias, const void *gate_pad,
                                    const void *resid_pad, int act, void *z_pad_out,
                                    void *y_pad_out, float *y_f32_out, int *err_device,
                                    void *stream) {
   FM_CHECK_ARG(x_pad && w && err_device, "fm_conv3x3_fwd_bf16: NULL input");
-  FM_CHECK_ARG(B >= 1 && H >= 2 && W >= 2 && ((long long)B * H * W) % kTM == 0,
-               "fm_conv3x3_fwd_bf16: B*H*W must be a multiple of 128 (got %d*%d*%d)", B, H, W);
+  FM_CHECK_ARG(B >= 1 && H >= 2 && W >= 2, "fm_conv3x3_fwd_bf16: need H, W >= 2");
   FM_CHECK_ARG(cout == 32 || cout == 64, "fm_conv3x3_fwd_bf16: cout must be 32 or 64");
   FM_CHECK_ARG(act == 0 || act == 1, "fm_conv3x3_fwd_bf16: act must be 0 or 1");
   FM_CHECK_ARG(z_pad_out || y_pad_out || y_f32_out, "fm_conv3x3_fwd_bf16: no output");
@@ -387,6 +605,12 @@ extern "C" int fm_conv3x3_fwd_bf16(int B, int H, int W, int cout, const void *x_
   a.act = act;
   a.err = err_device;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (cout == 64 && fm::tune_get("conv.kernel", 1) == 1) {
+    const int st = launch_fwd_res(a, s);
+    if (st != FM_ERR_UNSUPPORTED) return st;
+  }
+  FM_CHECK_ARG(((long long)B * H * W) % kTM == 0,
+               "fm_conv3x3_fwd_bf16: this shape needs B*H*W %% 128 == 0 (got %d*%d*%d)", B, H, W);
   return cout == 64 ? launch_fwd<64>(a, s) : launch_fwd<32>(a, s);
 }
 

@@ -229,7 +229,8 @@ int fm_tc_gemm_bf16(int M, int N, int K, const void *A, const void *B, float *C,
  *
  * fm_conv3x3_fwd_bf16: y = act(conv3x3(x, w) (+ bias) (* gelu'(gate)) (+ resid))
  * on the tcgen05 tensor cores (implicit GEMM, FP32 accumulation in tensor
- * memory).  cout 32 or 64; B*H*W % 128 == 0; act 0 = none, 1 = GELU (erf).
+ * memory).  cout 32 or 64; H, W >= 2 (cout 32: B*H*W % 128 == 0); act 0 =
+ * none, 1 = GELU (erf).  cout 64 runs the weight-resident persistent kernel.
  * Outputs (any subset): z_pad_out = value before act (bf16, padded),
  * y_pad_out (bf16, padded, halo written), y_f32_out ([B][H][W][cout] fp32).
  * fm_conv3x3_wgrad_bf16: dwt[t][ci][co] += sum_p dy[p][co] * x[p+t][ci]

@@ -34,8 +34,20 @@ def bf16r(t):
     return t.to(torch.bfloat16).to(torch.float64)
 
 
-@pytest.mark.parametrize("B,n", [(2, 16), (1, 32), (4, 8)])
-def test_conv_fwd_matches_cpu(cuda_device, B, n):
+@pytest.fixture(params=[1, 0], ids=["resident", "gather"])
+def conv_kernel(request):
+    """Both forward-convolution kernels: the weight-resident shifted-descriptor
+    kernel (default) and the per-tap gather kernel."""
+    L = _lib.lib()
+    L.fm_tune_set(b"conv.kernel", request.param)
+    yield request.param
+    L.fm_tune_clear()
+
+
+@pytest.mark.parametrize("B,n", [(2, 16), (1, 32), (4, 8), (3, 40)])
+def test_conv_fwd_matches_cpu(cuda_device, conv_kernel, B, n):
+    if conv_kernel == 0 and (B * n * n) % 128:
+        pytest.skip("the gather kernel needs B*H*W % 128 == 0")
     g = torch.Generator().manual_seed(B * 100 + n)
     x = bf16r(torch.randn(B, n, n, C, generator=g, dtype=torch.float64))
     w = bf16r(torch.randn(C, 9, C, generator=g, dtype=torch.float64) * 0.05)
@@ -57,6 +69,35 @@ def test_conv_fwd_matches_cpu(cuda_device, B, n):
     assert ((y.double().cpu() - want).abs() <= 1e-4 * scale).all()
     # the padded bf16 output carries the periodic halo
     assert torch.equal(ypad.cpu(), pad_periodic(y.cpu().to(torch.bfloat16).double()).to(torch.bfloat16))
+
+
+def test_conv_kernels_agree_bitwise(cuda_device):
+    """The two forward kernels issue the same MMA sequence: identical outputs."""
+    B, n = 2, 64
+    g = torch.Generator().manual_seed(5)
+    x = pad_periodic(torch.randn(B, n, n, C, generator=g)).to(torch.bfloat16).cuda().contiguous()
+    w = (torch.randn(C, 9, C, generator=g) * 0.05).to(torch.bfloat16).cuda().contiguous()
+    b = (torch.randn(C, generator=g) * 0.1).cuda()
+    res = torch.randn(B, n + 2, n + 2, C, generator=g).to(torch.bfloat16).cuda()
+    L = _lib.lib()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    outs = []
+    try:
+        for k in (0, 1):
+            L.fm_tune_set(b"conv.kernel", k)
+            y = torch.zeros(B, n + 2, n + 2, C, dtype=torch.bfloat16, device="cuda")
+            z = torch.zeros_like(y)
+            yf = torch.zeros(B, n, n, C, device="cuda")
+            _lib.check(L.fm_conv3x3_fwd_bf16(B, n, n, C, _p(x), _p(w), _p(b), _p(res), _p(res), 1,
+                                             _p(z), _p(y), _p(yf), _p(err), s), "conv")
+            outs.append((y, z, yf))
+    finally:
+        L.fm_tune_clear()
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    for a, c in zip(outs[0], outs[1]):
+        assert torch.equal(a, c)
 
 
 def test_conv_wgrad_and_dgrad_match_autograd(cuda_device):
