@@ -266,11 +266,75 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
     for name, x, y in zip(inits.MHD_FIELDS, a32, a64):
         y = y.cpu().numpy()
         errs[name] = float(np.abs(x.double().cpu().numpy() - y).max() / max(np.abs(y).max(), 1e-300))
+    out["surrogate_gs2d_512"] = run_surrogate_variant(torch)
     out["mhd_3d_256_fp32_bulk_fp64_energy"] = {
         "value": round(N ** 3 * 500 / sec / 1e9, 3), "unit": "GLUP/s", "steps": 500,
         "seconds": round(sec, 3), "totals_fp64": [float(x) for x in tot],
         "max_rel_error_vs_fp64_64cube_500steps": errs, "kernel": "mhd_stage"}
     return out
+
+
+def run_surrogate_variant(torch):
+    """The learned 16-step surrogate on 8 instances of 512^2 (trained weights in
+    formura_gb300/weights): network-jump throughput against the plain FP32
+    stencil on the same batch, and a 4096-step run with re-anchoring every 256
+    steps and stencil fallback, scored against the FP64 oracle."""
+    import numpy as np
+
+    from formura_gb300 import inits
+    from formura_gb300 import surrogate_run as sr
+    from formura_gb300.surrogate import JUMP, Surrogate
+    from oracle import oracle
+
+    B, Nn = 8, 512
+    net = Surrogate(seed=0)
+    net.load_npz(ROOT / "formura_gb300" / "weights" / "gs2d_surrogate.npz")
+    sizes, Fl, Kl = inits.gs2d_ensemble(B, seed=2024, sizes=(Nn,))
+    U0, V0 = inits.gs2d_ensemble_state(sizes, seed=2024)
+    Ft = torch.tensor(Fl, dtype=torch.float32, device="cuda")
+    Kt = torch.tensor(Kl, dtype=torch.float32, device="cuda")
+
+    def fresh():
+        return (torch.from_numpy(U0).cuda().view(B, Nn, Nn).clone(),
+                torch.from_numpy(V0).cuda().view(B, Nn, Nn).clone())
+
+    U, V = fresh()
+    net.predict(U, V, Ft, Kt)
+    jump_s = _event_time(torch, lambda: [net.predict(U, V, Ft, Kt) for _ in range(16)]) / 16
+    flops = 14 * 2 * 576 * 64 * B * (Nn // 4) ** 2
+    U, V = fresh()
+    sr.run_plain(U, V, Ft, Kt, JUMP)
+    plain16_s = _event_time(torch, lambda: sr.run_plain(U, V, Ft, Kt, JUMP))
+    Up, Vp = fresh()
+    plain_s = _event_time(torch, lambda: sr.run_plain(Up, Vp, Ft, Kt, 4096))
+    info = sr.run_with_surrogate(net, *fresh(), Ft, Kt, 4096, 256, 1e-2)  # warm-up
+    Us, Vs = fresh()
+    sur_s = _event_time(torch, lambda: sr.run_with_surrogate(net, Us, Vs, Ft, Kt, 4096, 256, 1e-2))
+    errs = []
+    for i in range(2):
+        u0 = U0[i * Nn * Nn:(i + 1) * Nn * Nn].reshape(Nn, Nn).astype(np.float64)
+        v0 = V0[i * Nn * Nn:(i + 1) * Nn * Nn].reshape(Nn, Nn).astype(np.float64)
+        uo, vo = oracle.gs2d_f64(u0, v0, 4096, Fl[i], Kl[i], 2e-5, 1e-5, 1.0, 0.01, fast=True)
+        us, vs = Us[i].double().cpu().numpy(), Vs[i].double().cpu().numpy()
+        errs.append(float(np.sqrt((np.linalg.norm(us - uo) ** 2 + np.linalg.norm(vs - vo) ** 2) /
+                                  (np.linalg.norm(uo) ** 2 + np.linalg.norm(vo) ** 2))))
+    held = sr.jump_error(net, n_inst=16, N=128, seed=99)
+    return {
+        "network_jump_ms": round(jump_s * 1e3, 3),
+        "conv_tflops": round(flops / jump_s / 1e12, 1),
+        "network_steps_per_s": round(B * JUMP / jump_s, 1),
+        "plain_stencil_16_steps_ms": round(plain16_s * 1e3, 3),
+        "plain_stencil_steps_per_s": round(B * 4096 / plain_s, 1),
+        "surrogate_run_steps_per_s": round(B * 4096 / sur_s, 1),
+        "speedup_vs_plain": round(plain_s / sur_s, 4),
+        "network_only_speed_ratio_vs_plain": round(plain16_s / jump_s, 4),
+        "fallback_instances": int(sum(info["fallback"])), "instances": B,
+        "rel_l2_vs_fp64_after_4096": errs,
+        "heldout_jump_rel_l2": held["state_rel_l2"],
+        "heldout_persistence_rel_l2": held["state_rel_l2_persistence"],
+        "config": "8 x 512^2, F~U[0.02,0.06], k~U[0.05,0.07]; 4096 steps, re-anchor every 256, "
+                  "fallback tolerance 1e-2",
+        "kernel": "conv3x3_fwd_res (tcgen05)"}
 
 
 def run_reference(args):
@@ -488,6 +552,24 @@ def run_profile_case(args):
         d0 = inits.diffusion_2d(n, n, seed=1)
         d = torch.from_numpy(d0).to(dev)
         kernels.diff2d_f64_forward(d, torch.empty_like(d), 0.4, args.profile_steps)
+    elif args.profile == "surrogate":
+        # `profile_steps` network jumps (and one training step) on `profile_batch` instances of n x n
+        from formura_gb300.surrogate import Surrogate
+
+        net = Surrogate(seed=0)
+        net.load_npz(ROOT / "formura_gb300" / "weights" / "gs2d_surrogate.npz")
+        sizes, F, k = inits.gs2d_ensemble(args.profile_batch, seed=1, sizes=(n,))
+        U0, V0 = inits.gs2d_ensemble_state(sizes, seed=1)
+        U = torch.from_numpy(U0).to(dev).view(args.profile_batch, n, n)
+        V = torch.from_numpy(V0).to(dev).view(args.profile_batch, n, n)
+        Ft = torch.tensor(F, dtype=torch.float32, device=dev)
+        Kt = torch.tensor(k, dtype=torch.float32, device=dev)
+        U1, V1 = U.clone(), V.clone()
+        for _ in range(args.profile_steps):
+            net.predict(U, V, Ft, Kt)
+        if args.profile_train:
+            net.train_step(U1, V1, Ft, Kt, U, V, lr=1e-6)
+        net.check_errors()
     torch.cuda.synchronize()
     print("profile case %s n=%d steps=%d done" % (args.profile, n, args.profile_steps))
 
@@ -502,11 +584,14 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
     ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",
-                                          "mhd", "diff2d"], default=None,
+                                          "mhd", "diff2d", "surrogate"], default=None,
                     help="run a small case of one kernel for an ncu capture, then exit")
     ap.add_argument("--profile-n", type=int, default=256)
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--profile-tb", type=int, default=0)
+    ap.add_argument("--profile-batch", type=int, default=8, help="surrogate case: instances")
+    ap.add_argument("--profile-train", action="store_true",
+                    help="surrogate case: also run one training step")
     ap.add_argument("--tune", action="append", help="KEY=VALUE tuning knob (fm_tune_set)")
     args = ap.parse_args()
     if args.profile:

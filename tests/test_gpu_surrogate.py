@@ -186,3 +186,54 @@ def test_training_reduces_loss(cuda_device):
         last = net.train_step(U0, V0, Ft, Kt, U1, V1, lr=1e-3).item()
     net.check_errors()
     assert last < 0.2 * first, (first, last)
+
+
+WEIGHTS = __import__("pathlib").Path(__file__).resolve().parents[1] / "formura_gb300" / \
+    "weights" / "gs2d_surrogate.npz"
+
+
+def test_trained_network_beats_the_method_without_it(cuda_device):
+    """What the trained network gains: on held-out pairs its 16-step prediction
+    is far closer to the stencil's than persistence (the no-model guess
+    S(t+16) = S(t)) and than the untrained network."""
+    from formura_gb300 import surrogate_run as sr
+
+    net = Surrogate(seed=0)
+    untrained = sr.jump_error(net, n_inst=8, N=128, seed=4242)
+    net.load_npz(WEIGHTS)
+    trained = sr.jump_error(net, n_inst=8, N=128, seed=4242)
+    assert trained["state_rel_l2"] < trained["state_rel_l2_persistence"] / 5, trained
+    assert trained["state_rel_l2"] < untrained["state_rel_l2"] / 5, (trained, untrained)
+
+
+def test_fallback_reproduces_the_plain_stencil(cuda_device):
+    """With the anchor criterion unmet the run falls back, and the result is the
+    plain FP32 stencil's bit for bit; with the criterion disabled it is not."""
+    from formura_gb300 import surrogate_run as sr
+
+    B, N = 2, 128
+    sizes, F, K = inits.gs2d_ensemble(B, seed=77, sizes=(N,))
+    U0, V0 = inits.gs2d_ensemble_state(sizes, seed=77)
+    Ft = torch.tensor(F, dtype=torch.float32, device="cuda")
+    Kt = torch.tensor(K, dtype=torch.float32, device="cuda")
+    net = Surrogate(seed=0)
+    net.load_npz(WEIGHTS)
+
+    def fresh():
+        return (torch.from_numpy(U0).cuda().view(B, N, N).clone(),
+                torch.from_numpy(V0).cuda().view(B, N, N).clone())
+
+    Up, Vp = fresh()
+    sr.run_plain(Up, Vp, Ft, Kt, 512)
+    Us, Vs = fresh()
+    info = sr.run_with_surrogate(net, Us, Vs, Ft, Kt, 512, 256, tol=1e-12)
+    assert all(info["fallback"])
+    assert torch.equal(Us, Up) and torch.equal(Vs, Vp)
+    Un, Vn = fresh()
+    info = sr.run_with_surrogate(net, Un, Vn, Ft, Kt, 512, 256, tol=1e30)
+    assert not any(info["fallback"])
+    assert not torch.equal(Un, Up)
+    # the unchecked surrogate run still tracks the stencil to a few percent
+    rel = torch.sqrt(((Un - Up) ** 2).sum() + ((Vn - Vp) ** 2).sum()) / \
+        torch.sqrt((Up ** 2).sum() + (Vp ** 2).sum())
+    assert rel.item() < 0.1, rel.item()
