@@ -337,7 +337,7 @@ int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
 /*
  * Process-wide tuning knobs.  Every knob has an automatic default; a set value
  * overrides it for later calls.  No knob changes results (all variants of a
- * kernel are bit-exact with each other).  Known keys:
+ * stencil kernel are bit-exact with each other).  Known keys:
  *   "gs3d_f64.kernel"  0 auto, 1 tile kernel (any nz), 2 full-z-row kernel (nz <= 256)
  *   "gs3d_f64.div"     0 Markstein division (3 FP64 ops), 1 integer-corrected (1 FP64 op +
  *                      128-bit integer products; default), 2 residual + integer compare
@@ -347,6 +347,11 @@ int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
  *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)
  *   "gs2d_ens.tile"    default output tile edge of ensembles (32 or 64)
  *   "gs2d_ens.tb"      default steps per shared-memory pass of ensembles
+ *   "conv.kernel"      fm_conv3x3_fwd_bf16 with 64 output channels: 1 weight-resident
+ *                      persistent kernel (default; falls back to 0 when its staged region
+ *                      does not fit in shared memory), 0 per-tap gather kernel
+ *                      (B*H*W % 128 == 0).  The two accumulate in different orders, so
+ *                      their outputs may differ in the last FP32 bits.
  * fm_tune_clear() restores every default.
  */
 int fm_tune_set(const char *key, int value);
