@@ -16,15 +16,25 @@
 //                     spans the whole periodic z row (gs3d_f64_row), or
 //                     computes it itself (gs3d_f64_tile, any nz).
 //
-// On GB300 the FP64 pipe (~1.7 lanes/clk/SM), not HBM, bounds these kernels:
-// the ~70 FP64 operations of one cell update take ~40x longer than moving its
-// 32 bytes.  Divisions by dx are the bulk of it; two exact methods exist:
+// On GB300 the FP64 pipe (2 lanes/clk/SM), not HBM, bounds these kernels:
+// the ~45 FP64 operations of one cell update take ~20x longer than moving its
+// 32 bytes.  Divisions by dx are the bulk of it; four exact methods exist:
 //   DIV = 0  fm::div_const   — Markstein: 1 DMUL + 2 DFMA
 //   DIV = 1  fm::div_const_i — 1 DMUL, then the rounding decided with 128-bit
-//                              integer products on the integer pipe (default:
-//                              10.9 GLUP/s at 256^3 against 6.2 for DIV = 0)
+//                              integer products on the integer pipe (10.9
+//                              GLUP/s at 256^3 against 6.2 for DIV = 0)
 //   DIV = 2  fm::div_const_r — 1 DMUL + 1 DFMA (exact residual), rounding
 //                              decided by integer compares of bit patterns.
+//   DIV = 3  fm::soft::div_const_s — no FP64 instruction: the quotient
+//                              significand from 32-bit partial products with
+//                              a reciprocal prepared on the host, the rounding
+//                              from the sign of an exact 64-bit remainder
+//                              (default; 15.2 GLUP/s alone).
+// With DIV = 3, MUL moves multiplications to the integer pipes as well
+// (fm::soft::mul_const_s / mul_s): MUL = 1 the five multiplications by a
+// constant (F, F+k, Du, Dv, dt) — the default, 18.0 GLUP/s — and MUL = 2
+// also U*V and (U*V)*V (17.6: the general product costs more integer work
+// than the FP64 time it frees).
 // The integer parts read doubles only through __double2hiint/__double2loint:
 // a 64-bit mask of a double's bit pattern is otherwise turned back into an
 // FP64 abs by the compiler, which costs as much as the DFMA it replaced.
@@ -32,6 +42,7 @@
 #include <cstdlib>
 
 #include "fm_common.cuh"
+#include "fm_softfp.cuh"
 #include "fm_tune.h"
 
 namespace {
@@ -39,19 +50,35 @@ namespace {
 struct Gs64 {
   double F, Fk, Du, Dv, dt;
   fm::DivConst dx;
+  fm::soft::DivConstS dxs;
+  fm::soft::MulConstS Fs, Fks, Dus, Dvs, dts;
 };
 
 template <int DIV>
 __device__ __forceinline__ double ddx(double x, const Gs64 &c) {
   if (DIV == 0) return fm::div_const(x, c.dx.d, c.dx.r);
   if (DIV == 2) return fm::div_const_r(x, c.dx.d, c.dx.r);
+  if (DIV == 3) return fm::soft::div_const_s(x, c.dxs);
   return fm::div_const_i(x, c.dx);
+}
+
+// k*x for one of the constants (MUL >= 1: on the integer pipes)
+template <int MUL>
+__device__ __forceinline__ double kmul(double k, const fm::soft::MulConstS &ks, double x) {
+  if (MUL >= 1) return fm::soft::mul_const_s(x, ks);
+  return k * x;
+}
+// x*y of two state-dependent values (MUL == 2: on the integer pipes)
+template <int MUL>
+__device__ __forceinline__ double vmul(double x, double y) {
+  if (MUL == 2) return fm::soft::mul_s(x, y);
+  return x * y;
 }
 
 constexpr int kRY = 4;  // y cells per thread
 
 // One cell's update from its fluxes (the U_next and V_next nodes).
-template <int DIV>
+template <int DIV, int MUL>
 __device__ __forceinline__ void gs_cell(double u, double v, double fxu_m, double fxu_p,
                                         double fyu_m, double fyu_p, double fzu_m,
                                         double fzu_p, double fxv_m, double fxv_p,
@@ -59,33 +86,33 @@ __device__ __forceinline__ void gs_cell(double u, double v, double fxu_m, double
                                         double fzv_p, const Gs64 &c, double &un,
                                         double &vn) {
   // U_next: U + dt*(((-(U*V*V)) + F*(1-U)) + Du*((lx + ly) + lz))
-  const double a_1 = u * v;
-  const double a_2 = a_1 * v;
+  const double a_1 = vmul<MUL>(u, v);
+  const double a_2 = vmul<MUL>(a_1, v);
   const double a_3 = -a_2;
   const double a_5 = 1.0 - u;
-  const double a_6 = c.F * a_5;
+  const double a_6 = kmul<MUL>(c.F, c.Fs, a_5);
   const double a_7 = a_3 + a_6;
   const double lx = ddx<DIV>(fxu_p - fxu_m, c);
   const double ly = ddx<DIV>(fyu_p - fyu_m, c);
   const double lz = ddx<DIV>(fzu_p - fzu_m, c);
   const double a_l = (lx + ly) + lz;
-  const double dU = a_7 + c.Du * a_l;
-  un = u + c.dt * dU;
+  const double dU = a_7 + kmul<MUL>(c.Du, c.Dus, a_l);
+  un = u + kmul<MUL>(c.dt, c.dts, dU);
   // V_next: V + dt*(((U*V*V) - (F+k)*V) + Dv*((mx + my) + mz))
-  const double b_6 = a_2 - c.Fk * v;
+  const double b_6 = a_2 - kmul<MUL>(c.Fk, c.Fks, v);
   const double mx = ddx<DIV>(fxv_p - fxv_m, c);
   const double my = ddx<DIV>(fyv_p - fyv_m, c);
   const double mz = ddx<DIV>(fzv_p - fzv_m, c);
   const double b_l = (mx + my) + mz;
-  const double dV = b_6 + c.Dv * b_l;
-  vn = v + c.dt * dV;
+  const double dV = b_6 + kmul<MUL>(c.Dv, c.Dvs, b_l);
+  vn = v + kmul<MUL>(c.dt, c.dts, dV);
 }
 
 // ---------------------------------------------------------------------------
 // gs3d_f64_row: CTA = nz threads (nz/32 warps along z, nz <= 256), each thread
 // kRY y cells; the CTA covers a full periodic z row, so no flux is computed
 // twice along z.  Tiles: (ny/kRY) y blocks x ceil(nx/xchunk) x chunks.
-template <int DIV>
+template <int DIV, int MUL>
 __global__ void __launch_bounds__(256)
     gs3d_f64_row(const double *__restrict__ U, const double *__restrict__ V,
                  double *__restrict__ Un, double *__restrict__ Vn, int nx, int ny, int nz,
@@ -174,7 +201,7 @@ __global__ void __launch_bounds__(256)
         const double fxu_p = ddx<DIV>(up[j] - uc[j], c);
         const double fxv_p = ddx<DIV>(vp[j] - vc[j], c);
         double un, vn;
-        gs_cell<DIV>(uc[j], vc[j], fxu[j], fxu_p, fyu[j], fyu[j + 1], fzu[j], fzu_p, fxv[j],
+        gs_cell<DIV, MUL>(uc[j], vc[j], fxu[j], fxu_p, fyu[j], fyu[j + 1], fzu[j], fzu_p, fxv[j],
                      fxv_p, fyv[j], fyv[j + 1], fzv[j], fzv_p, c, un, vn);
         Un[pc + off[j]] = un;
         Vn[pc + off[j]] = vn;
@@ -194,7 +221,7 @@ __global__ void __launch_bounds__(256)
 constexpr int kTileWarps = 4;
 constexpr int kTY = kTileWarps * kRY;
 
-template <int DIV>
+template <int DIV, int MUL>
 __global__ void __launch_bounds__(kTileWarps * 32)
     gs3d_f64_tile(const double *__restrict__ U, const double *__restrict__ V,
                   double *__restrict__ Un, double *__restrict__ Vn, int nx, int ny, int nz,
@@ -270,7 +297,7 @@ __global__ void __launch_bounds__(kTileWarps * 32)
         const double fxu_p = ddx<DIV>(up[j] - u, c);
         const double fxv_p = ddx<DIV>(vp[j] - v, c);
         double un, vn;
-        gs_cell<DIV>(u, v, fxu[j], fxu_p, fyu[j], fyu[j + 1], fzu_m, fzu_p, fxv[j], fxv_p,
+        gs_cell<DIV, MUL>(u, v, fxu[j], fxu_p, fyu[j], fyu[j + 1], fzu_m, fzu_p, fxv[j], fxv_p,
                      fyv[j], fyv[j + 1], fzv_m, fzv_p, c, un, vn);
         Un[pc + off[j]] = un;
         Vn[pc + off[j]] = vn;
@@ -285,7 +312,7 @@ __global__ void __launch_bounds__(kTileWarps * 32)
 
 struct LaunchPlan {
   bool row;
-  int div, threads, xchunk, ntiles_yz, ntiles, grid;
+  int div, mul, threads, xchunk, ntiles_yz, ntiles, grid;
 };
 
 template <typename K>
@@ -317,11 +344,50 @@ int pick_xchunk(int nx, long long tiles_per_chunk_row, int resident, int forced)
   return best_xc;
 }
 
-int plan_launch(int nx, int ny, int nz, double dx, LaunchPlan *lp) {
+// The instantiated (DIV, MUL) variants: (0,0) (1,0) (2,0) (3,0) (3,1) (3,2).
+template <int DIV, int MUL>
+struct Variant {
+  static int resident(bool row, int threads, int *out) {
+    return row ? resident_blocks(gs3d_f64_row<DIV, MUL>, threads, out)
+               : resident_blocks(gs3d_f64_tile<DIV, MUL>, threads, out);
+  }
+  static void launch(const LaunchPlan &lp, cudaStream_t s, const double *u, const double *v,
+                     double *un, double *vn, int nx, int ny, int nz, const Gs64 &c) {
+    if (lp.row)
+      gs3d_f64_row<DIV, MUL><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz,
+                                                            lp.xchunk, lp.ntiles, c);
+    else
+      gs3d_f64_tile<DIV, MUL><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz,
+                                                             lp.xchunk, lp.ntiles_yz,
+                                                             lp.ntiles, c);
+  }
+};
+
+template <typename F>
+auto dispatch(int div, int mul, F &&f) {
+  if (div == 3 && mul == 2) return f(Variant<3, 2>());
+  if (div == 3 && mul == 1) return f(Variant<3, 1>());
+  if (div == 3) return f(Variant<3, 0>());
+  if (div == 2) return f(Variant<2, 0>());
+  if (div == 1) return f(Variant<1, 0>());
+  return f(Variant<0, 0>());
+}
+
+bool soft_mul_ok(double k) {  // nonzero, normal, finite
+  const double a = k < 0 ? -k : k;
+  return a >= 0x1p-1022 && a <= 0x1.fffffffffffffp1023;
+}
+
+int plan_launch(int nx, int ny, int nz, const fm_gs_params *p, LaunchPlan *lp) {
   const int kind = fm::tune_get("gs3d_f64.kernel", 0);  // 0 auto, 1 tile, 2 row
-  lp->div = fm::tune_get("gs3d_f64.div", 1);
-  if (lp->div < 0 || lp->div > 2) lp->div = 1;
-  if (lp->div == 2 && !(dx >= 0x1p-20 && dx <= 0x1p20)) lp->div = 0;
+  lp->div = fm::tune_get("gs3d_f64.div", 3);
+  if (lp->div < 0 || lp->div > 3) lp->div = 3;
+  if (lp->div == 2 && !(p->dx >= 0x1p-20 && p->dx <= 0x1p20)) lp->div = 0;
+  lp->mul = lp->div == 3 ? fm::tune_get("gs3d_f64.mul", 1) : 0;
+  if (lp->mul < 0 || lp->mul > 2) lp->mul = 0;
+  if (lp->mul && !(soft_mul_ok(p->F) && soft_mul_ok(p->F + p->k) && soft_mul_ok(p->Du) &&
+                   soft_mul_ok(p->Dv) && soft_mul_ok(p->dt)))
+    lp->mul = 0;  // a zero or non-normal constant: hardware multiplications
   const bool row_ok = nz <= 256 && ny % kRY == 0;
   lp->row = (kind == 2 || kind == 0) && row_ok;
   if (kind == 1 || ny % kTY != 0) lp->row = false;
@@ -329,48 +395,27 @@ int plan_launch(int nx, int ny, int nz, double dx, LaunchPlan *lp) {
     fm::set_error("fm_gs3d_f64_forward: ny must be a multiple of %d for nz > 256", kTY);
     return FM_ERR_UNSUPPORTED;
   }
-  int resident = 0, st;
+  int resident = 0;
   const int forced = fm::tune_get("gs3d_f64.xchunk", 0);
-  if (lp->row) {
-    lp->threads = nz;
-    st = lp->div == 2 ? resident_blocks(gs3d_f64_row<2>, nz, &resident)
-         : lp->div == 1 ? resident_blocks(gs3d_f64_row<1>, nz, &resident)
-                        : resident_blocks(gs3d_f64_row<0>, nz, &resident);
-    if (st) return st;
-    lp->ntiles_yz = ny / kRY;
-  } else {
-    lp->threads = kTileWarps * 32;
-    st = lp->div == 2 ? resident_blocks(gs3d_f64_tile<2>, lp->threads, &resident)
-         : lp->div == 1 ? resident_blocks(gs3d_f64_tile<1>, lp->threads, &resident)
-                        : resident_blocks(gs3d_f64_tile<0>, lp->threads, &resident);
-    if (st) return st;
-    lp->ntiles_yz = (nz / 32) * (ny / kTY);
-  }
+  lp->threads = lp->row ? nz : kTileWarps * 32;
+  const bool row = lp->row;
+  const int threads = lp->threads;
+  const int st = dispatch(lp->div, lp->mul,
+                          [&](auto v) { return decltype(v)::resident(row, threads, &resident); });
+  if (st) return st;
+  lp->ntiles_yz = lp->row ? ny / kRY : (nz / 32) * (ny / kTY);
   lp->xchunk = pick_xchunk(nx, lp->ntiles_yz, resident, forced);
   lp->ntiles = lp->ntiles_yz * ((nx + lp->xchunk - 1) / lp->xchunk);
   lp->grid = std::min(lp->ntiles, resident);
   return FM_OK;
 }
 
-template <int DIV>
-void launch_div(const LaunchPlan &lp, cudaStream_t s, const double *u, const double *v,
-                double *un, double *vn, int nx, int ny, int nz, const Gs64 &c) {
-  if (lp.row)
-    gs3d_f64_row<DIV><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz, lp.xchunk,
-                                                     lp.ntiles, c);
-  else
-    gs3d_f64_tile<DIV><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz, lp.xchunk,
-                                                      lp.ntiles_yz, lp.ntiles, c);
-}
-
 void launch(const LaunchPlan &lp, cudaStream_t s, const double *u, const double *v, double *un,
             double *vn, int nx, int ny, int nz, const Gs64 &c) {
-  if (lp.div == 2)
-    launch_div<2>(lp, s, u, v, un, vn, nx, ny, nz, c);
-  else if (lp.div == 1)
-    launch_div<1>(lp, s, u, v, un, vn, nx, ny, nz, c);
-  else
-    launch_div<0>(lp, s, u, v, un, vn, nx, ny, nz, c);
+  dispatch(lp.div, lp.mul, [&](auto var) {
+    decltype(var)::launch(lp, s, u, v, un, vn, nx, ny, nz, c);
+    return 0;
+  });
 }
 
 }  // namespace
@@ -390,7 +435,7 @@ extern "C" int fm_gs3d_f64_forward(int nx, int ny, int nz, double *U, double *V,
   if (steps == 0) return FM_OK;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   LaunchPlan lp;
-  int st = plan_launch(nx, ny, nz, p->dx, &lp);
+  int st = plan_launch(nx, ny, nz, p, &lp);
   if (st) return st;
   Gs64 c;
   c.F = p->F;
@@ -399,6 +444,16 @@ extern "C" int fm_gs3d_f64_forward(int nx, int ny, int nz, double *U, double *V,
   c.Dv = p->Dv;
   c.dt = p->dt;
   c.dx = fm::make_div_const(p->dx);
+  c.dxs = fm::soft::make_div_const_s(p->dx);
+  if (lp.mul) {
+    c.Fs = fm::soft::make_mul_const_s(c.F);
+    c.Fks = fm::soft::make_mul_const_s(c.Fk);
+    c.Dus = fm::soft::make_mul_const_s(c.Du);
+    c.Dvs = fm::soft::make_mul_const_s(c.Dv);
+    c.dts = fm::soft::make_mul_const_s(c.dt);
+  } else {
+    c.Fs = c.Fks = c.Dus = c.Dvs = c.dts = fm::soft::MulConstS();
+  }
   double *cu = U, *cv = V, *nu = work_U, *nv = work_V;
   for (int i = 0; i < steps; ++i) {
     launch(lp, s, cu, cv, nu, nv, nx, ny, nz, c);

@@ -340,8 +340,12 @@ int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
  * stencil kernel are bit-exact with each other).  Known keys:
  *   "gs3d_f64.kernel"  0 auto, 1 tile kernel (any nz), 2 full-z-row kernel (nz <= 256)
  *   "gs3d_f64.div"     0 Markstein division (3 FP64 ops), 1 integer-corrected (1 FP64 op +
- *                      128-bit integer products; default), 2 residual + integer compare
- *                      (2 FP64 ops)
+ *                      128-bit integer products), 2 residual + integer compare
+ *                      (2 FP64 ops), 3 no FP64 op (significand from 32-bit partial
+ *                      products, rounding from an exact 64-bit remainder; default)
+ *   "gs3d_f64.mul"     with div 3: 0 hardware multiplications, 1 multiplications by the
+ *                      constants F, F+k, Du, Dv, dt on the integer pipes (default), 2 all
+ *                      of them
  *   "gs3d_f64.xchunk"  x planes per CTA tile (0 = automatic)
  *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_tb_forward (1..4)
  *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)

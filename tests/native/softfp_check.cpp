@@ -1,0 +1,27 @@
+// Host build of formura_gb300/csrc/fm_softfp.cuh for the CPU bit-exactness
+// checks in tests/test_softfp.py (compiled there with g++ into a temporary
+// shared library).  Each function applies one soft operation element-wise.
+#include "../../formura_gb300/csrc/fm_softfp.cuh"
+
+extern "C" {
+
+void softfp_div_const(const double *x, long n, double d, double *out) {
+  const fm::soft::DivConstS c = fm::soft::make_div_const_s(d);
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::div_const_s(x[i], c);
+}
+
+void softfp_mul_const(const double *x, long n, double y, double *out) {
+  const fm::soft::MulConstS c = fm::soft::make_mul_const_s(y);
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::mul_const_s(x[i], c);
+}
+
+void softfp_mul(const double *x, const double *y, long n, double *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::mul_s(x[i], y[i]);
+}
+
+void softfp_div_reciprocal_words(double d, unsigned *r_hi, unsigned *r_lo) {
+  const fm::soft::DivConstS c = fm::soft::make_div_const_s(d);
+  *r_hi = c.r_hi;
+  *r_lo = c.r_lo;
+}
+}

@@ -36,13 +36,16 @@ def test_gs3d_f64_bit_exact(cuda_device, shape, steps):
     assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
 
 
-@pytest.mark.parametrize("kernel,div,xchunk", [(1, 0, 0), (1, 1, 0), (1, 2, 0), (2, 0, 0),
-                                               (2, 1, 0), (2, 2, 0), (2, 2, 3), (1, 2, 5)])
-def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, xchunk):
+@pytest.mark.parametrize("kernel,div,mul,xchunk", [
+    (1, 0, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0), (2, 0, 0, 0), (2, 1, 0, 0), (2, 2, 0, 0),
+    (2, 2, 0, 3), (1, 2, 0, 5), (1, 3, 0, 0), (2, 3, 0, 0), (2, 3, 1, 0), (2, 3, 2, 0),
+    (1, 3, 2, 0), (2, 3, 2, 3)])
+def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, mul, xchunk):
     lib = _lib.lib()
     try:
         lib.fm_tune_set(b"gs3d_f64.kernel", kernel)
         lib.fm_tune_set(b"gs3d_f64.div", div)
+        lib.fm_tune_set(b"gs3d_f64.mul", mul)
         lib.fm_tune_set(b"gs3d_f64.xchunk", xchunk)
         for shape, steps in (((24, 32, 64), 9), ((9, 16, 256), 4), ((5, 48, 32), 3)):
             U0, V0 = inits.gray_scott_3d(*shape, seed=31, ncubes=3, side=8)
@@ -53,7 +56,17 @@ def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, xchunk):
         lib.fm_tune_clear()
 
 
-def test_gs3d_f64_bit_exact_other_constants(cuda_device):
+@pytest.fixture(params=[(1, 0), (3, 0), (3, 2)], ids=["div1", "softdiv", "softdiv_softmul"])
+def arith(request):
+    """Division / multiplication forms of the FP64 kernel (gs3d_f64.div, .mul)."""
+    lib = _lib.lib()
+    lib.fm_tune_set(b"gs3d_f64.div", request.param[0])
+    lib.fm_tune_set(b"gs3d_f64.mul", request.param[1])
+    yield request.param
+    lib.fm_tune_clear()
+
+
+def test_gs3d_f64_bit_exact_other_constants(cuda_device, arith):
     # tiny dt/dx and random fields exercise the division fast path widely
     rng = np.random.default_rng(0)
     U0 = rng.random((16, 32, 32))
@@ -64,7 +77,7 @@ def test_gs3d_f64_bit_exact_other_constants(cuda_device):
     assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
 
 
-def test_gs3d_f64_subnormal_front(cuda_device):
+def test_gs3d_f64_subnormal_front(cuda_device, arith):
     # V values deep in the subnormal range take the IEEE-division fallback.
     U0 = np.ones((8, 16, 32))
     V0 = np.zeros((8, 16, 32))
@@ -75,7 +88,7 @@ def test_gs3d_f64_subnormal_front(cuda_device):
     assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
 
 
-def test_gs3d_f64_full_size_properties(cuda_device):
+def test_gs3d_f64_full_size_properties(cuda_device, arith):
     """256^3: a periodic shift of the input shifts the output exactly, and the
     uniform state is an exact fixed point."""
     n = 256

@@ -1,0 +1,142 @@
+"""Bit-exactness of the integer-pipe binary64 operations (csrc/fm_softfp.cuh)
+against the host's IEEE arithmetic, on the CPU: the header is compiled as
+plain C++ (the same source the kernels inline) into a temporary library.
+
+Inputs: random significands over wide exponent ranges, the special values
+(signed zeros, subnormals, infinities, NaN), operands whose quotient lies
+right at a binade boundary (x = d * 2^k and neighbours), and products that are
+exact ties (one factor with a short significand), which exercise the
+round-half-even branch.
+"""
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+SRC = ROOT / "tests" / "native" / "softfp_check.cpp"
+
+
+def _build(tmp_path_factory, name, defines=()):
+    out = tmp_path_factory.mktemp("softfp") / name
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-shared", "-fPIC", *defines, "-o",
+                    str(out), str(SRC)], check=True)
+    L = ctypes.CDLL(str(out))
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.softfp_div_const.argtypes = [dp, ctypes.c_long, ctypes.c_double, dp]
+    L.softfp_mul_const.argtypes = [dp, ctypes.c_long, ctypes.c_double, dp]
+    L.softfp_mul.argtypes = [dp, dp, ctypes.c_long, dp]
+    return L
+
+
+@pytest.fixture(scope="module", params=["full", "fast_only"])
+def lib(tmp_path_factory, request):
+    """The full operations, and the fast path alone: with FM_SOFT_SLOW_SENTINEL
+    the slow path returns a marked NaN, so the fast path is checked on every
+    input it accepts (and must accept every normal-range case)."""
+    if request.param == "full":
+        return _build(tmp_path_factory, "libsoftfp_full.so")
+    return _build(tmp_path_factory, "libsoftfp_fast.so", ["-DFM_SOFT_SLOW_SENTINEL"])
+
+
+SENTINEL = np.uint64(0x7ff8dead0000beef)
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def random_doubles(rng, n, emin=-60, emax=60):
+    """Random signs, uniformly random 52-bit fractions, exponents in [emin, emax]."""
+    frac = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    e = rng.integers(emin + 1023, emax + 1024, n).astype(np.uint64)
+    s = rng.integers(0, 2, n).astype(np.uint64)
+    return ((s << np.uint64(63)) | (e << np.uint64(52)) | frac).view(np.float64)
+
+
+SPECIALS = np.array([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308 / 3, 1e-310,
+                     2.2250738585072014e-308, -2.2250738585072014e-308, 1.7976931348623157e308,
+                     -1.7976931348623157e308, np.inf, -np.inf, np.nan, 1.0, -1.0, 0.5, 2.0,
+                     1e-300, 1e300, 3e-308, 4e-308, 1e308])
+
+
+def same_bits(a, b, normal_inputs):
+    """Bitwise equality; slow-path sentinels are accepted only where an input
+    lies outside the normal range or the result is not a normal number."""
+    a64, b64 = a.view(np.uint64), b.view(np.uint64)
+    nan = np.isnan(a) & np.isnan(b) & (a64 != SENTINEL)
+    eq = (a64 == b64) | nan
+    fast_case = normal_inputs & (np.abs(b) >= 2.2250738585072014e-308) & np.isfinite(b)
+    slow_ok = (a64 == SENTINEL) & ~fast_case
+    good = eq | slow_ok
+    return np.all(good), np.flatnonzero(~good)
+
+
+def normal(v):
+    a = np.abs(v)
+    return ((a >= 2.2250738585072014e-308) & np.isfinite(a)) | (a == 0)
+
+
+def neighbours(v):
+    """v and its next-up/next-down binary64 neighbours."""
+    return np.concatenate([v, np.nextafter(v, np.inf), np.nextafter(v, -np.inf)])
+
+
+DIVISORS = [0.01, 1.0 / 256, 0.1, 3.0, 0.7, 1.0, 0.5, 1.5, 0.001, 7.0e-6, 2.0 ** -40,
+            2.0 ** 40 * 0.999, 0.0078125 * 1.0000000000000002]
+
+
+@pytest.mark.parametrize("d", DIVISORS)
+def test_div_const_matches_ieee(lib, d):
+    rng = np.random.default_rng(int(d * 1e6) + 17)
+    parts = [random_doubles(rng, 400_000), random_doubles(rng, 50_000, -1022, 1023),
+             SPECIALS, neighbours(d * 2.0 ** np.arange(-30, 31)),
+             neighbours(np.ldexp(d, np.arange(-1074, 1020, 7)))]
+    x = np.concatenate(parts)
+    with np.errstate(all="ignore"):
+        want = x / d
+    got = np.empty_like(x)
+    lib.softfp_div_const(_p(x), x.size, d, _p(got))
+    ok, bad = same_bits(got, want, normal(x))
+    assert ok, (d, x[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+@pytest.mark.parametrize("y", [0.5, 2e-5, 1e-5, 0.04, 0.1, 0.06 + 0.04, 1.0, -3.0, 1.5,
+                               1.0000000000000002, 1e300, 1e-300])
+def test_mul_const_matches_ieee(lib, y):
+    rng = np.random.default_rng(abs(hash(y)) % (1 << 31))
+    short = (rng.integers(1, 1 << 12, 50_000) * 2.0 ** rng.integers(-30, 30, 50_000))
+    x = np.concatenate([random_doubles(rng, 400_000), random_doubles(rng, 50_000, -1022, 1023),
+                        SPECIALS, short, neighbours(1.0 / np.array([y]))])
+    with np.errstate(all="ignore"):
+        want = x * y
+    got = np.empty_like(x)
+    lib.softfp_mul_const(_p(x), x.size, y, _p(got))
+    ok, bad = same_bits(got, want, normal(x))
+    assert ok, (y, x[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+def test_mul_matches_ieee(lib):
+    rng = np.random.default_rng(5)
+    n = 1_000_000
+    x = random_doubles(rng, n)
+    y = random_doubles(rng, n)
+    # exact ties: one factor with a short odd significand
+    k = 200_000
+    y[:k] = rng.integers(1, 1 << 10, k) * 2.0 ** rng.integers(-20, 20, k)
+    # binade edges: y = (2^53 - j) / 2^52 style factors around 1 and 2
+    y[k:k + 1000] = np.nextafter(1.0, 0.0)
+    y[k + 1000:k + 2000] = np.nextafter(2.0, 0.0)
+    # wide exponents (underflow / overflow to the slow path) and the specials
+    xs = np.concatenate([x, random_doubles(rng, 100_000, -1022, 1023),
+                         np.repeat(SPECIALS, SPECIALS.size)])
+    ys = np.concatenate([y, random_doubles(rng, 100_000, -1022, 1023),
+                         np.tile(SPECIALS, SPECIALS.size)])
+    with np.errstate(all="ignore"):
+        want = xs * ys
+    got = np.empty_like(xs)
+    lib.softfp_mul(_p(xs), _p(ys), xs.size, _p(got))
+    ok, bad = same_bits(got, want, normal(xs) & normal(ys))
+    assert ok, (xs[bad[:5]], ys[bad[:5]], got[bad[:5]], want[bad[:5]])
