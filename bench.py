@@ -9,8 +9,11 @@ Formura_Forward of the emitted program = 2000 time steps.
           on the launching stream; 268 MB of state > 129 MB L2 (no flush needed).
   e2e     GLUP/s through Formura_Forward on the host globals: pinned H2D copy of
           U,V, 2000 steps, D2H copy, every step.
-  roofline  the dominant kernel (gs3d_f64_step) against the FP64 FMA pipe
-          measured in this run, and its HBM fraction.
+  roofline  the dominant kernel (gs3d_f64_row) against the FP64 FMA pipe
+          measured in this run, and its HBM fraction.  Algorithmic work is the
+          generated DAG's 46 FP64 operations per cell update; the kernel runs the
+          divisions by dx and the multiplications by constants as exact integer
+          sequences, so the FP64 pipe executes 26 FP64 instructions per update.
   cpu_baseline  the oracle's OpenMP speed build on all host cores, on a
           bounded sample of the same workload.
 
@@ -483,6 +486,10 @@ def run_engine(args):
                              "frac": round(achieved_gbs / hbm_peak, 4),
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"},
                      "fp32_peak_tflops": round(fp32_peak, 2),
+                     "fp64_pipe_ops_per_lup": 26,
+                     "integer_pipe_ops_per_lup": "13 divisions by dx (12 + one y-face flux "
+                                                 "recomputed) + 5 multiplications by constants, "
+                                                 "correctly rounded on the integer pipes",
                      "kernel": "gs3d_f64_row", "ms_per_launch": round(per_launch * 1e3, 4)},
         "e2e": {"value": round(e2e, 4), "unit": "GLUP/s",
                 "h2d_bytes_per_step": 2 * 8 * N ** 3, "d2h_bytes_per_step": 2 * 8 * N ** 3},

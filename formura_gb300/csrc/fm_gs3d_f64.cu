@@ -110,37 +110,38 @@ __device__ __forceinline__ void gs_cell(double u, double v, double fxu_m, double
 
 // ---------------------------------------------------------------------------
 // gs3d_f64_row: CTA = nz threads (nz/32 warps along z, nz <= 256), each thread
-// kRY y cells; the CTA covers a full periodic z row, so no flux is computed
-// twice along z.  Tiles: (ny/kRY) y blocks x ceil(nx/xchunk) x chunks.
-template <int DIV, int MUL>
-__global__ void __launch_bounds__(256)
+// RY y cells (4: 128 registers, 2 CTAs per SM; 2: 80 registers, 3 CTAs — the
+// default with DIV = 3, 19.3 GLUP/s at 256^3 against 18.1 for RY = 4); the CTA covers a full periodic z row, so no flux is computed
+// twice along z.  Tiles: (ny/RY) y blocks x ceil(nx/xchunk) x chunks.
+template <int DIV, int MUL, int RY>
+__global__ void __launch_bounds__(256, RY >= 4 ? 2 : 3)
     gs3d_f64_row(const double *__restrict__ U, const double *__restrict__ V,
                  double *__restrict__ Un, double *__restrict__ Vn, int nx, int ny, int nz,
                  int xchunk, int ntiles, Gs64 c) {
   // [buffer][field][j][warp] lane-0 z fluxes, double-buffered by plane parity
-  __shared__ double s_fz[2][2][kRY][8];
+  __shared__ double s_fz[2][2][RY][8];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int wz = blockDim.x >> 5;
   const int wn = (w + 1 == wz) ? 0 : w + 1;
   const int z = threadIdx.x;
   const int zm = fm::wrap_dn(z, nz);
-  const int nyt = ny / kRY;
+  const int nyt = ny / RY;
   const size_t sx = (size_t)ny * nz;
   int buf = 0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int y0 = (t % nyt) * kRY;
+    const int y0 = (t % nyt) * RY;
     const int x0 = (t / nyt) * xchunk;
     const int x1 = min(x0 + xchunk, nx);
-    int off[kRY];
+    int off[RY];
 #pragma unroll
-    for (int j = 0; j < kRY; ++j) off[j] = (y0 + j) * nz + z;
+    for (int j = 0; j < RY; ++j) off[j] = (y0 + j) * nz + z;
     const int off_ym = fm::wrap_dn(y0, ny) * nz + z;
-    const int off_yp = fm::wrap_up(y0 + kRY - 1, ny) * nz + z;
-    double uc[kRY], vc[kRY], fxu[kRY], fxv[kRY];
+    const int off_yp = fm::wrap_up(y0 + RY - 1, ny) * nz + z;
+    double uc[RY], vc[RY], fxu[RY], fxv[RY];
     {
       const size_t pm = (size_t)fm::wrap_dn(x0, nx) * sx, pc = (size_t)x0 * sx;
 #pragma unroll
-      for (int j = 0; j < kRY; ++j) {
+      for (int j = 0; j < RY; ++j) {
         const double um = __ldg(U + pm + off[j]), vm = __ldg(V + pm + off[j]);
         uc[j] = __ldg(U + pc + off[j]);
         vc[j] = __ldg(V + pc + off[j]);
@@ -151,16 +152,16 @@ __global__ void __launch_bounds__(256)
     for (int x = x0; x < x1; ++x) {
       const size_t pc = (size_t)x * sx;
       const size_t pp = (size_t)fm::wrap_up(x, nx) * sx;
-      double up[kRY], vp[kRY];
+      double up[RY], vp[RY];
 #pragma unroll
-      for (int j = 0; j < kRY; ++j) {
+      for (int j = 0; j < RY; ++j) {
         up[j] = __ldg(U + pp + off[j]);
         vp[j] = __ldg(V + pp + off[j]);
       }
       // z fluxes at z-1/2
-      double fzu[kRY], fzv[kRY];
+      double fzu[RY], fzv[RY];
 #pragma unroll
-      for (int j = 0; j < kRY; ++j) {
+      for (int j = 0; j < RY; ++j) {
         double uzm = __shfl_up_sync(0xffffffffu, uc[j], 1);
         double vzm = __shfl_up_sync(0xffffffffu, vc[j], 1);
         if (lane == 0) {
@@ -175,23 +176,23 @@ __global__ void __launch_bounds__(256)
         }
       }
       // y fluxes: fy[j] at y0+j-1/2, j = 0..RY
-      double fyu[kRY + 1], fyv[kRY + 1];
+      double fyu[RY + 1], fyv[RY + 1];
       {
         const double um = __ldg(U + pc + off_ym), vm = __ldg(V + pc + off_ym);
         const double upp = __ldg(U + pc + off_yp), vpp = __ldg(V + pc + off_yp);
         fyu[0] = ddx<DIV>(uc[0] - um, c);
         fyv[0] = ddx<DIV>(vc[0] - vm, c);
 #pragma unroll
-        for (int j = 1; j < kRY; ++j) {
+        for (int j = 1; j < RY; ++j) {
           fyu[j] = ddx<DIV>(uc[j] - uc[j - 1], c);
           fyv[j] = ddx<DIV>(vc[j] - vc[j - 1], c);
         }
-        fyu[kRY] = ddx<DIV>(upp - uc[kRY - 1], c);
-        fyv[kRY] = ddx<DIV>(vpp - vc[kRY - 1], c);
+        fyu[RY] = ddx<DIV>(upp - uc[RY - 1], c);
+        fyv[RY] = ddx<DIV>(vpp - vc[RY - 1], c);
       }
       __syncthreads();
 #pragma unroll
-      for (int j = 0; j < kRY; ++j) {
+      for (int j = 0; j < RY; ++j) {
         double fzu_p = __shfl_down_sync(0xffffffffu, fzu[j], 1);
         double fzv_p = __shfl_down_sync(0xffffffffu, fzv[j], 1);
         if (lane == 31) {
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(kTileWarps * 32)
 
 struct LaunchPlan {
   bool row;
-  int div, mul, threads, xchunk, ntiles_yz, ntiles, grid;
+  int div, mul, ry, threads, xchunk, ntiles_yz, ntiles, grid;
 };
 
 template <typename K>
@@ -344,33 +345,38 @@ int pick_xchunk(int nx, long long tiles_per_chunk_row, int resident, int forced)
   return best_xc;
 }
 
-// The instantiated (DIV, MUL) variants: (0,0) (1,0) (2,0) (3,0) (3,1) (3,2).
-template <int DIV, int MUL>
+// The instantiated (DIV, MUL, RY) variants: DIV 0..2 with (0, 4); DIV 3 with
+// MUL 0..2 and RY 2 or 4.
+template <int DIV, int MUL, int RY>
 struct Variant {
   static int resident(bool row, int threads, int *out) {
-    return row ? resident_blocks(gs3d_f64_row<DIV, MUL>, threads, out)
+    return row ? resident_blocks(gs3d_f64_row<DIV, MUL, RY>, threads, out)
                : resident_blocks(gs3d_f64_tile<DIV, MUL>, threads, out);
   }
   static void launch(const LaunchPlan &lp, cudaStream_t s, const double *u, const double *v,
                      double *un, double *vn, int nx, int ny, int nz, const Gs64 &c) {
     if (lp.row)
-      gs3d_f64_row<DIV, MUL><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz,
-                                                            lp.xchunk, lp.ntiles, c);
+      gs3d_f64_row<DIV, MUL, RY><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz,
+                                                                lp.xchunk, lp.ntiles, c);
     else
-      gs3d_f64_tile<DIV, MUL><<<lp.grid, lp.threads, 0, s>>>(u, v, un, vn, nx, ny, nz,
-                                                             lp.xchunk, lp.ntiles_yz,
-                                                             lp.ntiles, c);
+      gs3d_f64_tile<DIV, MUL><<<lp.grid, lp.threads, 0, s>>>(
+          u, v, un, vn, nx, ny, nz, lp.xchunk, lp.ntiles_yz, lp.ntiles, c);
   }
 };
 
 template <typename F>
-auto dispatch(int div, int mul, F &&f) {
-  if (div == 3 && mul == 2) return f(Variant<3, 2>());
-  if (div == 3 && mul == 1) return f(Variant<3, 1>());
-  if (div == 3) return f(Variant<3, 0>());
-  if (div == 2) return f(Variant<2, 0>());
-  if (div == 1) return f(Variant<1, 0>());
-  return f(Variant<0, 0>());
+auto dispatch(const LaunchPlan &lp, F &&f) {
+  if (lp.div == 3 && lp.ry == 2) {
+    if (lp.mul == 2) return f(Variant<3, 2, 2>());
+    if (lp.mul == 1) return f(Variant<3, 1, 2>());
+    return f(Variant<3, 0, 2>());
+  }
+  if (lp.div == 3 && lp.mul == 2) return f(Variant<3, 2, 4>());
+  if (lp.div == 3 && lp.mul == 1) return f(Variant<3, 1, 4>());
+  if (lp.div == 3) return f(Variant<3, 0, 4>());
+  if (lp.div == 2) return f(Variant<2, 0, 4>());
+  if (lp.div == 1) return f(Variant<1, 0, 4>());
+  return f(Variant<0, 0, 4>());
 }
 
 bool soft_mul_ok(double k) {  // nonzero, normal, finite
@@ -388,7 +394,10 @@ int plan_launch(int nx, int ny, int nz, const fm_gs_params *p, LaunchPlan *lp) {
   if (lp->mul && !(soft_mul_ok(p->F) && soft_mul_ok(p->F + p->k) && soft_mul_ok(p->Du) &&
                    soft_mul_ok(p->Dv) && soft_mul_ok(p->dt)))
     lp->mul = 0;  // a zero or non-normal constant: hardware multiplications
-  const bool row_ok = nz <= 256 && ny % kRY == 0;
+  lp->ry = lp->div == 3 ? fm::tune_get("gs3d_f64.ry", 2) : 4;
+  if (lp->ry != 4) lp->ry = 2;
+  if (lp->div != 3) lp->ry = 4;  // the only row-kernel shape instantiated for them
+  const bool row_ok = nz <= 256 && ny % lp->ry == 0;
   lp->row = (kind == 2 || kind == 0) && row_ok;
   if (kind == 1 || ny % kTY != 0) lp->row = false;
   if (!lp->row && ny % kTY != 0) {
@@ -400,10 +409,10 @@ int plan_launch(int nx, int ny, int nz, const fm_gs_params *p, LaunchPlan *lp) {
   lp->threads = lp->row ? nz : kTileWarps * 32;
   const bool row = lp->row;
   const int threads = lp->threads;
-  const int st = dispatch(lp->div, lp->mul,
-                          [&](auto v) { return decltype(v)::resident(row, threads, &resident); });
+  const int st =
+      dispatch(*lp, [&](auto v) { return decltype(v)::resident(row, threads, &resident); });
   if (st) return st;
-  lp->ntiles_yz = lp->row ? ny / kRY : (nz / 32) * (ny / kTY);
+  lp->ntiles_yz = lp->row ? ny / lp->ry : (nz / 32) * (ny / kTY);
   lp->xchunk = pick_xchunk(nx, lp->ntiles_yz, resident, forced);
   lp->ntiles = lp->ntiles_yz * ((nx + lp->xchunk - 1) / lp->xchunk);
   lp->grid = std::min(lp->ntiles, resident);
@@ -412,7 +421,7 @@ int plan_launch(int nx, int ny, int nz, const fm_gs_params *p, LaunchPlan *lp) {
 
 void launch(const LaunchPlan &lp, cudaStream_t s, const double *u, const double *v, double *un,
             double *vn, int nx, int ny, int nz, const Gs64 &c) {
-  dispatch(lp.div, lp.mul, [&](auto var) {
+  dispatch(lp, [&](auto var) {
     decltype(var)::launch(lp, s, u, v, un, vn, nx, ny, nz, c);
     return 0;
   });

@@ -78,7 +78,12 @@ static __device__ __noinline__ double div_slow(double x, double d) { return __dd
 static __device__ __noinline__ double mul_slow(double x, double y) { return __dmul_rn(x, y); }
 #elif defined(FM_SOFT_SLOW_SENTINEL)
 // Host checks of the fast path alone: the slow path returns a marked NaN.
-inline double sentinel() { double s; const uint64_t b = 0x7ff8dead0000beefull; memcpy(&s, &b, 8); return s; }
+inline double sentinel() {
+  double s;
+  const uint64_t b = 0x7ff8dead0000beefull;
+  memcpy(&s, &b, 8);
+  return s;
+}
 inline double div_slow(double, double) { return sentinel(); }
 inline double mul_slow(double, double) { return sentinel(); }
 #else

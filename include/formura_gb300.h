@@ -346,6 +346,8 @@ int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
  *   "gs3d_f64.mul"     with div 3: 0 hardware multiplications, 1 multiplications by the
  *                      constants F, F+k, Du, Dv, dt on the integer pipes (default), 2 all
  *                      of them
+ *   "gs3d_f64.ry"      with div 3, y cells per thread of the full-z-row kernel: 2 (3 CTAs
+ *                      per SM; default) or 4 (2 CTAs per SM)
  *   "gs3d_f64.xchunk"  x planes per CTA tile (0 = automatic)
  *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_tb_forward (1..4)
  *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)

@@ -36,17 +36,19 @@ def test_gs3d_f64_bit_exact(cuda_device, shape, steps):
     assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
 
 
-@pytest.mark.parametrize("kernel,div,mul,xchunk", [
-    (1, 0, 0, 0), (1, 1, 0, 0), (1, 2, 0, 0), (2, 0, 0, 0), (2, 1, 0, 0), (2, 2, 0, 0),
-    (2, 2, 0, 3), (1, 2, 0, 5), (1, 3, 0, 0), (2, 3, 0, 0), (2, 3, 1, 0), (2, 3, 2, 0),
-    (1, 3, 2, 0), (2, 3, 2, 3)])
-def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, mul, xchunk):
+@pytest.mark.parametrize("kernel,div,mul,xchunk,ry", [
+    (1, 0, 0, 0, 4), (1, 1, 0, 0, 4), (1, 2, 0, 0, 4), (2, 0, 0, 0, 4), (2, 1, 0, 0, 4),
+    (2, 2, 0, 0, 4), (2, 2, 0, 3, 4), (1, 2, 0, 5, 4), (1, 3, 0, 0, 4), (2, 3, 0, 0, 4),
+    (2, 3, 1, 0, 4), (2, 3, 2, 0, 4), (1, 3, 2, 0, 4), (2, 3, 2, 3, 4), (2, 3, 0, 0, 2),
+    (2, 3, 1, 0, 2), (2, 3, 2, 5, 2), (1, 3, 1, 0, 2), (2, 3, 1, 7, 2)])
+def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, mul, xchunk, ry):
     lib = _lib.lib()
     try:
         lib.fm_tune_set(b"gs3d_f64.kernel", kernel)
         lib.fm_tune_set(b"gs3d_f64.div", div)
         lib.fm_tune_set(b"gs3d_f64.mul", mul)
         lib.fm_tune_set(b"gs3d_f64.xchunk", xchunk)
+        lib.fm_tune_set(b"gs3d_f64.ry", ry)
         for shape, steps in (((24, 32, 64), 9), ((9, 16, 256), 4), ((5, 48, 32), 3)):
             U0, V0 = inits.gray_scott_3d(*shape, seed=31, ncubes=3, side=8)
             U, V = run_f64(U0, V0, steps, cuda_device)
@@ -56,7 +58,8 @@ def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, mul, xchunk)
         lib.fm_tune_clear()
 
 
-@pytest.fixture(params=[(1, 0), (3, 0), (3, 2)], ids=["div1", "softdiv", "softdiv_softmul"])
+@pytest.fixture(params=[(1, 0), (3, 0), (3, 1), (3, 2)],
+                ids=["div1", "softdiv", "softdiv_softkmul", "softdiv_softmul"])
 def arith(request):
     """Division / multiplication forms of the FP64 kernel (gs3d_f64.div, .mul)."""
     lib = _lib.lib()

@@ -140,3 +140,4 @@ def test_mul_matches_ieee(lib):
     lib.softfp_mul(_p(xs), _p(ys), xs.size, _p(got))
     ok, bad = same_bits(got, want, normal(xs) & normal(ys))
     assert ok, (xs[bad[:5]], ys[bad[:5]], got[bad[:5]], want[bad[:5]])
+
