@@ -128,8 +128,8 @@ def measure_fma_peak(torch, kernels, fp64: bool, sms: int):
 
 
 def read_profile_traffic():
-    """dram bytes per launch of gs3d_f64_step from the committed ncu summary."""
-    p = ROOT / "profiles" / "gs3d_f64_step_256.md"
+    """dram bytes per launch of gs3d_f64_row from the committed ncu summary."""
+    p = ROOT / "profiles" / "gs3d_f64_row_256.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
