@@ -39,7 +39,7 @@ import itertools
 import os
 import subprocess
 from pathlib import Path
-from typing import Dict, List, Optional, Sequence
+from typing import Dict, List, Optional, Sequence, Tuple
 
 from . import build as _build
 
@@ -56,6 +56,8 @@ class Program:
       * ``gs3d_f32k_tb`` — the float fast form with Kahan accumulation,
         temporally blocked (``temporal_blocking_interval`` > 1 -> depth <= 4)
       * ``diff2d_f64`` — examples/diffusion.fmr form in 2D, double
+      * ``fmr``        — any program: ``fmr_source`` is compiled by the front end
+        (formura_gb300.fmr) into generated CUDA kernels
     ``constants`` are the .fmr constants of ``step`` (F, k, Du, Dv, dt, dx /
     Dt, Dx).  ``intra_node_shape``, ``mpi_grid_shape``, ``monitor_interval``
     and ``temporal_blocking_interval`` are the YAML keys of
@@ -70,6 +72,7 @@ class Program:
     temporal_blocking_interval: int = 1
     mpi_grid_shape: Optional[Sequence[int]] = None
     axes: Optional[Sequence[str]] = None
+    fmr_source: Optional[str] = None  # form "fmr": the program text
 
     @property
     def dim(self) -> int:
@@ -77,7 +80,21 @@ class Program:
 
     @property
     def axis_names(self) -> List[str]:
+        if self.form == "fmr":
+            return list(self.compiled().axes)
         return list(self.axes) if self.axes else list(AXES3[: self.dim])
+
+    def compiled(self):
+        """The manifested program of a form-"fmr" Program (cached)."""
+        from .fmr import compile_source
+
+        return compile_source(self.fmr_source, tuple(self.shape))
+
+    def states(self) -> List[Tuple[str, str]]:
+        """(name, C element type) of every global state array."""
+        if self.form == "fmr":
+            return list(self.compiled().state)
+        return [(n, self.elem) for n in self.state_names + self.extra_state_names]
 
     @property
     def shape(self) -> List[int]:
@@ -109,6 +126,13 @@ class Program:
             raise ValueError(
                 "%s: mpi_grid_shape %s — this engine runs one GPU per program; the "
                 "domain is periodic on that GPU (use [1,...])" % (self.name, list(self.mpi_grid_shape)))
+        if self.form == "fmr":
+            if not self.fmr_source:
+                raise ValueError("%s: form fmr needs fmr_source" % self.name)
+            if self.monitor_interval < 1:
+                raise ValueError("%s: monitor_interval must be >= 1" % self.name)
+            self.compiled()
+            return
         if self.form not in FORMS:
             raise ValueError("%s: unknown form %r (known: %s)" % (self.name, self.form, sorted(FORMS)))
         want_dim = FORMS[self.form]["dim"]
@@ -158,8 +182,8 @@ def emit_header(p: Program) -> str:
     for a, n in zip(ax, p.shape):
         lines.append("#define N%s  %d" % (a.upper(), n))
     lines.append("")
-    for s in p.state_names + p.extra_state_names:
-        lines.append("extern %s %s%s;" % (p.elem, s, dims))
+    for s, t in p.states():
+        lines.append("extern %s %s%s;" % (t, s, dims))
     lines.append("")
     lines.append("struct Formura_Navigator {")
     lines.append("int time_step;")
@@ -237,43 +261,111 @@ def _work_elems(p: Program) -> str:
     return "NCELLS"
 
 
+def _fmr_parts(p: Program):
+    """Kernels, device buffers and the step loop of a form-"fmr" program."""
+    from .fmr.emit_cuda import emit_kernels
+
+    mmp = p.compiled()
+    kern, levels = emit_kernels(mmp)
+    states = [n for n, _ in mmp.state]
+    sidx = {n: i for i, n in enumerate(states)}
+    arrays = sorted(mmp.arrays.values(), key=lambda a: a.node)
+    aidx = {a.node: i for i, a in enumerate(arrays if arrays else [])}
+    alloc = ["  for (int i = 0; i < kNState; ++i)",
+             '    if ((st = fm_malloc(&g_next[i], kBytes[i]))) return fail(st, "fm_malloc(next)");']
+    inner = [a for a in arrays if a.store_of is None]
+    for a in inner:
+        alloc.append('  if ((st = fm_malloc(&g_arr[%d], NCELLS * sizeof(%s)))) return fail(st, "fm_malloc(array)");'
+                     % (aidx[a.node], a.ctype))
+    alloc.append("  { int dev = 0; cudaGetDevice(&dev); int sms = 0;"
+                 " cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);"
+                 " long long need = ((long long)NCELLS + 255) / 256;"
+                 " g_grid = (int)(need < (long long)sms * 16 ? need : (long long)sms * 16); }")
+    run = ["  cudaStream_t s = (cudaStream_t)g_stream;",
+           "  for (int t = 0; t < steps; ++t) {"]
+    for kname, sn, ar, aw in levels:
+        args = ["(const %s*)g_dev[%d]" % (dict(mmp.state)[n], sidx[n]) for n in sn]
+        args += ["(const %s*)g_arr[%d]" % (mmp.arrays[x].ctype, aidx[x]) if mmp.arrays[x].store_of is None
+                 else "(const %s*)g_next[%d]" % (mmp.arrays[x].ctype, sidx[mmp.arrays[x].store_of])
+                 for x in ar]
+        for arr in aw:
+            if arr.store_of is None:
+                args.append("(%s*)g_arr[%d]" % (arr.ctype, aidx[arr.node]))
+            else:
+                args.append("(%s*)g_next[%d]" % (arr.ctype, sidx[arr.store_of]))
+        run.append("    %s<<<g_grid, 256, 0, s>>>(%s);" % (kname, ", ".join(args)))
+    run += ["    for (int i = 0; i < kNState; ++i) { void *x = g_dev[i]; g_dev[i] = g_next[i]; g_next[i] = x; }",
+            "  }",
+            "  cudaError_t e = cudaGetLastError();",
+            "  if (e != cudaSuccess) {",
+            '    snprintf(g_msg, sizeof g_msg, "generated kernels: %s", cudaGetErrorString(e));',
+            "    return FM_ERR_CUDA;",
+            "  }",
+            "  return 0;"]
+    free = ["  for (int i = 0; i < kNState; ++i) { fm_free(g_next[i]); g_next[i] = 0; }"]
+    free += ["  fm_free(g_arr[%d]); g_arr[%d] = 0;" % (aidx[a.node], aidx[a.node]) for a in inner]
+    decls = ["static void *g_next[%d] = {0};" % max(1, len(states)),
+             "static void *g_arr[%d] = {0};" % max(1, len(arrays)),
+             "static int g_grid = 1;"]
+    return kern, decls, alloc, run, free
+
+
 def emit_source(p: Program) -> str:
+    """The host side of the generated-code API (``<name>.cpp``, or for form
+    "fmr" ``<name>.cu`` with the generated kernels in front of it)."""
     p.validate()
     dims = "".join("[%d]" % n for n in p.shape)
-    states = p.state_names + p.extra_state_names
+    states = p.states()
     ncells = 1
     for n in p.shape:
         ncells *= n
     ax = p.axis_names
+    fmr = p.form == "fmr"
     out: List[str] = []
     w = out.append
-    w("/* %s.cpp — emitted by formura_gb300.backend (form %s).\n"
+    w("/* %s.%s — emitted by formura_gb300.backend (form %s).\n"
       " * Host side of Formura's generated-code API on one GB300; the time steps run\n"
-      " * in libformura_gb300.so (include/formura_gb300.h). */" % (p.name, p.form))
+      " * in %s. */" % (p.name, "cu" if fmr else "cpp", p.form,
+                       "the kernels generated below" if fmr else
+                       "libformura_gb300.so (include/formura_gb300.h)"))
     w('#include "%s.h"' % p.name)
     w('#include "formura_gb300.h"')
     w("#include <math.h>")
     w("#include <stddef.h>")
     w("#include <stdio.h>")
+    if fmr:
+        w("#include <cuda_runtime.h>")
+        w('#include "fm_softfp.cuh"')
     w("")
     w("#define NCELLS ((size_t)%d)" % ncells)
     w("#define FMR_EXPORT __attribute__((visibility(\"default\")))")
     w("")
+    if fmr:
+        kern, decls, alloc, run, free = _fmr_parts(p)
+        w("namespace {")
+        w(kern)
+        w("}  // namespace")
+        w("")
     w('extern "C" {')
-    for s in states:
-        w("FMR_EXPORT %s %s%s __attribute__((aligned(4096)));" % (p.elem, s, dims))
+    for sname, t in states:
+        w("FMR_EXPORT %s %s%s __attribute__((aligned(4096)));" % (t, sname, dims))
     w("FMR_EXPORT struct Formura_Navigator navi;")
     w("}")
     w("")
     w("static const int kNState = %d;" % len(states))
-    w("static void *const kHost[%d] = {%s};" % (len(states), ", ".join("(void*)%s" % s for s in states)))
+    w("static void *const kHost[%d] = {%s};" % (len(states), ", ".join("(void*)%s" % n for n, _ in states)))
+    w("static const size_t kBytes[%d] = {%s};" % (len(states), ", ".join("NCELLS * sizeof(%s)" % t for _, t in states)))
+    w("static const int kIsDouble[%d] = {%s};" % (len(states), ", ".join("1" if t == "double" else "0" for _, t in states)))
+    w("static const int kIsFloat[%d] = {%s};" % (len(states), ", ".join("1" if t == "float" else "0" for _, t in states)))
     w("static void *g_dev[%d] = {0};" % len(states))
     w("static void *g_work = 0;")
     w("static double *g_totals = 0;   /* device: per-state totals + scratch */")
     w("static void *g_stream = 0;")
     w("static int g_ready = 0;")
     w("static char g_msg[600];")
-    w("static const size_t kBytes = NCELLS * sizeof(%s);" % p.elem)
+    if fmr:
+        for d in decls:
+            w(d)
     w("")
     w("static int fail(int st, const char *where) {")
     w('  snprintf(g_msg, sizeof g_msg, "%s: %s (%s)", where, fm_status_name(st), fm_last_error());')
@@ -284,11 +376,15 @@ def emit_source(p: Program) -> str:
     w("  if (g_ready) return 0;")
     w("  int st;")
     w("  for (int i = 0; i < kNState; ++i) {")
-    w('    if ((st = fm_malloc(&g_dev[i], kBytes))) return fail(st, "fm_malloc(state)");')
-    w("    fm_host_register(kHost[i], kBytes);  /* pinned: best effort */")
+    w('    if ((st = fm_malloc(&g_dev[i], kBytes[i]))) return fail(st, "fm_malloc(state)");')
+    w("    fm_host_register(kHost[i], kBytes[i]);  /* pinned: best effort */")
     w("  }")
-    w('  if ((st = fm_malloc(&g_work, (%s) * sizeof(%s)))) return fail(st, "fm_malloc(work)");'
-      % (_work_elems(p), p.elem))
+    if fmr:
+        for line in alloc:
+            w(line)
+    else:
+        w('  if ((st = fm_malloc(&g_work, (%s) * sizeof(%s)))) return fail(st, "fm_malloc(work)");'
+          % (_work_elems(p), p.elem))
     w("  const size_t scratch = fm_sum_f64_scratch_elems((int64_t)NCELLS);")
     w('  if ((st = fm_malloc((void**)&g_totals, (kNState + scratch) * sizeof(double)))) return fail(st, "fm_malloc(totals)");')
     w("  g_ready = 1;")
@@ -296,7 +392,11 @@ def emit_source(p: Program) -> str:
     w("}")
     w("")
     w("static int run_steps(int steps) {")
-    w("  %s" % _forward_call(p))
+    if fmr:
+        for line in run:
+            w(line)
+    else:
+        w("  %s" % _forward_call(p))
     w("}")
     w("")
     w('extern "C" {')
@@ -316,14 +416,14 @@ def emit_source(p: Program) -> str:
     w("FMR_EXPORT int Formura_Upload (void) {")
     w("  int st = ensure_device(); if (st) return st;")
     w("  for (int i = 0; i < kNState; ++i)")
-    w('    if ((st = fm_memcpy_h2d(g_dev[i], kHost[i], kBytes, g_stream))) return fail(st, "upload");')
+    w('    if ((st = fm_memcpy_h2d(g_dev[i], kHost[i], kBytes[i], g_stream))) return fail(st, "upload");')
     w("  return 0;")
     w("}")
     w("")
     w("FMR_EXPORT int Formura_Download (void) {")
     w("  int st = ensure_device(); if (st) return st;")
     w("  for (int i = 0; i < kNState; ++i)")
-    w('    if ((st = fm_memcpy_d2h(kHost[i], g_dev[i], kBytes, g_stream))) return fail(st, "download");')
+    w('    if ((st = fm_memcpy_d2h(kHost[i], g_dev[i], kBytes[i], g_stream))) return fail(st, "download");')
     w('  if ((st = fm_stream_sync(g_stream))) return fail(st, "download sync");')
     w("  return 0;")
     w("}")
@@ -355,14 +455,14 @@ def emit_source(p: Program) -> str:
     w("FMR_EXPORT int Formura_Conserved_Totals (double *totals) {")
     w("  int st = ensure_device(); if (st) return st;")
     w("  if (!totals) return fail(FM_ERR_ARG, \"Formura_Conserved_Totals: NULL\");")
-    if p.elem == "double":
-        w("  for (int i = 0; i < kNState; ++i)")
-        w("    if ((st = fm_sum_f64((int64_t)NCELLS, (const double*)g_dev[i], g_totals + kNState, g_totals + i, g_stream)))")
-        w('      return fail(st, "fm_sum_f64");')
-    else:
-        w("  for (int i = 0; i < kNState; ++i)")
-        w("    if ((st = fm_sum_f32_as_f64((int64_t)NCELLS, (const float*)g_dev[i], g_totals + kNState, g_totals + i, g_stream)))")
-        w('      return fail(st, "fm_sum_f32_as_f64");')
+    w("  if ((st = fm_memset(g_totals, 0, kNState * sizeof(double), g_stream))) return fail(st, \"totals\");")
+    w("  for (int i = 0; i < kNState; ++i) {")
+    w("    if (kIsDouble[i])")
+    w("      st = fm_sum_f64((int64_t)NCELLS, (const double*)g_dev[i], g_totals + kNState, g_totals + i, g_stream);")
+    w("    else if (kIsFloat[i])")
+    w("      st = fm_sum_f32_as_f64((int64_t)NCELLS, (const float*)g_dev[i], g_totals + kNState, g_totals + i, g_stream);")
+    w('    if (st) return fail(st, "conserved totals");')
+    w("  }")
     w('  if ((st = fm_memcpy_d2h(totals, g_totals, kNState * sizeof(double), g_stream))) return fail(st, "totals");')
     w('  if ((st = fm_stream_sync(g_stream))) return fail(st, "totals sync");')
     w("  for (int i = 0; i < kNState; ++i) if (!isfinite(totals[i])) return fail(FM_ERR_NONFINITE, \"non-finite state\");")
@@ -374,6 +474,9 @@ def emit_source(p: Program) -> str:
     w("  fm_stream_sync(g_stream);")
     w("  for (int i = 0; i < kNState; ++i) { fm_free(g_dev[i]); g_dev[i] = 0; fm_host_unregister(kHost[i]); }")
     w("  fm_free(g_work); g_work = 0; fm_free(g_totals); g_totals = 0;")
+    if fmr:
+        for line in free:
+            w(line)
     w("  g_ready = 0;")
     w("  return 0;")
     w("}")
@@ -403,14 +506,25 @@ def build_program(p: Program, outdir: Optional[Path] = None, verbose: bool = Fal
     if so.exists() and stamp.exists() and stamp.read_text() == key:
         return so
     (outdir / (p.name + ".h")).write_text(hdr)
-    (outdir / (p.name + ".cpp")).write_text(src)
-    cmd = [
-        os.environ.get("CXX", "g++"), "-O2", "-fPIC", "-shared", "-std=c++17",
-        "-fvisibility=hidden", "-I", str(outdir), "-I", str(_build.INCLUDE),
-        "-o", str(so) + ".tmp", str(outdir / (p.name + ".cpp")),
-        "-L", str(lib.parent), "-lformura_gb300",
-        "-Wl,-rpath," + str(lib.parent), "-lm",
-    ]
+    if p.form == "fmr":
+        # generated kernels: nvcc with the library's flags (sm_103a, no FMA contraction)
+        (outdir / (p.name + ".cu")).write_text(src)
+        cmd = [
+            _build._nvcc(), *_build.NVCC_FLAGS, "-shared", "-I", str(outdir),
+            "-I", str(_build.INCLUDE), "-I", str(_build.CSRC),
+            "-o", str(so) + ".tmp", str(outdir / (p.name + ".cu")),
+            "-L", str(lib.parent), "-lformura_gb300", "-cudart=shared",
+            "-Xlinker", "-rpath," + str(lib.parent),
+        ]
+    else:
+        (outdir / (p.name + ".cpp")).write_text(src)
+        cmd = [
+            os.environ.get("CXX", "g++"), "-O2", "-fPIC", "-shared", "-std=c++17",
+            "-fvisibility=hidden", "-I", str(outdir), "-I", str(_build.INCLUDE),
+            "-o", str(so) + ".tmp", str(outdir / (p.name + ".cpp")),
+            "-L", str(lib.parent), "-lformura_gb300",
+            "-Wl,-rpath," + str(lib.parent), "-lm",
+        ]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError("building %s failed:\n%s" % (p.name, r.stdout))

@@ -1,0 +1,207 @@
+"""CUDA code generation for a manifested Formura program.
+
+One kernel per level of the manifested program (mm.Level): every thread
+evaluates the level's cell program for one cell and writes each of the
+level's arrays.  Arrays are dense, row-major, last axis fastest, with
+periodic boundaries: a read at cursor c of axis a uses the wrapped coordinate
+(x_a + c) mod N_a, computed once per (axis, cursor) per cell.  The grid
+shape is a compile-time constant of the generated file.
+
+Arithmetic keeps the C semantics of the reference's generated code
+(src/Formura/MPICxx/Translate.hs:568-620): one IEEE operation per node in
+the node's C type, ``**`` -> ``pow``, ``>?``/``<?`` -> right-folded
+``fmax``/``fmin`` chains, ``<%`` -> ``fmin(0, fmax(..)) + fmax(0, fmin(..))``,
+``if`` -> ``?:``, extern functions called on doubles.  The file is compiled
+with ``--fmad=false``, so no multiply-add is contracted.  Two exact
+substitutions are made (bit-identical results, see csrc/fm_softfp.cuh):
+a division by a positive normal constant runs as ``fm::soft::div_const_s``
+and a multiplication of a double by a nonzero normal double constant as
+``fm::soft::mul_const_s``, both on the integer pipes.
+"""
+from __future__ import annotations
+
+import math
+import struct
+from typing import Dict, List, Sequence, Tuple
+
+from . import mm as MM
+
+AXVARS = ["c%d" % i for i in range(8)]
+
+
+def _double_fields(d: float):
+    b = struct.unpack("<Q", struct.pack("<d", d))[0]
+    return b, (b & ((1 << 52) - 1)) | (1 << 52), (b >> 52) & 0x7FF
+
+
+def div_const_fields(d: float) -> str:
+    """Initializer of fm::soft::DivConstS for a positive normal d."""
+    _, md, ed = _double_fields(d)
+    R = -(-(1 << 115) // md)
+    return "{%du, %du, %du, %du, %d, %s}" % (R >> 32, R & 0xFFFFFFFF, md >> 32, md & 0xFFFFFFFF,
+                                           ed, float(d).hex())
+
+
+def mul_const_fields(y: float) -> str:
+    """Initializer of fm::soft::MulConstS for a nonzero normal y."""
+    b, my, ey = _double_fields(y)
+    bb = my << 11
+    return "{%du, %du, %du, %du, %du, %d, %s}" % (bb >> 32, bb & 0xFFFFFFFF, my >> 32,
+                                                 my & 0xFFFFFFFF, (b >> 32) & 0x80000000, ey,
+                                                 float(y).hex())
+
+
+def _normal_double(v) -> bool:
+    if not isinstance(v, float):
+        return False
+    a = abs(v)
+    return math.isfinite(a) and a >= 2.2250738585072014e-308
+
+
+def _wrap_name(ax: int, c: int) -> str:
+    if c == 0:
+        return AXVARS[ax]
+    return "%s_%s%d" % (AXVARS[ax], "p" if c > 0 else "m", abs(c))
+
+
+class LevelEmitter:
+    def __init__(self, mmp: MM.MMProgram, level: MM.Level, li: int, soft_div: bool,
+                 soft_mul: bool):
+        self.mmp, self.level, self.li = mmp, level, li
+        self.soft_div, self.soft_mul = soft_div, soft_mul
+        self.shape = mmp.shape
+        self.dim = mmp.dim
+
+    def idx_expr(self, cursor: Sequence[int]) -> str:
+        parts = [_wrap_name(a, c) for a, c in enumerate(cursor)]
+        e = "(size_t)%s" % parts[0]
+        for a in range(1, self.dim):
+            e = "(%s * %d + %s)" % (e, self.shape[a], parts[a])
+        return e
+
+    def emit(self) -> Tuple[str, List[str], List[int], List[MM.Array]]:
+        L = self.level
+        state_names = sorted({s for s, _ in L.reads_state})
+        arr_ids = sorted({a for a, _ in L.reads_arrays})
+        stypes = dict(self.mmp.state)
+        params = []
+        for s in state_names:
+            params.append("const %s *__restrict__ s_%s" % (stypes[s], s))
+        for a in arr_ids:
+            arr = self.mmp.arrays[a]
+            params.append("const %s *__restrict__ r_%s" % (arr.ctype, arr.name))
+        for arr in L.arrays:
+            params.append("%s *__restrict__ w_%s" % (arr.ctype, arr.name))
+        ncells = 1
+        for n in self.shape:
+            ncells *= n
+        body: List[str] = []
+        w = body.append
+        # coordinates
+        w("    size_t rest = (size_t)idx;")
+        for a in reversed(range(self.dim)):
+            if a == 0:
+                w("    const int %s = (int)rest;" % AXVARS[a])
+            else:
+                w("    const int %s = (int)(rest %% %du); rest /= %du;" % (AXVARS[a], self.shape[a],
+                                                                       self.shape[a]))
+        needed = set()
+        for m in L.micro:
+            if m.kind in ("loadS", "loadM"):
+                for a, c in enumerate(m.args[0]):
+                    if c:
+                        needed.add((a, c))
+        for a, c in sorted(needed):
+            n = self.shape[a]
+            v = _wrap_name(a, c)
+            if abs(c) < n:
+                if c > 0:
+                    w("    const int %s = %s + %d >= %d ? %s + %d : %s + %d;" %
+                      (v, AXVARS[a], c, n, AXVARS[a], c - n, AXVARS[a], c))
+                else:
+                    w("    const int %s = %s - %d < 0 ? %s + %d : %s - %d;" %
+                      (v, AXVARS[a], -c, AXVARS[a], n + c, AXVARS[a], -c))
+            else:
+                w("    const int %s = ((%s + %d) %% %d + %d) %% %d;" % (v, AXVARS[a], c, n, n, n))
+        const_vals: Dict[int, object] = {}
+        for i, m in enumerate(L.micro):
+            t = m.ctype
+            name = "a%d" % i
+            k = m.kind
+            if k == "const":
+                const_vals[i] = m.args[0]
+                w("    const %s %s = %s;" % (t, name, MM.c_literal(m.args[0], t)))
+            elif k == "loadS":
+                w("    const %s %s = s_%s[%s];" % (t, name, m.args[1], self.idx_expr(m.args[0])))
+            elif k == "loadM":
+                arr = self.mmp.arrays[m.args[1]]
+                w("    const %s %s = r_%s[%s];" % (t, name, arr.name, self.idx_expr(m.args[0])))
+            elif k == "index":
+                w("    const %s %s = (%s)%s;" % (t, name, t, AXVARS[m.args[0]]))
+            elif k == "uni":
+                op, a = m.args
+                if op.startswith("external-call/"):
+                    f = op.split("/", 1)[1]
+                    w("    const %s %s = %s((double)a%d);" % (t, name, f, a))
+                else:
+                    w("    const %s %s = (%sa%d);" % (t, name, op, a))
+            elif k == "bin":
+                op, a, b = m.args
+                ta, tb = L.micro[a].ctype, L.micro[b].ctype
+                if op == "**":
+                    w("    const %s %s = pow((double)a%d, (double)a%d);" % (t, name, a, b))
+                elif (op == "/" and self.soft_div and t == "double" and ta == "double" and
+                      b in const_vals and _normal_double(const_vals[b]) and const_vals[b] > 0):
+                    w("    const %s %s = fm::soft::div_const_s(a%d, fm::soft::DivConstS%s);" %
+                      (t, name, a, div_const_fields(const_vals[b])))
+                elif (op == "*" and self.soft_mul and t == "double" and
+                      ((b in const_vals and ta == "double" and _normal_double(const_vals[b])) or
+                       (a in const_vals and tb == "double" and _normal_double(const_vals[a])))):
+                    x, c = (a, b) if b in const_vals else (b, a)
+                    w("    const %s %s = fm::soft::mul_const_s(a%d, fm::soft::MulConstS%s);" %
+                      (t, name, x, mul_const_fields(const_vals[c])))
+                else:
+                    w("    const %s %s = (a%d %s a%d);" % (t, name, a, op, b))
+            elif k == "ite":
+                c, a, b = m.args
+                w("    const %s %s = (a%d ? a%d : a%d);" % (t, name, c, a, b))
+            elif k == "nary":
+                op, xs = m.args
+                names = ["(double)a%d" % x for x in xs]
+
+                def chain(fn, items):
+                    acc = items[-1]
+                    for it in reversed(items[:-1]):
+                        acc = "%s(%s, %s)" % (fn, it, acc)
+                    return acc
+
+                if op == ">?":
+                    e = chain("fmax", names)
+                elif op == "<?":
+                    e = chain("fmin", names)
+                else:
+                    e = "fmin(0.0, %s) + fmax(0.0, %s)" % (chain("fmax", names), chain("fmin", names))
+                w("    const %s %s = %s;" % (t, name, e))
+            else:
+                raise MM.OM.FmrSemanticError("cannot emit %s" % k)
+        for arr in L.arrays:
+            w("    w_%s[idx] = a%d;" % (arr.name, arr.root))
+        kname = "fmr_level_%d" % self.li
+        src = ["__global__ void __launch_bounds__(256) %s(%s) {" % (kname, ", ".join(params)),
+               "  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < %dll;"
+               " idx += (long long)gridDim.x * blockDim.x) {" % ncells]
+        src += body
+        src += ["  }", "}", ""]
+        return "\n".join(src), state_names, arr_ids, L.arrays
+
+
+def emit_kernels(mmp: MM.MMProgram, soft_div: bool = True, soft_mul: bool = True):
+    """Kernel source and, per level, (kernel name, state names read, arrays
+    read, arrays written)."""
+    parts = []
+    levels = []
+    for li, L in enumerate(mmp.levels):
+        src, sn, ar, aw = LevelEmitter(mmp, L, li, soft_div, soft_mul).emit()
+        parts.append(src)
+        levels.append(("fmr_level_%d" % li, sn, ar, aw))
+    return "\n".join(parts), levels

@@ -22,6 +22,10 @@ from ._lib import FormuraError, STATUS_NAMES, lib as _core_lib
 from .backend import Program, _delta_name
 
 
+_C_TYPES = {"double": (ctypes.c_double, np.float64), "float": (ctypes.c_float, np.float32),
+            "int": (ctypes.c_int, np.int32), "bool": (ctypes.c_bool, np.bool_)}
+
+
 def navigator_type(p: Program):
     fields = [("time_step", ctypes.c_int)]
     for a in p.axis_names:
@@ -55,11 +59,11 @@ class FormuraProgram:
         L.Formura_Set_Stream.argtypes = [ctypes.c_void_p]
         L.Formura_Conserved_Totals.argtypes = [ctypes.POINTER(ctypes.c_double)]
         L.Formura_Last_Error.restype = ctypes.c_char_p
-        ctype = ctypes.c_float if program.elem == "float" else ctypes.c_double
-        dtype = np.float32 if program.elem == "float" else np.float64
         n = int(np.prod(program.shape))
         self.state: Dict[str, np.ndarray] = {}
-        for s in program.state_names + program.extra_state_names:
+        self.state_names = [s for s, _ in program.states()]
+        for s, t in program.states():
+            ctype, dtype = _C_TYPES[t]
             buf = (ctype * n).in_dll(L, s)
             self.state[s] = np.frombuffer(buf, dtype=dtype).reshape(program.shape)
         self.steps_per_forward = program.steps_per_forward
@@ -98,7 +102,7 @@ class FormuraProgram:
         self._check(self.lib.Formura_Set_Stream(ctypes.c_void_p(stream_ptr)), "Formura_Set_Stream")
 
     def conserved_totals(self) -> np.ndarray:
-        k = len(self.program.state_names) + len(self.program.extra_state_names)
+        k = len(self.state_names)
         out = (ctypes.c_double * k)()
         self._check(self.lib.Formura_Conserved_Totals(out), "Formura_Conserved_Totals")
         return np.array(out[:], dtype=np.float64)

@@ -1,0 +1,189 @@
+"""The .fmr front end (formura_gb300/fmr) on the CPU.
+
+Parser: the operator table and statement forms of src/Formura/Parser.hs.
+Evaluation and manifestation: through the C oracle (oracle/fmr_c.py), the
+front end reproduces bit for bit
+  * the reference's generated examples-generated/pearson.c (golden SHA-256s
+    in tests/golden/pearson_ref.json; the .fmr is read from the reference tree
+    when it is present),
+  * the hand-written restatements of the pearson-3d form (oracle.gs3d_f64),
+    of the diffusion form (oracle.diff2d_f64) and of examples/3d-mhd-rk4.fmr
+    (oracle.mhd_f64; reference tree needed for the .fmr).
+"""
+import hashlib
+import json
+import shutil
+import subprocess
+from fractions import Fraction
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from formura_gb300 import backend, inits
+from formura_gb300.fmr import compile_source, config, load_program, mm, om
+from formura_gb300.fmr import parser as P
+from oracle import fmr_c, oracle
+
+ROOT = Path(__file__).resolve().parents[1]
+EX = ROOT / "examples"
+REF = Path("/root/reference")
+GS = dict(F=0.04, k=0.06, Du=2e-5, Dv=1e-5, dt=0.5, dx=0.01)
+
+
+def sha(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+# -- parser -------------------------------------------------------------------------
+
+def expr(src):
+    return P.Parser(src).rexpr()
+
+
+def test_operator_precedence():
+    # unary minus is looser than * (Parser.hs:201-203): -U*V*V = -((U*V)*V)
+    e = expr("-U * V*V + F * (1-U)")
+    assert isinstance(e, P.Binop) and e.op == "+"
+    assert isinstance(e.a, P.Unop) and e.a.op == "-"
+    assert e.a.a == P.Binop("*", P.Binop("*", P.Ident("U"), P.Ident("V")), P.Ident("V"))
+    # application binds tighter than '.', '.' tighter than '*'
+    e = expr("(∂ i . ∂ i) U")
+    assert isinstance(e, P.Apply) and isinstance(e.f, P.Binop) and e.f.op == "."
+    # a chain of one min/max operator is one n-ary node; comparison is loosest
+    e = expr("a >? b >? c <= d")
+    assert e.op == "<=" and isinstance(e.a, P.Nary) and len(e.a.items) == 3
+    e = expr("a <% b <% c")
+    assert isinstance(e, P.Nary) and e.op == "<%" and len(e.items) == 3
+    # ** is left-assoc and above *
+    e = expr("2 * a ** 2 ** 3")
+    assert e.op == "*" and e.b.op == "**" and e.b.a.op == "**"
+
+
+def test_grid_indices_and_statements():
+    e = expr("a[i+1/2, j] - a[, j-3/2]")
+    assert e.a.entries == [("i", Fraction(1, 2)), ("j", Fraction(0))]
+    assert e.b.entries == [(None, Fraction(0)), ("j", Fraction(-3, 2))]
+    prog = P.parse("dimension :: 1\naxes :: x\n# comment\n"
+                   "double :: a = 1, b   # typed, one without value\n"
+                   "manifest :: m = a + \\\n  b\n"
+                   "begin function y = f(x)\n  y = x\nend function\n"
+                   "begin function g(x, z) returns (z, x)\nend function\n")
+    assert prog.dimension == 1 and prog.axes == ["x"]
+    kinds = [type(s).__name__ for s in prog.stmts]
+    assert kinds == ["TypeDecl", "TypeDecl", "Subst", "TypeDecl", "Subst", "Subst", "Subst"]
+    assert prog.stmts[3].modifiers == ["manifest"]
+    f = prog.stmts[5].rhs
+    assert isinstance(f, P.Lambda) and isinstance(f.body, P.Let)
+
+
+def test_parses_every_example():
+    files = sorted(EX.glob("*.fmr"))
+    if (REF / "examples").exists():
+        files += sorted((REF / "examples").glob("*.fmr"))
+    # outdated in-file configuration syntax or a syntax stress test: the
+    # reference's own grammar rejects these too
+    rejected = {"av-mhd-3d.fmr", "hydro.fmr", "mhd.fmr", "test.fmr"}
+    for f in files:
+        if f.name in rejected:
+            with pytest.raises(P.FmrSyntaxError):
+                P.parse_file(f)
+        else:
+            P.parse_file(f)
+
+
+# -- evaluation -------------------------------------------------------------------------
+
+def test_half_offsets_become_shifts():
+    src = ("dimension :: 1\naxes :: x\n"
+           "begin function init() returns u\n double [] :: u = 0\nend function\n"
+           "begin function step(u) returns u_next\n"
+           "  f = u[i+1/2] - u[i-1/2]\n  u_next = f[i+1/2] - f[i-1/2]\nend function\n")
+    omp = om.build_om(P.parse(src), [8])
+    shifts = sorted(n.args[0] for n in omp.step.nodes if n.kind == "shift")
+    assert shifts == [(-1,), (1,)]
+    mmp = mm.manifest(omp, [8])
+    cursors = sorted(m.args[0] for m in mmp.levels[0].micro if m.kind == "loadS")
+    assert cursors == [(-1,), (0,), (1,)]
+
+
+def test_type_errors_are_reported():
+    bad = ("dimension :: 1\naxes :: x\n"
+           "begin function init() returns u\n double [] :: u = 0\nend function\n"
+           "begin function step(u) returns u_next\n  u_next = u + u[i+1/2]\nend function\n")
+    with pytest.raises(om.FmrSemanticError):
+        om.build_om(P.parse(bad), [8])
+    with pytest.raises(om.FmrSemanticError):
+        om.build_om(P.parse(bad.replace("u + u[i+1/2]", "v")), [8])
+
+
+def test_config_reader():
+    cfg = config.loads("initial_walls:\n  x: [136]\n  z: [100,180]\nintra_node_shape: [256, 8]\n"
+                       "monitor_interval: 64  # comment\noption_strings: ['omp', 'nbux2']\n")
+    assert cfg == {"initial_walls": {"x": [136], "z": [100, 180]}, "intra_node_shape": [256, 8],
+                   "monitor_interval": 64, "option_strings": ["omp", "nbux2"]}
+
+
+def test_constants_follow_c_semantics():
+    # folded on the host: the same double operations (and libm pow) as the C
+    src = (EX / "fmr-features.fmr").read_text()
+    mmp = compile_source(src, (40, 24))
+    consts = {m.args[0] for L in mmp.levels for m in L.micro if m.kind == "const"}
+    assert 0.25 ** 2 + 1.0 / 3.0 in consts
+
+
+# -- pins through the C oracle ------------------------------------------------------------
+
+def test_gray_scott_3d_matches_hand_oracle():
+    o = fmr_c.FmrOracle((EX / "gray-scott-3d.fmr").read_text(), [16, 16, 32])
+    U0, V0 = inits.gray_scott_3d(16, 16, 32, seed=3, ncubes=2, side=6)
+    out = o.run({"U": U0, "V": V0}, 20)
+    Uo, Vo = oracle.gs3d_f64(U0, V0, 20, **GS)
+    assert np.array_equal(out["U"], Uo) and np.array_equal(out["V"], Vo)
+
+
+def test_diffusion_2d_matches_hand_oracle():
+    o = fmr_c.FmrOracle((EX / "diffusion-2d.fmr").read_text(), [64, 48])
+    d0 = inits.diffusion_2d(64, 48, seed=2)
+    assert np.array_equal(o.run({"dens": d0}, 30)["dens"], oracle.diff2d_f64(d0, 30, Dt=0.4, Dx=1.0))
+
+
+@pytest.mark.skipif(not (REF / "examples-generated" / "pearson.fmr").exists(),
+                    reason="reference tree not present")
+def test_pearson_fmr_reproduces_reference_generated_c():
+    g = json.loads((ROOT / "tests" / "golden" / "pearson_ref.json").read_text())
+    o = fmr_c.FmrOracle((REF / "examples-generated" / "pearson.fmr").read_text(),
+                        [g["n"], g["n"]])
+    for case in g["cases"]:
+        U0, V0 = inits.gray_scott_2d_square(g["n"], g["n"], seed=case["seed"], frac=0.05)
+        out = o.run({"U": U0, "V": V0}, case["time_step"])
+        assert sha(out["U"], out["V"]) == case["sha256"]
+
+
+@pytest.mark.skipif(not (REF / "examples" / "3d-mhd-rk4.fmr").exists(),
+                    reason="reference tree not present")
+def test_mhd_rk4_matches_hand_oracle():
+    n = 12
+    o = fmr_c.FmrOracle((REF / "examples" / "3d-mhd-rk4.fmr").read_text(), [n, n, n])
+    f0 = inits.mhd_3d(n, seed=3)
+    out = o.run(dict(zip(o.state_names, f0)), 2)
+    for name, r in zip(o.state_names, oracle.mhd_f64(f0, 2)):
+        assert np.array_equal(out[name], r), name
+
+
+# -- code generation -------------------------------------------------------------------------
+
+@pytest.mark.skipif(shutil.which("nvcc") is None and not Path("/usr/local/cuda/bin/nvcc").exists(),
+                    reason="nvcc not available")
+def test_generated_program_compiles(tmp_path):
+    p = load_program(EX / "fmr-features.fmr")
+    assert p.name == "fmr_fmr_features" and [t for _, t in p.states()] == ["double", "float"]
+    hdr = backend.emit_header(p)
+    assert "extern double p[40][24];" in hdr and "extern float q[40][24];" in hdr
+    so = backend.build_program(p, outdir=tmp_path)
+    syms = subprocess.run(["nm", "-D", str(so)], capture_output=True, text=True).stdout
+    for name in ("Formura_Init", "Formura_Forward", "navi", "p", "q"):
+        assert (" %s\n" % name) in syms, name
