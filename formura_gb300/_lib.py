@@ -93,6 +93,11 @@ SIGNATURES = {
                             ctypes.c_float, c_int, c_int, c_void_p]),
     "fm_sur_gelu_bwd": (c_int, [ctypes.c_longlong, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f64_scratch_elems": (c_size_t, [c_int64]),
+    "fm_snapshot_create": (c_int, [ctypes.POINTER(c_void_p), c_int, ctypes.POINTER(c_int), c_int]),
+    "fm_snapshot_plane_elems": (ctypes.c_longlong, [c_void_p, c_int]),
+    "fm_snapshot_begin": (c_int, [c_void_p, c_void_p, c_int, c_int, c_void_p]),
+    "fm_snapshot_wait": (c_int, [c_void_p, c_void_p]),
+    "fm_snapshot_destroy": (None, [c_void_p]),
     "fm_sum_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f32_as_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_tune_set": (c_int, [ctypes.c_char_p, c_int]),

@@ -210,6 +210,13 @@ def emit_header(p: Program) -> str:
     lines.append("int Formura_Set_Stream (void *cuda_stream);")
     lines.append("int Formura_Conserved_Totals (double *totals);")
     lines.append("int Formura_Finalize (void);")
+    lines.append("/* Monitor planes of the device state: Begin gathers plane `index` of axis")
+    lines.append("   `axis` of every state array (asynchronous copy to the host); Wait writes")
+    lines.append("   them, state after state, to `out`.  Write_Monitor writes the mid-planes of")
+    lines.append("   axes 0..d-2 in the format of examples/pearson-3d-main.cpp write_monitor. */")
+    lines.append("int Formura_Monitor_Begin (int axis, int index);")
+    lines.append("int Formura_Monitor_Wait (void *out);")
+    lines.append("int Formura_Write_Monitor (const char *dir, int rank);")
     lines.append("const char *Formura_Last_Error (void);")
     lines += ["", "#ifdef __cplusplus", "}", "#endif", ""]
     return "\n".join(lines)
@@ -331,8 +338,10 @@ def emit_source(p: Program) -> str:
     w('#include "%s.h"' % p.name)
     w('#include "formura_gb300.h"')
     w("#include <math.h>")
+    w("#include <ctype.h>")
     w("#include <stddef.h>")
     w("#include <stdio.h>")
+    w("#include <stdlib.h>")
     if fmr:
         w("#include <cuda_runtime.h>")
         w('#include "fm_softfp.cuh"')
@@ -363,6 +372,10 @@ def emit_source(p: Program) -> str:
     w("static void *g_stream = 0;")
     w("static int g_ready = 0;")
     w("static char g_msg[600];")
+    w("static fm_snapshot *g_snap[%d] = {0};" % len(states))
+    w("static int g_snap_axis = -1;")
+    w("static const int kShape[%d] = {%s};" % (p.dim, ", ".join(str(n) for n in p.shape)))
+    w("static const char *const kAxisNames[%d] = {%s};" % (p.dim, ", ".join('"%s"' % a for a in ax)))
     if fmr:
         for d in decls:
             w(d)
@@ -474,6 +487,8 @@ def emit_source(p: Program) -> str:
     w("  fm_stream_sync(g_stream);")
     w("  for (int i = 0; i < kNState; ++i) { fm_free(g_dev[i]); g_dev[i] = 0; fm_host_unregister(kHost[i]); }")
     w("  fm_free(g_work); g_work = 0; fm_free(g_totals); g_totals = 0;")
+    w("  for (int i = 0; i < kNState; ++i) { fm_snapshot_destroy(g_snap[i]); g_snap[i] = 0; }")
+    w("  g_snap_axis = -1;")
     if fmr:
         for line in free:
             w(line)
@@ -482,6 +497,54 @@ def emit_source(p: Program) -> str:
     w("}")
     w("")
     w("FMR_EXPORT const char *Formura_Last_Error (void) { return g_msg; }")
+    w("")
+    w("FMR_EXPORT int Formura_Monitor_Begin (int axis, int index) {")
+    w("  int st = ensure_device(); if (st) return st;")
+    w("  for (int i = 0; i < kNState; ++i) {")
+    w("    if (!g_snap[i] && (st = fm_snapshot_create(&g_snap[i], %d, kShape, (int)(kBytes[i] / NCELLS))))" % p.dim)
+    w('      return fail(st, "Formura_Monitor_Begin");')
+    w("    if ((st = fm_snapshot_begin(g_snap[i], g_dev[i], axis, index, g_stream))) return fail(st, \"Formura_Monitor_Begin\");")
+    w("  }")
+    w("  g_snap_axis = axis;")
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Monitor_Wait (void *out) {")
+    w("  if (g_snap_axis < 0) return fail(FM_ERR_ARG, \"Formura_Monitor_Wait: no plane in flight\");")
+    w("  char *o = (char*)out;")
+    w("  int st;")
+    w("  for (int i = 0; i < kNState; ++i) {")
+    w("    if ((st = fm_snapshot_wait(g_snap[i], o))) return fail(st, \"Formura_Monitor_Wait\");")
+    w("    o += (size_t)fm_snapshot_plane_elems(g_snap[i], g_snap_axis) * (kBytes[i] / NCELLS);")
+    w("  }")
+    w("  g_snap_axis = -1;")
+    w("  return 0;")
+    w("}")
+    w("")
+    w("FMR_EXPORT int Formura_Write_Monitor (const char *dir, int rank) {")
+    w("  int st = ensure_device(); if (st) return st;")
+    w("  int pos[%d];" % (2 * p.dim))
+    w("  for (int a = 0; a < %d; ++a) { pos[a] = 0; pos[%d + a] = kShape[a]; }" % (p.dim, p.dim))
+    w("  for (int a = 0; a + 1 < %d || (%d == 1 && a == 0); ++a) {" % (p.dim, p.dim))
+    w("    size_t bytes = 0;")
+    w("    for (int i = 0; i < kNState; ++i) bytes += (size_t)(NCELLS / kShape[a]) * (kBytes[i] / NCELLS);")
+    w("    void *buf = malloc(bytes);")
+    w('    if (!buf) return fail(FM_ERR_NOMEM, "Formura_Write_Monitor");')
+    w("    if ((st = Formura_Monitor_Begin(a, kShape[a] / 2)) || (st = Formura_Monitor_Wait(buf))) { free(buf); return st; }")
+    w("    char fn[1024], up[64];")
+    w("    size_t k = 0;")
+    w("    for (; kAxisNames[a][k] && k + 1 < sizeof up; ++k) up[k] = (char)toupper((unsigned char)kAxisNames[a][k]);")
+    w("    up[k] = 0;")
+    w('    snprintf(fn, sizeof fn, "%s/monitor%s-%06d-%d.txt", dir, up, navi.time_step, rank);')
+    w('    FILE *fp = fopen(fn, "wb");')
+    w('    if (!fp) { free(buf); snprintf(g_msg, sizeof g_msg, "cannot open %s", fn); return FM_ERR_ARG; }')
+    w("    fwrite(pos, sizeof(int), %d, fp);" % (2 * p.dim))
+    w("    fwrite(buf, 1, bytes, fp);")
+    w("    fclose(fp);")
+    w("    free(buf);")
+    w("  }")
+    w("  return 0;")
+    w("}")
     w("")
     w("}  /* extern \"C\" */")
     w("")

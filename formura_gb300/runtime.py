@@ -59,6 +59,10 @@ class FormuraProgram:
         L.Formura_Set_Stream.argtypes = [ctypes.c_void_p]
         L.Formura_Conserved_Totals.argtypes = [ctypes.POINTER(ctypes.c_double)]
         L.Formura_Last_Error.restype = ctypes.c_char_p
+        L.Formura_Monitor_Begin.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.Formura_Monitor_Wait.argtypes = [ctypes.c_void_p]
+        L.Formura_Write_Monitor.argtypes = [ctypes.c_char_p, ctypes.c_int]
+        self._monitor_axis = None
         n = int(np.prod(program.shape))
         self.state: Dict[str, np.ndarray] = {}
         self.state_names = [s for s, _ in program.states()]
@@ -106,6 +110,35 @@ class FormuraProgram:
         out = (ctypes.c_double * k)()
         self._check(self.lib.Formura_Conserved_Totals(out), "Formura_Conserved_Totals")
         return np.array(out[:], dtype=np.float64)
+
+    def monitor_begin(self, axis: int, index: int):
+        """Start copying plane `index` of axis `axis` of every state array from
+        the device (asynchronous: the stepping may continue meanwhile)."""
+        self._check(self.lib.Formura_Monitor_Begin(int(axis), int(index)), "Formura_Monitor_Begin")
+        self._monitor_axis = int(axis)
+
+    def monitor_wait(self) -> Dict[str, np.ndarray]:
+        """The planes started by :meth:`monitor_begin`, per state array."""
+        if self._monitor_axis is None:
+            raise FormuraError(1, "monitor_wait", "no plane in flight")
+        a = self._monitor_axis
+        pshape = [n for k, n in enumerate(self.program.shape) if k != a] or [1]
+        dtypes = [self.state[n].dtype for n in self.state_names]
+        sizes = [int(np.prod(pshape)) * d.itemsize for d in dtypes]
+        buf = np.empty(sum(sizes), dtype=np.uint8)
+        self._check(self.lib.Formura_Monitor_Wait(buf.ctypes.data), "Formura_Monitor_Wait")
+        self._monitor_axis = None
+        out, off = {}, 0
+        for n, d, nb in zip(self.state_names, dtypes, sizes):
+            out[n] = buf[off:off + nb].view(d).reshape(pshape).copy()
+            off += nb
+        return out
+
+    def write_monitor(self, directory, rank: int = 0):
+        """Monitor files of the device state, as the reference drivers write
+        them from the host globals (examples/pearson-3d-main.cpp:116-157)."""
+        self._check(self.lib.Formura_Write_Monitor(str(directory).encode(), int(rank)),
+                    "Formura_Write_Monitor")
 
     def finalize(self):
         self._check(self.lib.Formura_Finalize(), "Formura_Finalize")

@@ -332,6 +332,27 @@ int fm_sum_f64(int64_t n, const double *a, double *partials, double *out_device,
 int fm_sum_f32_as_f64(int64_t n, const float *a, double *partials,
                       double *out_device, void *stream);
 
+/* ---- plane snapshots (monitor output) --------------------------------------- */
+
+/*
+ * No counterpart in the reference: its drivers read mid-planes of the host
+ * globals for their monitor files (examples/pearson-3d-main.cpp:116-157).
+ * With the state resident on the GPU, fm_snapshot_begin gathers the plane
+ * (axis, index) of a row-major device array with `shape` into device staging
+ * on `stream` (ordered before every later kernel on that stream, so the array
+ * may be overwritten right after) and copies it to pinned host staging on an
+ * internal stream; fm_snapshot_wait blocks until that copy is done and
+ * writes the plane (row-major over the remaining axes) to host_out, which
+ * must hold fm_snapshot_plane_elems(s, axis) elements.  One snapshot may be
+ * in flight per object.  elem_size: 1, 2, 4 or 8 bytes; 1 <= ndim <= 8.
+ */
+typedef struct fm_snapshot fm_snapshot;
+int fm_snapshot_create(fm_snapshot **out, int ndim, const int *shape, int elem_size);
+long long fm_snapshot_plane_elems(const fm_snapshot *s, int axis);
+int fm_snapshot_begin(fm_snapshot *s, const void *array, int axis, int index, void *stream);
+int fm_snapshot_wait(fm_snapshot *s, void *host_out);
+void fm_snapshot_destroy(fm_snapshot *s);
+
 /* ---- tuning ------------------------------------------------------------------ */
 
 /*
