@@ -594,6 +594,22 @@ def run_profile_case(args):
         d0 = inits.diffusion_2d(n, n, seed=1)
         d = torch.from_numpy(d0).to(dev)
         kernels.diff2d_f64_forward(d, torch.empty_like(d), 0.4, args.profile_steps)
+    elif args.profile == "fmr_gs3d":
+        # examples/gray-scott-3d.fmr through the front end: `profile_steps` steps at n^3
+        from formura_gb300.fmr import load_program
+        from formura_gb300.runtime import load_program as load_lib
+
+        p = load_program(ROOT / "examples" / "gray-scott-3d.fmr", intra_node_shape=[n, n, n],
+                         monitor_interval=args.profile_steps)
+        prog = load_lib(p)
+        prog.init()
+        U0, V0 = inits.gray_scott_3d(n, n, n, seed=1)
+        prog.state["U"][...] = U0
+        prog.state["V"][...] = V0
+        prog.upload()
+        prog.advance(1)
+        prog.download()
+        prog.finalize()
     elif args.profile == "surrogate":
         # `profile_steps` network jumps (and one training step) on `profile_batch` instances of n x n
         from formura_gb300.surrogate import Surrogate
@@ -626,7 +642,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
     ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",
-                                          "mhd", "diff2d", "surrogate"], default=None,
+                                          "mhd", "diff2d", "surrogate", "fmr_gs3d"],
+                    default=None,
                     help="run a small case of one kernel for an ncu capture, then exit")
     ap.add_argument("--profile-n", type=int, default=256)
     ap.add_argument("--profile-steps", type=int, default=4)
