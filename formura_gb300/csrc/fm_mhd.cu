@@ -23,6 +23,7 @@
 #include <algorithm>
 
 #include "fm_common.cuh"
+#include "fm_tune.h"
 
 namespace {
 
@@ -164,6 +165,132 @@ __global__ void __launch_bounds__(128)
     reinterpret_cast<R *>(O.p[q])[c] = ld<R>(S.p[q], c) + (k.dt_c * f[q]);
 }
 
+// mhd_stage_tile: the same stage, with the composite quantities of the y and z
+// derivatives computed ONCE per point.  A CTA owns a 32 (z) x 8 (y) tile of
+// one x plane; it first evaluates, for every point of the tile and a 2-point
+// periodic halo in y and z (36 x 12 points), the 20 values the y and z
+// derivatives read (d*v_a, v_a, P, B_a*B_c, E_ca, s, B_a for a = y, z) into
+// shared memory ([value][point], conflict-free along z); the y and z
+// derivatives then read their four neighbours there.  The x derivatives
+// evaluate the composites at x-2 .. x+2 as mhd_stage does.  Every value is
+// the same IEEE expression as in axis_q, so results are bit-identical with
+// mhd_stage (and, for R = double, with the all-FP64 program).
+constexpr int kTZ = 32, kTY = 8, kH = 2, kRZ = kTZ + 2 * kH, kRY = kTY + 2 * kH;
+constexpr int kNP = kRZ * kRY;  // 432 points
+constexpr int kNV = 20;
+
+template <typename R>
+__global__ void __launch_bounds__(256)
+    mhd_stage_tile(Fields Q, Fields S, Fields O, int n, MhdC<R> k) {
+  extern __shared__ __align__(16) unsigned char mhd_smem[];
+  R *sv = reinterpret_cast<R *>(mhd_smem);  // [kNV][kNP]
+  const int tz = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int z0 = blockIdx.x * kTZ, y0 = blockIdx.y * kTY, x = blockIdx.z;
+  const size_t sx = (size_t)n * n, sy = (size_t)n;
+  for (int pt = threadIdx.x; pt < kNP; pt += 256) {
+    const int ry = pt / kRZ, rz = pt - ry * kRZ;
+    int gy = (y0 - kH + ry) % n;
+    gy = gy < 0 ? gy + n : gy;
+    int gz = (z0 - kH + rz) % n;
+    gz = gz < 0 ? gz + n : gz;
+    const size_t i = (size_t)x * sx + (size_t)gy * sy + gz;
+    const R dn = ld<R>(Q.p[0], i);
+    const R v[3] = {ld<R>(Q.p[1], i), ld<R>(Q.p[2], i), ld<R>(Q.p[3], i)};
+    const R B[3] = {ld<R>(Q.p[4], i), ld<R>(Q.p[5], i), ld<R>(Q.p[6], i)};
+    const R s = ld<R>(Q.p[7], i), Psi = ld<R>(Q.p[8], i);
+    const R d = k.dens0 + dn;
+    const R b2 = ((B[0] * B[0]) + (B[1] * B[1])) + (B[2] * B[2]);
+    sv[0 * kNP + pt] = d * v[1];
+    sv[1 * kNP + pt] = d * v[2];
+    sv[2 * kNP + pt] = v[1];
+    sv[3 * kNP + pt] = v[2];
+    sv[4 * kNP + pt] = ((k.dp_ddens * d) + (k.dp_ds * s)) + (k.c8 * b2);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      sv[(5 + c) * kNP + pt] = B[1] * B[c];
+      sv[(8 + c) * kNP + pt] = B[2] * B[c];
+      const R zy = R(0) * (c == 1 ? R(1) : R(0));
+      const R zz = R(0) * (c == 2 ? R(1) : R(0));
+      sv[(11 + c) * kNP + pt] = ((-(zy * Psi)) + (v[c] * B[1])) - (v[1] * B[c]);
+      sv[(14 + c) * kNP + pt] = ((-(zz * Psi)) + (v[c] * B[2])) - (v[2] * B[c]);
+    }
+    sv[17 * kNP + pt] = s;
+    sv[18 * kNP + pt] = B[1];
+    sv[19 * kNP + pt] = B[2];
+  }
+  __syncthreads();
+  const int y = y0 + ty, z = z0 + tz;
+  if (y >= n || z >= n) return;
+  const size_t c = (size_t)x * sx + (size_t)y * sy + z;
+  const int p0 = (ty + kH) * kRZ + (tz + kH);
+  auto dy = [&](int v) {
+    const R *b = sv + v * kNP + p0;
+    return d4<R>(b[-2 * kRZ], b[-kRZ], b[kRZ], b[2 * kRZ], k);
+  };
+  auto dz = [&](int v) {
+    const R *b = sv + v * kNP + p0;
+    return d4<R>(b[-2], b[-1], b[1], b[2], k);
+  };
+  R dm[3], dv[3], dP[3], dBB[3][3], dE[3][3], ds[3], dB[3];
+  {
+    const int im2 = x - 2 < 0 ? x - 2 + n : x - 2;
+    const int im1 = x - 1 < 0 ? x - 1 + n : x - 1;
+    const int ip1 = x + 1 >= n ? x + 1 - n : x + 1;
+    const int ip2 = x + 2 >= n ? x + 2 - n : x + 2;
+    const size_t base = c - (size_t)x * sx;
+    const AxisQ<R> qm2 = axis_q<R>(Q, base + (size_t)im2 * sx, 0, k);
+    const AxisQ<R> qm1 = axis_q<R>(Q, base + (size_t)im1 * sx, 0, k);
+    const AxisQ<R> qp1 = axis_q<R>(Q, base + (size_t)ip1 * sx, 0, k);
+    const AxisQ<R> qp2 = axis_q<R>(Q, base + (size_t)ip2 * sx, 0, k);
+    dm[0] = d4<R>(qm2.m, qm1.m, qp1.m, qp2.m, k);
+    dv[0] = d4<R>(qm2.v, qm1.v, qp1.v, qp2.v, k);
+    dP[0] = d4<R>(qm2.P, qm1.P, qp1.P, qp2.P, k);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dBB[0][i] = d4<R>(qm2.BB[i], qm1.BB[i], qp1.BB[i], qp2.BB[i], k);
+      dE[i][0] = d4<R>(qm2.E[i], qm1.E[i], qp1.E[i], qp2.E[i], k);
+    }
+    ds[0] = d4<R>(qm2.s, qm1.s, qp1.s, qp2.s, k);
+    dB[0] = d4<R>(qm2.B, qm1.B, qp1.B, qp2.B, k);
+  }
+  dm[1] = dy(0);
+  dm[2] = dz(1);
+  dv[1] = dy(2);
+  dv[2] = dz(3);
+  dP[1] = dy(4);
+  dP[2] = dz(4);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    dBB[1][i] = dy(5 + i);
+    dBB[2][i] = dz(8 + i);
+    dE[i][1] = dy(11 + i);
+    dE[i][2] = dz(14 + i);
+  }
+  ds[1] = dy(17);
+  ds[2] = dz(17);
+  dB[1] = dy(18);
+  dB[2] = dz(19);
+  const R dn = ld<R>(Q.p[0], c);
+  const R v[3] = {ld<R>(Q.p[1], c), sv[2 * kNP + p0], sv[3 * kNP + p0]};
+  const R Psi = ld<R>(Q.p[8], c);
+  const R dens = k.dens0 + dn;
+  R f[NF];
+  f[0] = -(((dm[0]) + (dm[1])) + (dm[2]));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const R A = ((v[0] * dv[i]) + (v[1] * dv[i])) + (v[2] * dv[i]);
+    const R Y = ((dBB[0][i]) + (dBB[1][i])) + (dBB[2][i]);
+    f[1 + i] = ((-A) - vdiv(dP[i], dens)) + vdiv(k.c4 * Y, dens);
+    f[4 + i] = ((dE[i][0]) + (dE[i][1])) + (dE[i][2]);
+  }
+  f[7] = ((v[0] * ds[0]) + (v[1] * ds[1])) + (v[2] * ds[2]);
+  const R divB = ((dB[0]) + (dB[1])) + (dB[2]);
+  f[8] = (-(k.c_h2 * divB)) - (k.ch2_cp2 * Psi);
+#pragma unroll
+  for (int q = 0; q < NF; ++q)
+    reinterpret_cast<R *>(O.p[q])[c] = ld<R>(S.p[q], c) + (k.dt_c * f[q]);
+}
+
 // `<%` of three: fmin(0, fmax(a, fmax(b, c))) + fmax(0, fmin(a, fmin(b, c)))
 template <typename R>
 __device__ __forceinline__ R minmod3(R a, R b, R c) {
@@ -249,6 +376,127 @@ __global__ void __launch_bounds__(128)
   reinterpret_cast<R *>(S.p[7])[c] = (R)((double)nv[7] + heat);
 }
 
+// mhd_finish_march: the same finishing step with every face flux computed
+// once.  The flux at a face is the same function of the same four values for
+// the cell on either side (face(u[i-1], u[i], u[i+1], u[i+2]) is cell i's
+// "+1/2" and cell i+1's "-1/2" flux), so it can be shared exactly:
+//   x: each thread marches along x over a chunk of planes and carries the
+//      flux at x+1/2 into the next plane as its x-1/2 flux (5-value window);
+//   y, z: per plane the CTA stages the field over its 32 (z) x 8 (y) tile plus
+//      a 2-point periodic halo into shared memory and computes the fluxes of
+//      the tile's faces (9 x 32 in y, 8 x 33 in z) once into shared memory.
+// Fields are processed one at a time in the order 1..6, 8, 7, 0: the
+// numerical heat (with s, field 7) reads the new velocities and fields of
+// 1..6 back from S, and the step's input density from S before field 0 is
+// overwritten.  Per cell: w = N_f; w = (w + f_{x-1/2}) - f_{x+1/2}; then y,
+// then z — the order of mhd_finish, so results are bit-identical with it.
+template <typename R>
+__global__ void __launch_bounds__(256)
+    mhd_finish_march(Fields N, Fields S, int n, int xchunk, int ntiles_yz, int ntiles,
+                     MhdC<R> k) {
+  __shared__ R su[kRY][kRZ];
+  __shared__ R sfy[kTY + 1][kTZ];
+  __shared__ R sfz[kTY][kTZ + 1];
+  const int tz = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const size_t sx = (size_t)n * n, sy = (size_t)n;
+  const int ntz = (n + kTZ - 1) / kTZ;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tyz = t % ntiles_yz;
+    const int z0 = (tyz % ntz) * kTZ, y0 = (tyz / ntz) * kTY;
+    const int x0 = (t / ntiles_yz) * xchunk;
+    const int x1 = min(x0 + xchunk, n);
+    const int y = y0 + ty, z = z0 + tz;
+    const bool own = y < n && z < n;
+    const size_t yz = own ? (size_t)y * sy + z : 0;
+    for (int oi = 0; oi < NF; ++oi) {
+      const int f = oi < 6 ? oi + 1 : (oi == 6 ? 8 : (oi == 7 ? 7 : 0));  // 1..6, 8, 7, 0
+      const R *uf = reinterpret_cast<const R *>(N.p[f]);
+      R win[5];
+      R fxm = R(0);
+      if (own) {
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+          int q = (x0 - 2 + d) % n;
+          q = q < 0 ? q + n : q;
+          win[d + 1] = __ldg(uf + (size_t)q * sx + yz);
+        }
+        fxm = face<R>(win[1], win[2], win[3], win[4]);  // flux at x0 - 1/2
+      }
+      for (int x = x0; x < x1; ++x) {
+        // stage plane x of field f (tile + 2-point halo in y and z)
+        for (int pt = threadIdx.x; pt < kNP; pt += 256) {
+          const int ry = pt / kRZ, rz = pt - ry * kRZ;
+          int gy = (y0 - kH + ry) % n;
+          gy = gy < 0 ? gy + n : gy;
+          int gz = (z0 - kH + rz) % n;
+          gz = gz < 0 ? gz + n : gz;
+          su[ry][rz] = __ldg(uf + (size_t)x * sx + (size_t)gy * sy + gz);
+        }
+        __syncthreads();
+        // y faces of rows y0-1 .. y0+kTY-1 (the face above each row), z faces
+        for (int q = threadIdx.x; q < (kTY + 1) * kTZ + kTY * (kTZ + 1); q += 256) {
+          if (q < (kTY + 1) * kTZ) {
+            const int r = q / kTZ, c = q - r * kTZ;  // face between rows r-1 and r (tile rows)
+            const int cz = c + kH;
+            sfy[r][c] = face<R>(su[r][cz], su[r + 1][cz], su[r + 2][cz], su[r + 3][cz]);
+          } else {
+            const int q2 = q - (kTY + 1) * kTZ;
+            const int r = q2 / (kTZ + 1), c = q2 - r * (kTZ + 1);
+            const int ry = r + kH;
+            sfz[r][c] = face<R>(su[ry][c], su[ry][c + 1], su[ry][c + 2], su[ry][c + 3]);
+          }
+        }
+        __syncthreads();
+        if (own) {
+          // x window: win[0..4] = u[x-2 .. x+2]
+          int q = (x + 2) % n;
+          win[0] = win[1];
+          win[1] = win[2];
+          win[2] = win[3];
+          win[3] = win[4];
+          win[4] = __ldg(uf + (size_t)q * sx + yz);
+          const R fxp = face<R>(win[1], win[2], win[3], win[4]);
+          const size_t c = (size_t)x * sx + yz;
+          R w = su[ty + kH][tz + kH];
+          w = (w + fxm) - fxp;
+          w = (w + sfy[ty][tz]) - sfy[ty + 1][tz];
+          w = (w + sfz[ty][tz]) - sfz[ty][tz + 1];
+          fxm = fxp;
+          R *out = reinterpret_cast<R *>(S.p[f]);
+          if (f == 0) {
+            out[c] = vmax(w, R(-0.9));
+          } else if (f == 7) {
+            // numerical_heat (3d-mhd-rk4.fmr:141-143), always in FP64; the new
+            // velocities and fields were written to S by fields 1..6; dens = the
+            // step's input density perturbation, still in S (field 0 comes last)
+            const double r1 = ld<R>(N.p[1], c), r2 = ld<R>(N.p[2], c), r3 = ld<R>(N.p[3], c);
+            const double b1 = ld<R>(N.p[4], c), b2 = ld<R>(N.p[5], c), b3 = ld<R>(N.p[6], c);
+            const R *Sp1 = reinterpret_cast<const R *>(S.p[1]);
+            const R *Sp2 = reinterpret_cast<const R *>(S.p[2]);
+            const R *Sp3 = reinterpret_cast<const R *>(S.p[3]);
+            const R *Sp4 = reinterpret_cast<const R *>(S.p[4]);
+            const R *Sp5 = reinterpret_cast<const R *>(S.p[5]);
+            const R *Sp6 = reinterpret_cast<const R *>(S.p[6]);
+            const double n1 = Sp1[c], n2 = Sp2[c], n3 = Sp3[c];
+            const double m1 = Sp4[c], m2 = Sp5[c], m3 = Sp6[c];
+            const double svr = ((r1 * r1) + (r2 * r2)) + (r3 * r3);
+            const double svn = ((n1 * n1) + (n2 * n2)) + (n3 * n3);
+            const double sbr = ((b1 * b1) + (b2 * b2)) + (b3 * b3);
+            const double sbn = ((m1 * m1) + (m2 * m2)) + (m3 * m3);
+            const double dens_in = reinterpret_cast<const R *>(S.p[0])[c];
+            const double den8 = (8.0 * 3.141592653589793) * (1.0 + dens_in);
+            const double heat = (0.5 * (svr - svn)) + (__ddiv_rn(1.0, den8) * (sbr - sbn));
+            out[c] = (R)((double)w + heat);
+          } else {
+            out[c] = w;
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
 // Conserved totals in FP64: mass perturbation, kinetic + magnetic energy,
 // s, and the x-momentum; fixed tree as in fm_reduce.cu.
 template <typename R>
@@ -331,12 +579,43 @@ int mhd_forward(int n, R *const *fields, R *work, int steps, cudaStream_t s) {
   const MhdC<R> k4 = make_consts<R>(n, dt / 4.0), k3 = make_consts<R>(n, dt / 3.0),
                 k2 = make_consts<R>(n, dt / 2.0), k1 = make_consts<R>(n, dt);
   const dim3 grid((n + 31) / 32, (n + 3) / 4, n);
+  const int stage_kernel = fm::tune_get("mhd.stage", 1);  // 1 tiled (default), 0 per-point
+  const dim3 tgrid((n + kTZ - 1) / kTZ, (n + kTY - 1) / kTY, n);
+  const size_t tsmem = (size_t)kNV * kNP * sizeof(R);
+  if (stage_kernel == 1)
+    FM_TRY_CUDA(cudaFuncSetAttribute(mhd_stage_tile<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tsmem));
+  auto stage = [&](const Fields &in, Fields &out, const MhdC<R> &kk) {
+    if (stage_kernel == 1)
+      mhd_stage_tile<R><<<tgrid, 256, tsmem, s>>>(in, S, out, n, kk);
+    else
+      mhd_stage<R><<<grid, 128, 0, s>>>(in, S, out, n, kk);
+  };
+  // 1 x-march, 0 per-point; default: x-march for double (0.155 vs 0.129 GLUP/s at 256^3),
+  // per-point for float (3.13 vs 2.75: the staging costs more than the shared faces save)
+  const int finish_kernel = fm::tune_get("mhd.finish", sizeof(R) == 8 ? 1 : 0);
+  int sms = 0;
+  int st = fm::device_sm_count(&sms);
+  if (st) return st;
+  const int ntiles_yz = ((n + kTZ - 1) / kTZ) * ((n + kTY - 1) / kTY);
+  int xchunk = fm::tune_get("mhd.xchunk", 0);
+  if (xchunk <= 0) {  // enough tiles for ~4 CTAs per SM, chunks of at most 32 planes
+    xchunk = 32;
+    while (xchunk > 4 && (long long)ntiles_yz * ((n + xchunk - 1) / xchunk) < 4ll * sms)
+      xchunk /= 2;
+  }
+  xchunk = std::min(xchunk, n);
+  const int ntiles = ntiles_yz * ((n + xchunk - 1) / xchunk);
+  const int fgrid = std::min(ntiles, 8 * sms);
   for (int i = 0; i < steps; ++i) {
-    mhd_stage<R><<<grid, 128, 0, s>>>(S, S, A, n, k4);
-    mhd_stage<R><<<grid, 128, 0, s>>>(A, S, B, n, k3);
-    mhd_stage<R><<<grid, 128, 0, s>>>(B, S, A, n, k2);
-    mhd_stage<R><<<grid, 128, 0, s>>>(A, S, B, n, k1);
-    mhd_finish<R><<<grid, 128, 0, s>>>(B, S, n, k1);
+    stage(S, A, k4);
+    stage(A, B, k3);
+    stage(B, A, k2);
+    stage(A, B, k1);
+    if (finish_kernel == 1)
+      mhd_finish_march<R><<<fgrid, 256, 0, s>>>(B, S, n, xchunk, ntiles_yz, ntiles, k1);
+    else
+      mhd_finish<R><<<grid, 128, 0, s>>>(B, S, n, k1);
   }
   FM_TRY_CUDA(cudaGetLastError());
   return FM_OK;

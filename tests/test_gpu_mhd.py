@@ -77,3 +77,32 @@ def test_mhd_totals_conserve_mass(cuda_device):
     # kinetic + magnetic energy exchanges with pressure and is dissipated by the
     # artificial viscosity and the Psi damping: finite and not growing
     assert np.isfinite(tot1).all() and tot1[1] < 1.001 * tot0[1]
+
+
+@pytest.mark.parametrize("n", [12, 40])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_mhd_kernel_variants_agree(cuda_device, n, dtype):
+    """The shared-memory stage kernel (mhd.stage = 1, default) and the
+    per-point one (0), the x-marching finish kernel with shared face fluxes
+    (mhd.finish = 1, default; several x chunks) and the per-point one (0)
+    evaluate the same expressions: identical bits, also for sizes that are not
+    multiples of the 32 x 8 tile."""
+    from formura_gb300 import _lib
+
+    f0 = inits.mhd_3d(n, seed=11, amp=0.05)
+    outs = []
+    L = _lib.lib()
+    try:
+        for kern, fin, xc in ((0, 0, 0), (1, 1, 0), (1, 1, 5), (0, 1, 1)):
+            L.fm_tune_clear()
+            L.fm_tune_set(b"mhd.stage", kern)
+            L.fm_tune_set(b"mhd.finish", fin)
+            L.fm_tune_set(b"mhd.xchunk", xc)
+            t = [torch.from_numpy(x).to(dtype).to(cuda_device) for x in f0]
+            kernels.mhd_forward(t, torch.empty(18 * n ** 3, dtype=dtype, device=cuda_device), 3)
+            outs.append([x.cpu().numpy() for x in t])
+    finally:
+        L.fm_tune_clear()
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
