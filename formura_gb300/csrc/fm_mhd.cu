@@ -497,6 +497,173 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The flux at the face between ua and ub from the slopes at both cells: the
+// expression of face() with slope(um, ua, ub) = sla and slope(ua, ub, u2) = slb.
+template <typename R>
+__device__ __forceinline__ R face_from_slopes(R ua, R ub, R sla, R slb) {
+  const R ul = ua + (R(0.5) * sla);
+  const R ur = ub - (R(0.5) * slb);
+  return av_flux<R>(ur - ul, ub - ua);
+}
+
+// mhd_finish_v2: the finishing step with every slope computed once per cell
+// and axis (a slope is shared by the two faces of its cell) and every face
+// flux once per face (shared by the two cells of the face), all 9 fields per
+// plane.  CTA = a 32 (z) x 8 (y) tile marching along x over a chunk of
+// planes.  Per plane: the 9 fields over the tile and a 2-point periodic halo
+// are staged into shared memory; y slopes (10 rows) and z slopes (34 columns)
+// go to shared memory, then the 9 y faces and 33 z faces of the tile; x
+// slopes and faces are carried in registers along the march.  Same
+// expressions and the same accumulation order as mhd_finish: bit-identical.
+constexpr int kFY = kTY + 1, kFZ = kTZ + 1;      // faces per column / row
+constexpr int kSY = kTY + 2, kSZ = kTZ + 2;      // slopes per column / row
+template <typename R>
+struct FinishSmem {
+  R u[NF][kRY][kRZ];
+  R sly[NF][kSY][kTZ];
+  R slz[NF][kTY][kSZ];
+  R fy[NF][kFY][kTZ];
+  R fz[NF][kTY][kFZ];
+};
+
+template <typename R>
+__global__ void __launch_bounds__(256, 2)
+    mhd_finish_v2(Fields N, Fields S, int n, int xchunk, int ntiles_yz, int ntiles, MhdC<R> k) {
+  extern __shared__ __align__(16) unsigned char fin_smem[];
+  FinishSmem<R> &sm = *reinterpret_cast<FinishSmem<R> *>(fin_smem);
+  const int tz = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const size_t sx = (size_t)n * n, sy = (size_t)n;
+  const int ntz = (n + kTZ - 1) / kTZ;
+  const R *uf[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) uf[f] = reinterpret_cast<const R *>(N.p[f]);
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tyz = t % ntiles_yz;
+    const int z0 = (tyz % ntz) * kTZ, y0 = (tyz / ntz) * kTY;
+    const int x0 = (t / ntiles_yz) * xchunk;
+    const int x1 = min(x0 + xchunk, n);
+    const int y = y0 + ty, z = z0 + tz;
+    const bool own = y < n && z < n;
+    const size_t yz = own ? (size_t)y * sy + z : 0;
+    // in-plane offsets of the (up to two) region points this thread stages
+    size_t soff[2];
+    int spt[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int pt = threadIdx.x + 256 * j;
+      spt[j] = pt < kNP ? pt : -1;
+      const int ptc = pt < kNP ? pt : 0;
+      const int ry = ptc / kRZ, rz = ptc - ry * kRZ;
+      int gy = (y0 - kH + ry) % n;
+      gy = gy < 0 ? gy + n : gy;
+      int gz = (z0 - kH + rz) % n;
+      gz = gz < 0 ? gz + n : gz;
+      soff[j] = (size_t)gy * sy + gz;
+    }
+    // x carry per field: u[x], u[x+1], slope at x, flux at x-1/2
+    R cu1[NF], cu2[NF], csl[NF], cfm[NF];
+    if (own) {
+      int q[4];
+#pragma unroll
+      for (int d = 0; d < 4; ++d) {
+        q[d] = (x0 - 2 + d) % n;
+        q[d] = q[d] < 0 ? q[d] + n : q[d];
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        const R a = __ldg(uf[f] + (size_t)q[0] * sx + yz), b = __ldg(uf[f] + (size_t)q[1] * sx + yz);
+        const R c = __ldg(uf[f] + (size_t)q[2] * sx + yz), d = __ldg(uf[f] + (size_t)q[3] * sx + yz);
+        const R slm = slope<R>(a, b, c);  // at x0-1
+        const R sl0 = slope<R>(b, c, d);  // at x0
+        cfm[f] = face_from_slopes<R>(b, c, slm, sl0);
+        cu1[f] = c;
+        cu2[f] = d;
+        csl[f] = sl0;
+      }
+    }
+    for (int x = x0; x < x1; ++x) {
+      const size_t px = (size_t)x * sx;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        if (spt[j] >= 0) {
+          const int ry = spt[j] / kRZ, rz = spt[j] - ry * kRZ;
+#pragma unroll
+          for (int f = 0; f < NF; ++f) sm.u[f][ry][rz] = __ldg(uf[f] + px + soff[j]);
+        }
+      }
+      __syncthreads();
+      // slopes: y at region rows 1..10 over the tile columns; z at region
+      // columns 1..34 over the tile rows
+      for (int q = threadIdx.x; q < NF * kSY * kTZ; q += 256) {
+        const int f = q / (kSY * kTZ), rem = q - f * (kSY * kTZ);
+        const int r = rem / kTZ, c = rem - r * kTZ;
+        const int ry = r + 1, rz = c + kH;
+        sm.sly[f][r][c] = slope<R>(sm.u[f][ry - 1][rz], sm.u[f][ry][rz], sm.u[f][ry + 1][rz]);
+      }
+      for (int q = threadIdx.x; q < NF * kTY * kSZ; q += 256) {
+        const int f = q / (kTY * kSZ), rem = q - f * (kTY * kSZ);
+        const int r = rem / kSZ, c = rem - r * kSZ;
+        const int ry = r + kH, rz = c + 1;
+        sm.slz[f][r][c] = slope<R>(sm.u[f][ry][rz - 1], sm.u[f][ry][rz], sm.u[f][ry][rz + 1]);
+      }
+      __syncthreads();
+      // faces: y face i lies between region rows i+1 and i+2 (slope rows i, i+1);
+      // z face j between region columns j+1 and j+2 (slope columns j, j+1)
+      for (int q = threadIdx.x; q < NF * kFY * kTZ; q += 256) {
+        const int f = q / (kFY * kTZ), rem = q - f * (kFY * kTZ);
+        const int i = rem / kTZ, c = rem - i * kTZ;
+        sm.fy[f][i][c] = face_from_slopes<R>(sm.u[f][i + 1][c + kH], sm.u[f][i + 2][c + kH],
+                                             sm.sly[f][i][c], sm.sly[f][i + 1][c]);
+      }
+      for (int q = threadIdx.x; q < NF * kTY * kFZ; q += 256) {
+        const int f = q / (kTY * kFZ), rem = q - f * (kTY * kFZ);
+        const int r = rem / kFZ, j = rem - r * kFZ;
+        sm.fz[f][r][j] = face_from_slopes<R>(sm.u[f][r + kH][j + 1], sm.u[f][r + kH][j + 2],
+                                             sm.slz[f][r][j], sm.slz[f][r][j + 1]);
+      }
+      __syncthreads();
+      if (own) {
+        const int q2 = (x + 2) % n;
+        const size_t c = px + yz;
+        R nv[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const R u2 = __ldg(uf[f] + (size_t)q2 * sx + yz);
+          const R sl1 = slope<R>(cu1[f], cu2[f], u2);  // at x+1
+          const R fxp = face_from_slopes<R>(cu1[f], cu2[f], csl[f], sl1);
+          R w = sm.u[f][ty + kH][tz + kH];
+          w = (w + cfm[f]) - fxp;
+          w = (w + sm.fy[f][ty][tz]) - sm.fy[f][ty + 1][tz];
+          w = (w + sm.fz[f][ty][tz]) - sm.fz[f][ty][tz + 1];
+          nv[f] = w;
+          cfm[f] = fxp;
+          cu1[f] = cu2[f];
+          cu2[f] = u2;
+          csl[f] = sl1;
+        }
+        // numerical_heat (3d-mhd-rk4.fmr:141-143), always in FP64
+        const double r1 = sm.u[1][ty + kH][tz + kH], r2 = sm.u[2][ty + kH][tz + kH];
+        const double r3 = sm.u[3][ty + kH][tz + kH], b1 = sm.u[4][ty + kH][tz + kH];
+        const double b2 = sm.u[5][ty + kH][tz + kH], b3 = sm.u[6][ty + kH][tz + kH];
+        const double n1 = nv[1], n2 = nv[2], n3 = nv[3], m1 = nv[4], m2 = nv[5], m3 = nv[6];
+        const double svr = ((r1 * r1) + (r2 * r2)) + (r3 * r3);
+        const double svn = ((n1 * n1) + (n2 * n2)) + (n3 * n3);
+        const double sbr = ((b1 * b1) + (b2 * b2)) + (b3 * b3);
+        const double sbn = ((m1 * m1) + (m2 * m2)) + (m3 * m3);
+        const double dens_in = reinterpret_cast<const R *>(S.p[0])[c];
+        const double den8 = (8.0 * 3.141592653589793) * (1.0 + dens_in);
+        const double heat = (0.5 * (svr - svn)) + (__ddiv_rn(1.0, den8) * (sbr - sbn));
+        reinterpret_cast<R *>(S.p[0])[c] = vmax(nv[0], R(-0.9));
+#pragma unroll
+        for (int f = 1; f < NF; ++f)
+          if (f != 7) reinterpret_cast<R *>(S.p[f])[c] = nv[f];
+        reinterpret_cast<R *>(S.p[7])[c] = (R)((double)nv[7] + heat);
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // Conserved totals in FP64: mass perturbation, kinetic + magnetic energy,
 // s, and the x-momentum; fixed tree as in fm_reduce.cu.
 template <typename R>
@@ -591,9 +758,15 @@ int mhd_forward(int n, R *const *fields, R *work, int steps, cudaStream_t s) {
     else
       mhd_stage<R><<<grid, 128, 0, s>>>(in, S, out, n, kk);
   };
-  // 1 x-march, 0 per-point; default: x-march for double (0.155 vs 0.129 GLUP/s at 256^3),
-  // per-point for float (3.13 vs 2.75: the staging costs more than the shared faces save)
-  const int finish_kernel = fm::tune_get("mhd.finish", sizeof(R) == 8 ? 1 : 0);
+  // 2 shared slopes and faces, all fields per plane; 1 x-march one field at a time;
+  // 0 per-point.  Measured at 256^3 (GLUP/s of the whole step, 0/1/2): float
+  // 3.13/2.75/2.49, double 0.129/0.155/0.171 — the shared-memory forms pay for
+  // their staging and barriers at 2 CTAs per SM unless the arithmetic is FP64.
+  const int finish_kernel = fm::tune_get("mhd.finish", sizeof(R) == 8 ? 2 : 0);
+  const size_t fsmem = sizeof(FinishSmem<R>);
+  if (finish_kernel == 2)
+    FM_TRY_CUDA(cudaFuncSetAttribute(mhd_finish_v2<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)fsmem));
   int sms = 0;
   int st = fm::device_sm_count(&sms);
   if (st) return st;
@@ -612,7 +785,9 @@ int mhd_forward(int n, R *const *fields, R *work, int steps, cudaStream_t s) {
     stage(A, B, k3);
     stage(B, A, k2);
     stage(A, B, k1);
-    if (finish_kernel == 1)
+    if (finish_kernel == 2)
+      mhd_finish_v2<R><<<fgrid, 256, fsmem, s>>>(B, S, n, xchunk, ntiles_yz, ntiles, k1);
+    else if (finish_kernel == 1)
       mhd_finish_march<R><<<fgrid, 256, 0, s>>>(B, S, n, xchunk, ntiles_yz, ntiles, k1);
     else
       mhd_finish<R><<<grid, 128, 0, s>>>(B, S, n, k1);
