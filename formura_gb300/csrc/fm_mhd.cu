@@ -291,6 +291,57 @@ __global__ void __launch_bounds__(256)
     reinterpret_cast<R *>(O.p[q])[c] = ld<R>(S.p[q], c) + (k.dt_c * f[q]);
 }
 
+// Exact binary64 values of binary32 quantities for the FP64 numerical heat of
+// the float path, built on the integer pipes (the FP64 pipe is the scarce one):
+// a float widens to double exactly (rebias the exponent, shift the fraction),
+// and the square of a float is exact in double (a 24-bit significand squared
+// has at most 48 bits).  Zero is handled inline; subnormal, infinite and NaN
+// inputs take the FP64 instructions.  For R = double both are the plain
+// operations.
+__device__ __forceinline__ double widen(float a) {
+  const unsigned b = __float_as_uint(a);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u) {
+    const unsigned m = b & 0x7fffffu;
+    return __hiloint2double((int)((b & 0x80000000u) | ((e + 896u) << 20) | (m >> 3)),
+                            (int)(m << 29));
+  }
+  if ((b << 1) == 0u) return __hiloint2double((int)(b & 0x80000000u), 0);
+  return (double)a;
+}
+__device__ __forceinline__ double widen(double a) { return a; }
+
+__device__ __forceinline__ double exact_sq(float a) {
+  const unsigned b = __float_as_uint(a);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e - 1u < 254u) {
+    const unsigned M = (b & 0x7fffffu) | 0x800000u;
+    const unsigned long long P = (unsigned long long)M * M;  // in [2^46, 2^48)
+    const unsigned top = (unsigned)(P >> 47);                // 1 if P >= 2^47
+    const unsigned long long F = (P << (5 + (top ^ 1u))) & 0x000fffffffffffffull;
+    const unsigned E = 2u * e + 769u + top;                  // biased exponent
+    return __hiloint2double((int)((E << 20) | (unsigned)(F >> 32)), (int)(unsigned)F);
+  }
+  if ((b << 1) == 0u) return 0.0;
+  const double d = (double)a;
+  return d * d;
+}
+__device__ __forceinline__ double exact_sq(double a) { return a * a; }
+
+// numerical_heat (3d-mhd-rk4.fmr:141-143) in FP64: r, b the velocity and field
+// of the stage output, nn, nm after the viscosity step, dens the step's input
+// density perturbation.
+template <typename R>
+__device__ __forceinline__ double numerical_heat(const R r[3], const R b[3], const R nn[3],
+                                                 const R nm[3], R dens) {
+  const double svr = (exact_sq(r[0]) + exact_sq(r[1])) + exact_sq(r[2]);
+  const double svn = (exact_sq(nn[0]) + exact_sq(nn[1])) + exact_sq(nn[2]);
+  const double sbr = (exact_sq(b[0]) + exact_sq(b[1])) + exact_sq(b[2]);
+  const double sbn = (exact_sq(nm[0]) + exact_sq(nm[1])) + exact_sq(nm[2]);
+  const double den8 = (8.0 * 3.141592653589793) * (1.0 + widen(dens));
+  return (0.5 * (svr - svn)) + (__ddiv_rn(1.0, den8) * (sbr - sbn));
+}
+
 // `<%` of three: fmin(0, fmax(a, fmax(b, c))) + fmax(0, fmin(a, fmin(b, c)))
 template <typename R>
 __device__ __forceinline__ R minmod3(R a, R b, R c) {
@@ -357,23 +408,18 @@ __global__ void __launch_bounds__(128)
     nv[f] = w;
   }
   // numerical_heat (3d-mhd-rk4.fmr:141-143), always in FP64; dens = the
-  // step's input density perturbation.
-  const double r1 = ld<R>(N.p[1], c), r2 = ld<R>(N.p[2], c), r3 = ld<R>(N.p[3], c);
-  const double b1 = ld<R>(N.p[4], c), b2 = ld<R>(N.p[5], c), b3 = ld<R>(N.p[6], c);
-  const double n1 = nv[1], n2 = nv[2], n3 = nv[3], m1 = nv[4], m2 = nv[5], m3 = nv[6];
-  const double svr = ((r1 * r1) + (r2 * r2)) + (r3 * r3);
-  const double svn = ((n1 * n1) + (n2 * n2)) + (n3 * n3);
-  const double sbr = ((b1 * b1) + (b2 * b2)) + (b3 * b3);
-  const double sbn = ((m1 * m1) + (m2 * m2)) + (m3 * m3);
-  // S is written below, so it is read through the coherent path (not __ldg)
-  const double dens_in = reinterpret_cast<const R *>(S.p[0])[c];
-  const double den8 = (8.0 * 3.141592653589793) * (1.0 + dens_in);
-  const double heat = (0.5 * (svr - svn)) + (__ddiv_rn(1.0, den8) * (sbr - sbn));
+  // step's input density perturbation.  S is written below, so it is read
+  // through the coherent path (not __ldg).
+  const R r[3] = {ld<R>(N.p[1], c), ld<R>(N.p[2], c), ld<R>(N.p[3], c)};
+  const R b[3] = {ld<R>(N.p[4], c), ld<R>(N.p[5], c), ld<R>(N.p[6], c)};
+  const R nn[3] = {nv[1], nv[2], nv[3]}, nm[3] = {nv[4], nv[5], nv[6]};
+  const double heat =
+      numerical_heat<R>(r, b, nn, nm, reinterpret_cast<const R *>(S.p[0])[c]);
   reinterpret_cast<R *>(S.p[0])[c] = vmax(nv[0], R(-0.9));
 #pragma unroll
   for (int f = 1; f < NF; ++f)
     if (f != 7) reinterpret_cast<R *>(S.p[f])[c] = nv[f];
-  reinterpret_cast<R *>(S.p[7])[c] = (R)((double)nv[7] + heat);
+  reinterpret_cast<R *>(S.p[7])[c] = (R)(widen(nv[7]) + heat);
 }
 
 // mhd_finish_march: the same finishing step with every face flux computed
@@ -469,24 +515,17 @@ __global__ void __launch_bounds__(256)
             // numerical_heat (3d-mhd-rk4.fmr:141-143), always in FP64; the new
             // velocities and fields were written to S by fields 1..6; dens = the
             // step's input density perturbation, still in S (field 0 comes last)
-            const double r1 = ld<R>(N.p[1], c), r2 = ld<R>(N.p[2], c), r3 = ld<R>(N.p[3], c);
-            const double b1 = ld<R>(N.p[4], c), b2 = ld<R>(N.p[5], c), b3 = ld<R>(N.p[6], c);
-            const R *Sp1 = reinterpret_cast<const R *>(S.p[1]);
-            const R *Sp2 = reinterpret_cast<const R *>(S.p[2]);
-            const R *Sp3 = reinterpret_cast<const R *>(S.p[3]);
-            const R *Sp4 = reinterpret_cast<const R *>(S.p[4]);
-            const R *Sp5 = reinterpret_cast<const R *>(S.p[5]);
-            const R *Sp6 = reinterpret_cast<const R *>(S.p[6]);
-            const double n1 = Sp1[c], n2 = Sp2[c], n3 = Sp3[c];
-            const double m1 = Sp4[c], m2 = Sp5[c], m3 = Sp6[c];
-            const double svr = ((r1 * r1) + (r2 * r2)) + (r3 * r3);
-            const double svn = ((n1 * n1) + (n2 * n2)) + (n3 * n3);
-            const double sbr = ((b1 * b1) + (b2 * b2)) + (b3 * b3);
-            const double sbn = ((m1 * m1) + (m2 * m2)) + (m3 * m3);
-            const double dens_in = reinterpret_cast<const R *>(S.p[0])[c];
-            const double den8 = (8.0 * 3.141592653589793) * (1.0 + dens_in);
-            const double heat = (0.5 * (svr - svn)) + (__ddiv_rn(1.0, den8) * (sbr - sbn));
-            out[c] = (R)((double)w + heat);
+            const R r[3] = {ld<R>(N.p[1], c), ld<R>(N.p[2], c), ld<R>(N.p[3], c)};
+            const R b[3] = {ld<R>(N.p[4], c), ld<R>(N.p[5], c), ld<R>(N.p[6], c)};
+            const R nn[3] = {reinterpret_cast<const R *>(S.p[1])[c],
+                             reinterpret_cast<const R *>(S.p[2])[c],
+                             reinterpret_cast<const R *>(S.p[3])[c]};
+            const R nm[3] = {reinterpret_cast<const R *>(S.p[4])[c],
+                             reinterpret_cast<const R *>(S.p[5])[c],
+                             reinterpret_cast<const R *>(S.p[6])[c]};
+            const double heat =
+                numerical_heat<R>(r, b, nn, nm, reinterpret_cast<const R *>(S.p[0])[c]);
+            out[c] = (R)(widen(w) + heat);
           } else {
             out[c] = w;
           }
@@ -642,22 +681,17 @@ __global__ void __launch_bounds__(256, 2)
           csl[f] = sl1;
         }
         // numerical_heat (3d-mhd-rk4.fmr:141-143), always in FP64
-        const double r1 = sm.u[1][ty + kH][tz + kH], r2 = sm.u[2][ty + kH][tz + kH];
-        const double r3 = sm.u[3][ty + kH][tz + kH], b1 = sm.u[4][ty + kH][tz + kH];
-        const double b2 = sm.u[5][ty + kH][tz + kH], b3 = sm.u[6][ty + kH][tz + kH];
-        const double n1 = nv[1], n2 = nv[2], n3 = nv[3], m1 = nv[4], m2 = nv[5], m3 = nv[6];
-        const double svr = ((r1 * r1) + (r2 * r2)) + (r3 * r3);
-        const double svn = ((n1 * n1) + (n2 * n2)) + (n3 * n3);
-        const double sbr = ((b1 * b1) + (b2 * b2)) + (b3 * b3);
-        const double sbn = ((m1 * m1) + (m2 * m2)) + (m3 * m3);
-        const double dens_in = reinterpret_cast<const R *>(S.p[0])[c];
-        const double den8 = (8.0 * 3.141592653589793) * (1.0 + dens_in);
-        const double heat = (0.5 * (svr - svn)) + (__ddiv_rn(1.0, den8) * (sbr - sbn));
+        const int cy = ty + kH, cz = tz + kH;
+        const R r[3] = {sm.u[1][cy][cz], sm.u[2][cy][cz], sm.u[3][cy][cz]};
+        const R b[3] = {sm.u[4][cy][cz], sm.u[5][cy][cz], sm.u[6][cy][cz]};
+        const R nn[3] = {nv[1], nv[2], nv[3]}, nm[3] = {nv[4], nv[5], nv[6]};
+        const double heat =
+            numerical_heat<R>(r, b, nn, nm, reinterpret_cast<const R *>(S.p[0])[c]);
         reinterpret_cast<R *>(S.p[0])[c] = vmax(nv[0], R(-0.9));
 #pragma unroll
         for (int f = 1; f < NF; ++f)
           if (f != 7) reinterpret_cast<R *>(S.p[f])[c] = nv[f];
-        reinterpret_cast<R *>(S.p[7])[c] = (R)((double)nv[7] + heat);
+        reinterpret_cast<R *>(S.p[7])[c] = (R)(widen(nv[7]) + heat);
       }
       __syncthreads();
     }
