@@ -16,6 +16,8 @@
 #include <mutex>
 
 #include "fm_common.cuh"
+#include "fm_softfp.cuh"
+#include "fm_tune.h"
 
 namespace {
 
@@ -118,6 +120,86 @@ __global__ void __launch_bounds__(256)
   dst[(size_t)x * ny + y] = diff_cell(src, x, y, nx, ny, lane, coef);
 }
 
+// x * 0.5 for a double, exactly, on the integer pipe: for normal x with a
+// biased exponent >= 2 the product is x with the exponent lowered by one;
+// zero is unchanged.  A result that would be subnormal (exponent 1), a
+// subnormal x, Inf and NaN take the FP64 multiplication out of line.
+static __device__ __noinline__ double half_slow(double x) { return __dmul_rn(x, 0.5); }
+__device__ __forceinline__ double half(double x) {
+  const unsigned h = (unsigned)__double2hiint(x), l = (unsigned)__double2loint(x);
+  const unsigned e = (h >> 20) & 0x7ffu;
+  double r = __hiloint2double((int)(h - (1u << 20)), (int)l);
+  if (((h << 1) | l) == 0u) r = x;
+  else if (e - 2u >= 2045u) r = half_slow(x);
+  return r;
+}
+
+// diff2d_tb: K steps per grid barrier.  A CTA owns a TX x TY tile; per block of
+// k <= K steps it stages the tile and a k-cell periodic halo into shared
+// memory, advances k steps there (step s updates the cells within k - s of
+// the tile), and writes the tile back.  Per cell, the expressions of
+// diff_cell, with x * 0.5 by half() and coef * g by fm::soft::mul_const_s
+// (when coef is normal and nonzero): the same values, bit for bit, with half
+// of the FP64 instructions.
+constexpr int kDX = 16, kDY = 32;
+template <int K>
+__global__ void __launch_bounds__(256)
+    diff2d_tb(double *a, double *b, int nx, int ny, double coef, fm::soft::MulConstS cs,
+              int soft_coef, int steps, int ntx, int nty, GridSync *gs) {
+  constexpr int RX = kDX + 2 * K, RY = kDY + 2 * K;
+  __shared__ double buf[2][RX][RY];
+  unsigned gen = 0;
+  double *src = a, *dst = b;
+  const int ntiles = ntx * nty;
+  for (int done = 0; done < steps; done += K) {
+    const int k = min(K, steps - done);
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const int x0 = (t / nty) * kDX, y0 = (t % nty) * kDY;
+      const int rx = kDX + 2 * k, ry = kDY + 2 * k;
+      for (int q = threadIdx.x; q < rx * ry; q += 256) {
+        const int i = q / ry, j = q - i * ry;
+        int gx = (x0 - k + i) % nx;
+        gx = gx < 0 ? gx + nx : gx;
+        int gy = (y0 - k + j) % ny;
+        gy = gy < 0 ? gy + ny : gy;
+        buf[0][i][j] = __ldcg(src + (size_t)gx * ny + gy);
+      }
+      __syncthreads();
+      for (int st = 1; st <= k; ++st) {
+        const int lo = st, hx = rx - st, hy = ry - st;  // update [lo, hx) x [lo, hy)
+        const int w = hy - lo;
+        const double(*in)[RY] = buf[(st - 1) & 1];
+        double(*out)[RY] = buf[st & 1];
+        for (int q = threadIdx.x; q < (hx - lo) * w; q += 256) {
+          const int i = lo + q / w, j = lo + q % w;
+          const double av = in[i][j];
+          const double f_1 = half(av - in[i][j - 1]);
+          const double f_0 = half(in[i][j + 1] - av);
+          const double e_0 = half(in[i + 1][j] - av);
+          const double e_1 = half(av - in[i - 1][j]);
+          const double e_2 = half(e_0 - e_1);
+          const double f_2 = half(f_0 - f_1);
+          const double g = e_2 + f_2;
+          const double h = soft_coef ? fm::soft::mul_const_s(g, cs) : coef * g;
+          out[i][j] = av + h;
+        }
+        __syncthreads();
+      }
+      const double(*res)[RY] = buf[k & 1];
+      const int rows = min(kDX, nx - x0), cols = min(kDY, ny - y0);
+      for (int q = threadIdx.x; q < rows * cols; q += 256) {
+        const int i = q / cols, j = q - i * cols;
+        __stcg(dst + (size_t)(x0 + i) * ny + (y0 + j), res[i + k][j + k]);
+      }
+      __syncthreads();
+    }
+    if (!grid_barrier(gs, gridDim.x, gen)) return;
+    double *tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+}
+
 std::mutex g_mu;
 GridSync *g_sync[64] = {nullptr};
 
@@ -152,6 +234,40 @@ extern "C" int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
   int coop = 0, dev = 0;
   FM_TRY_CUDA(cudaGetDevice(&dev));
   FM_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  const int tb = fm::tune_get("diff2d.tb", 4);  // steps per grid barrier; 0: one step per barrier
+  if (coop && (tb == 2 || tb == 4 || tb == 8)) {
+    const int ntx = (nx + kDX - 1) / kDX, nty = (ny + kDY - 1) / kDY;
+    const void *fn = tb == 2 ? (const void *)diff2d_tb<2>
+                     : tb == 4 ? (const void *)diff2d_tb<4> : (const void *)diff2d_tb<8>;
+    int per = 0;
+    FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, 256, 0));
+    const int grid = (int)std::min<long long>((long long)ntx * nty, (long long)sms * std::max(per, 1));
+    if (per >= 1) {
+      GridSync *gs = nullptr;
+      st = get_sync(&gs);
+      if (st) return st;
+      FM_TRY_CUDA(cudaMemsetAsync(gs, 0, sizeof(GridSync), s));
+      const double ac = coef < 0 ? -coef : coef;
+      int soft = ac >= 0x1p-1022 && ac <= 0x1.fffffffffffffp1023;
+      fm::soft::MulConstS cs = soft ? fm::soft::make_mul_const_s(coef) : fm::soft::MulConstS();
+      double *a = dens, *b = work;
+      int nxv = nx, nyv = ny, stv = steps, ntxv = ntx, ntyv = nty;
+      double cf = coef;
+      void *args[] = {&a, &b, &nxv, &nyv, &cf, &cs, &soft, &stv, &ntxv, &ntyv, &gs};
+      FM_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s));
+      GridSync host;
+      FM_TRY_CUDA(cudaMemcpyAsync(&host, gs, sizeof(GridSync), cudaMemcpyDeviceToHost, s));
+      FM_TRY_CUDA(cudaStreamSynchronize(s));
+      if (host.err) {
+        fm::set_error("fm_diff2d_f64_forward: grid barrier wait gave up");
+        return FM_ERR_TIMEOUT;
+      }
+      const int blocks = (steps + tb - 1) / tb;
+      if (blocks & 1) FM_TRY_CUDA(cudaMemcpyAsync(dens, work, n * sizeof(double),
+                                                  cudaMemcpyDeviceToDevice, s));
+      return FM_OK;
+    }
+  }
   if (coop && per_sm >= 1 && want >= 1) {
     GridSync *gs = nullptr;
     st = get_sync(&gs);

@@ -374,6 +374,8 @@ void fm_snapshot_destroy(fm_snapshot *s);
  *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)
  *   "gs2d_ens.tile"    default output tile edge of ensembles (32 or 64)
  *   "gs2d_ens.tb"      default steps per shared-memory pass of ensembles
+ *   "diff2d.tb"        steps per grid barrier of fm_diff2d_f64_forward on shared-memory
+ *                      tiles with a halo: 2, 4 (default) or 8; 0 = one step per barrier
  *   "mhd.stage"        Runge-Kutta stage kernel of fm_mhd_forward_*: 1 shared-memory tile
  *                      kernel (default), 0 per-point kernel
  *   "mhd.finish"       artificial-viscosity kernel of fm_mhd_forward_*: 2 x-marching kernel

@@ -38,3 +38,25 @@ def test_diffusion_program_drop_in(cuda_device):
     assert np.array_equal(prog.state["dens"], want)
     tot = prog.conserved_totals()
     assert abs(tot[0] - d0.sum()) < 1e-9 * d0.sum()
+
+
+@pytest.mark.parametrize("tb", [0, 2, 4, 8])
+@pytest.mark.parametrize("shape,steps", [((256, 256), 37), ((40, 64), 13), ((1, 32), 5),
+                                         ((19, 96), 9)])
+def test_diffusion_temporal_blocking_bit_exact(cuda_device, tb, shape, steps):
+    """K steps per grid barrier on shared-memory tiles with a K-cell halo
+    (diffusion.tb = K; 0 = one step per barrier), the exact x*0.5 and coef*g
+    on the integer pipes: bit-exact for every K, step counts that are not
+    multiples of K, and shapes that are not multiples of the 16 x 32 tile."""
+    from formura_gb300 import _lib
+
+    L = _lib.lib()
+    try:
+        L.fm_tune_set(b"diff2d.tb", tb)
+        d0 = inits.diffusion_2d(*shape, seed=steps)
+        d = torch.from_numpy(d0).cuda()
+        kernels.diff2d_f64_forward(d, torch.empty_like(d), 0.1, steps)
+        want = oracle.diff2d_f64(d0, steps, Dt=0.1, Dx=1.0)
+        assert np.array_equal(d.cpu().numpy(), want)
+    finally:
+        L.fm_tune_clear()
