@@ -238,7 +238,7 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
         "graph_captured": True, "one_persistent_launch": True,
         "sequential_per_instance_launches_glups": round(seq_cells * 100 / ssec / 1e9, 2),
         "sequential_sample": "32 of 512 instances x 100 steps, one launch per step",
-        "kernel": "gs2d_ensemble"}
+        "kernel": "gs2d_ens_wf (wavefront strips)" if res["tile"] == 1 else "gs2d_ensemble"}
     e.close()
     del Ue, Ve, wU, wV, bufs
     # -- 2D diffusion 256^2 FP64, 1000 steps in one persistent launch

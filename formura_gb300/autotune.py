@@ -25,7 +25,8 @@ from ._lib import lib
 from . import kernels
 
 ENSEMBLE_CANDIDATES: Tuple[Tuple[int, int], ...] = (
-    (32, 2), (32, 4), (32, 8), (64, 1), (64, 2), (64, 4), (64, 8))
+    (32, 2), (32, 4), (32, 8), (64, 1), (64, 2), (64, 4), (64, 8),
+    (1, 2), (1, 4), (1, 6), (1, 8))  # tile 1: wavefront strips streamed along x
 
 
 def _cache_path() -> Path:

@@ -217,6 +217,148 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---------------------------------------------------------------- wavefront form
+// gs2d_ens_wf<T>: one WARP owns a strip of 64 consecutive y cells of one
+// instance (two cells per lane; periodic wrap inside the instance) and streams
+// it along x over a chunk of planes, advancing up to T time levels in a
+// pipeline: at iteration i it loads plane i (level 0) and level s = 1..T
+// advances plane i-s from level s-1's planes i-s-1, i-s, i-s+1, held in a
+// 3-plane register window per level; the y neighbours are the lane's other
+// cell or the next/previous lane's (warp shuffles).  No shared memory and no
+// block barrier: warps run independently.  Level s is valid on strip cells
+// [s, 64-s), so a strip writes its middle 64-2T cells (its output strip) and
+// the planes [x0, x1) of its chunk.  Blocks of T steps meet at the grid
+// barrier, as in gs2d_ensemble.  Same gs2_cell arithmetic: bit-identical.
+struct WfTile {
+  int inst;
+  int ys;      // first output y of the strip
+  int x0, x1;  // output planes [x0, x1)
+};
+constexpr int kWfWidth = 64;
+
+template <int T>
+__global__ void __launch_bounds__(128)
+    gs2d_ens_wf(const EnsInst *__restrict__ insts, const WfTile *__restrict__ tiles, int ntiles,
+                float *U0, float *V0, float *U1, float *V1, int steps, int tb, GridSync *gs) {
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const int nw = gridDim.x * 4;
+  const int jA = 2 * lane, jB = jA + 1;
+  unsigned gen = 0;
+  int blk = 0;
+  for (int done = 0; done < steps; done += tb, ++blk) {
+    const int tr = min(tb, steps - done);  // levels of this block, <= T
+    const float *Us = (blk & 1) ? U1 : U0;
+    const float *Vs = (blk & 1) ? V1 : V0;
+    float *Ud = (blk & 1) ? U0 : U1;
+    float *Vd = (blk & 1) ? V0 : V1;
+    for (int t = gw; t < ntiles; t += nw) {
+      const WfTile tl = tiles[t];
+      const EnsInst in = insts[tl.inst];
+      const int n = in.n;
+      const Gs2Const c = in.c;
+      const float *Ui = Us + in.off, *Vi = Vs + in.off;
+      float *Uo = Ud + in.off, *Vo = Vd + in.off;
+      int yA = (tl.ys - T + jA) % n;
+      yA = yA < 0 ? yA + n : yA;
+      int yB = (tl.ys - T + jB) % n;
+      yB = yB < 0 ? yB + n : yB;
+      const bool oA = jA >= T && jA < kWfWidth - T && tl.ys + jA - T < n;
+      const bool oB = jB >= T && jB < kWfWidth - T && tl.ys + jB - T < n;
+      float wu[T][3][2], wv[T][3][2];
+#pragma unroll
+      for (int s = 0; s < T; ++s)
+#pragma unroll
+        for (int p = 0; p < 3; ++p) wu[s][p][0] = wu[s][p][1] = wv[s][p][0] = wv[s][p][1] = 0.0f;
+      constexpr int kPF = 2;
+      float pu[kPF][2], pv[kPF][2];
+#pragma unroll
+      for (int k = 0; k < kPF; ++k) {
+        int x = (tl.x0 - tr + k) % n;
+        x = x < 0 ? x + n : x;
+        const size_t r = (size_t)x * n;
+        pu[k][0] = __ldcg(Ui + r + yA);
+        pu[k][1] = __ldcg(Ui + r + yB);
+        pv[k][0] = __ldcg(Vi + r + yA);
+        pv[k][1] = __ldcg(Vi + r + yB);
+      }
+      const int iend = tl.x1 + tr;
+      for (int i = tl.x0 - tr; i < iend; ++i) {
+        // level 0: plane i
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          wu[0][0][q] = wu[0][1][q];
+          wu[0][1][q] = wu[0][2][q];
+          wu[0][2][q] = pu[0][q];
+          wv[0][0][q] = wv[0][1][q];
+          wv[0][1][q] = wv[0][2][q];
+          wv[0][2][q] = pv[0][q];
+        }
+#pragma unroll
+        for (int k = 0; k + 1 < kPF; ++k)
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            pu[k][q] = pu[k + 1][q];
+            pv[k][q] = pv[k + 1][q];
+          }
+        if (i + kPF < iend) {
+          int x = (i + kPF) % n;
+          x = x < 0 ? x + n : x;
+          const size_t r = (size_t)x * n;
+          pu[kPF - 1][0] = __ldcg(Ui + r + yA);
+          pu[kPF - 1][1] = __ldcg(Ui + r + yB);
+          pv[kPF - 1][0] = __ldcg(Vi + r + yA);
+          pv[kPF - 1][1] = __ldcg(Vi + r + yB);
+        }
+        // levels 1..tr: level s advances plane i-s
+#pragma unroll
+        for (int s = 1; s <= T; ++s) {
+          if (s > tr) break;
+          const float uA = wu[s - 1][1][0], uB = wu[s - 1][1][1];
+          const float vA = wv[s - 1][1][0], vB = wv[s - 1][1][1];
+          const float uAl = __shfl_up_sync(0xffffffffu, uB, 1);    // cell jA - 1
+          const float uBr = __shfl_down_sync(0xffffffffu, uA, 1);  // cell jB + 1
+          const float vAl = __shfl_up_sync(0xffffffffu, vB, 1);
+          const float vBr = __shfl_down_sync(0xffffffffu, vA, 1);
+          float unA, vnA, unB, vnB;
+          gs2_cell(uA, vA, wu[s - 1][2][0], wu[s - 1][0][0], uB, uAl, wv[s - 1][2][0],
+                   wv[s - 1][0][0], vB, vAl, c, unA, vnA);
+          gs2_cell(uB, vB, wu[s - 1][2][1], wu[s - 1][0][1], uBr, uA, wv[s - 1][2][1],
+                   wv[s - 1][0][1], vBr, vA, c, unB, vnB);
+          if (s < tr) {
+            wu[s][0][0] = wu[s][1][0];
+            wu[s][1][0] = wu[s][2][0];
+            wu[s][2][0] = unA;
+            wu[s][0][1] = wu[s][1][1];
+            wu[s][1][1] = wu[s][2][1];
+            wu[s][2][1] = unB;
+            wv[s][0][0] = wv[s][1][0];
+            wv[s][1][0] = wv[s][2][0];
+            wv[s][2][0] = vnA;
+            wv[s][0][1] = wv[s][1][1];
+            wv[s][1][1] = wv[s][2][1];
+            wv[s][2][1] = vnB;
+          } else {
+            const int pp = i - tr;
+            if (pp >= tl.x0) {
+              const size_t r = (size_t)pp * n;
+              if (oA) {
+                __stcg(Uo + r + yA, unA);
+                __stcg(Vo + r + yA, vnA);
+              }
+              if (oB) {
+                __stcg(Uo + r + yB, unB);
+                __stcg(Vo + r + yB, vnB);
+              }
+            }
+          }
+        }
+      }
+    }
+    if (!grid_barrier(gs, gridDim.x, gen)) return;
+  }
+}
+
 }  // namespace
 
 // ============================================================== C ABI
@@ -229,6 +371,8 @@ struct fm_ensemble {
   EnsInst *d_inst = nullptr;
   EnsTile *d_tiles = nullptr;
   int ntiles = 0;
+  int kind = 0;  // 0 shared-memory tiles, 1 wavefront strips
+  int xchunk = 0;
   GridSync *d_sync = nullptr;
   // captured graph of the last forward call
   cudaGraphExec_t gexec = nullptr;
@@ -252,6 +396,16 @@ const void *pick_kernel(int ts, int tb) {
 #undef FM_ENS_CASE
   return nullptr;
 }
+
+const void *pick_wf(int tb) {
+  if (tb <= 2) return (const void *)gs2d_ens_wf<2>;
+  if (tb <= 4) return (const void *)gs2d_ens_wf<4>;
+  if (tb <= 6) return (const void *)gs2d_ens_wf<6>;
+  if (tb <= 8) return (const void *)gs2d_ens_wf<8>;
+  return nullptr;
+}
+
+int wf_tmax(int tb) { return tb <= 2 ? 2 : tb <= 4 ? 4 : tb <= 6 ? 6 : 8; }
 
 int kernel_tmax(int ts, int tb) {
   for (int t : {1, 2, 4, 8})
@@ -303,12 +457,13 @@ extern "C" int fm_gs2d_ensemble_create(fm_ensemble **out, int n_inst, const int 
                                        double dt, double dx, int tile, int tb) {
   FM_CHECK_ARG(out && sizes && F && k && n_inst >= 1, "fm_gs2d_ensemble_create: bad arguments");
   *out = nullptr;
-  if (tile == 0) tile = fm::tune_get("gs2d_ens.tile", 64);
-  if (tb == 0) tb = fm::tune_get("gs2d_ens.tb", 4);
-  FM_CHECK_ARG(pick_kernel(tile, tb) != nullptr,
-               "fm_gs2d_ensemble_create: unsupported tile %d / tb %d (tile 32 or 64, tb 1..8)",
-               tile, tb);
-  {
+  if (tile == 0) tile = fm::tune_get("gs2d_ens.tile", 1);
+  const int kind = tile == 1 ? 1 : 0;
+  if (tb == 0) tb = fm::tune_get("gs2d_ens.tb", kind == 1 ? 2 : 4);
+  FM_CHECK_ARG(kind == 1 ? (tb >= 1 && tb <= 8) : pick_kernel(tile, tb) != nullptr,
+               "fm_gs2d_ensemble_create: unsupported tile %d / tb %d (tile 32 or 64, or 1 for "
+               "wavefront strips; tb 1..8)", tile, tb);
+  if (kind == 0) {
     int dev = 0, optin = 0;
     FM_TRY_CUDA(cudaGetDevice(&dev));
     FM_TRY_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -323,8 +478,12 @@ extern "C" int fm_gs2d_ensemble_create(fm_ensemble **out, int n_inst, const int 
   e->n_inst = n_inst;
   e->ts = tile;
   e->tb = tb;
+  e->kind = kind;
+  e->xchunk = std::max(1, fm::tune_get("gs2d_ens.xchunk", 64));
+  const int wf_out = kWfWidth - 2 * wf_tmax(tb);  // output y per strip
   std::vector<EnsInst> hi(n_inst);
   std::vector<EnsTile> ht;
+  std::vector<WfTile> hw;
   long long off = 0;
   for (int i = 0; i < n_inst; ++i) {
     if (sizes[i] < 1) {
@@ -345,20 +504,28 @@ extern "C" int fm_gs2d_ensemble_create(fm_ensemble **out, int n_inst, const int 
     hi[i].c.dt = (float)dt;
     e->offsets.push_back(off);
     e->sizes.push_back(n);
-    for (int x0 = 0; x0 < n; x0 += tile)
-      for (int y0 = 0; y0 < n; y0 += tile) ht.push_back(EnsTile{i, x0, y0});
+    if (kind == 0) {
+      for (int x0 = 0; x0 < n; x0 += tile)
+        for (int y0 = 0; y0 < n; y0 += tile) ht.push_back(EnsTile{i, x0, y0});
+    } else {
+      for (int x0 = 0; x0 < n; x0 += e->xchunk)
+        for (int ys = 0; ys < n; ys += wf_out)
+          hw.push_back(WfTile{i, ys, x0, std::min(x0 + e->xchunk, n)});
+    }
     off += (long long)n * n;
   }
   e->total = off;
-  e->ntiles = (int)ht.size();
+  e->ntiles = kind == 0 ? (int)ht.size() : (int)hw.size();
+  const size_t tile_bytes = kind == 0 ? sizeof(EnsTile) * ht.size() : sizeof(WfTile) * hw.size();
+  const void *tile_src = kind == 0 ? (const void *)ht.data() : (const void *)hw.data();
   cudaError_t err;
   if ((err = cudaMalloc(&e->d_inst, sizeof(EnsInst) * n_inst)) != cudaSuccess ||
-      (err = cudaMalloc(&e->d_tiles, sizeof(EnsTile) * ht.size())) != cudaSuccess ||
+      (err = cudaMalloc((void **)&e->d_tiles, tile_bytes)) != cudaSuccess ||
       (err = cudaMalloc(&e->d_sync, sizeof(GridSync))) != cudaSuccess ||
       (err = cudaMemcpy(e->d_inst, hi.data(), sizeof(EnsInst) * n_inst,
                         cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (err = cudaMemcpy(e->d_tiles, ht.data(), sizeof(EnsTile) * ht.size(),
-                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+      (err = cudaMemcpy(e->d_tiles, tile_src, tile_bytes, cudaMemcpyHostToDevice)) !=
+          cudaSuccess) {
     cudaFree(e->d_inst);
     cudaFree(e->d_tiles);
     cudaFree(e->d_sync);
@@ -390,6 +557,21 @@ struct EnsLaunch {
 // Kernel choice, shared-memory opt-in and grid size; no stream work, so it
 // runs before a graph capture begins.
 int ens_prepare(fm_ensemble *e, EnsLaunch *L) {
+  if (e->kind == 1) {
+    L->kern = pick_wf(e->tb);
+    L->smem = 0;
+    int sms = 0;
+    int st = fm::device_sm_count(&sms);
+    if (st) return st;
+    int per_sm = 0;
+    FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L->kern, 128, 0));
+    if (per_sm < 1) {
+      fm::set_error("fm_gs2d_ensemble_forward: wavefront kernel does not fit on an SM");
+      return FM_ERR_UNSUPPORTED;
+    }
+    L->grid = std::max(1, std::min((e->ntiles + 3) / 4, sms * per_sm));
+    return FM_OK;
+  }
   const int tmax = kernel_tmax(e->ts, e->tb);
   L->kern = pick_kernel(e->ts, e->tb);
   L->smem = ens_smem(e->ts, tmax);
@@ -419,7 +601,8 @@ int ens_launch(fm_ensemble *e, const EnsLaunch &L, float *U, float *V, float *wU
   int nt = e->ntiles, stp = steps, tb = e->tb;
   GridSync *gs = e->d_sync;
   void *args[] = {&di, &dt, &nt, &U, &V, &wU, &wV, &stp, &tb, &gs};
-  FM_TRY_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(32, 8), args, smem, s));
+  FM_TRY_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), e->kind == 1 ? dim3(128) : dim3(32, 8),
+                                          args, smem, s));
   return FM_OK;
 }
 

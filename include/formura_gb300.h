@@ -149,8 +149,10 @@ int fm_gs2d_f32_forward(int nx, int ny, float *U, float *V, float *work_U,
  * (bit-identical results).
  *
  * fm_gs2d_ensemble_create builds the plan (device instance and tile tables):
- * `tile` = output tile edge (32 or 64; 0 = tuned default), `tb` = time steps
- * per shared-memory pass (1..8; 0 = tuned default).
+ * `tile` = output tile edge of the shared-memory kernel (32 or 64), or 1 for
+ * the wavefront kernel (one warp streams a 64-cell y strip along x, time
+ * levels pipelined in registers); 0 = tuned default; `tb` = time steps per
+ * pass over the state (1..8; 0 = tuned default).
  * fm_gs2d_ensemble_forward advances every instance `steps` steps in ONE
  * cooperative persistent launch (grid barrier between passes, bounded
  * waits); with use_graph != 0 the launch is captured once into a CUDA graph
@@ -372,7 +374,9 @@ void fm_snapshot_destroy(fm_snapshot *s);
  *   "gs3d_f64.xchunk"  x planes per CTA tile (0 = automatic)
  *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_tb_forward (1..4)
  *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)
- *   "gs2d_ens.tile"    default output tile edge of ensembles (32 or 64)
+ *   "gs2d_ens.tile"    default ensemble kernel: 1 wavefront strips (default), 32 or 64
+ *                      shared-memory tiles of that edge
+ *   "gs2d_ens.xchunk"  x planes per wavefront strip (default 64)
  *   "gs2d_ens.tb"      default steps per shared-memory pass of ensembles
  *   "diff2d.tb"        steps per grid barrier of fm_diff2d_f64_forward on shared-memory
  *                      tiles with a halo: 2, 4 (default) or 8; 0 = one step per barrier

@@ -1,5 +1,6 @@
 """Uneven 2D Gray-Scott ensembles in one persistent launch: bit-exact per
-instance against the oracle's binary32 pearson-2d DAG, for every tile and
+instance against the oracle's binary32 pearson-2d DAG, for every tile (32, 64; 1 = the
+wavefront strips) and
 blocking depth, with and without the captured CUDA graph."""
 import numpy as np
 import pytest
@@ -30,7 +31,8 @@ def run_ensemble(sizes, F, k, steps, tile, tb, use_graph, seed=3, calls=1):
     return e, U0, V0, U.cpu().numpy(), V.cpu().numpy()
 
 
-@pytest.mark.parametrize("tile,tb", [(64, 4), (32, 1), (32, 8), (64, 8), (64, 2), (32, 3)])
+@pytest.mark.parametrize("tile,tb", [(64, 4), (32, 1), (32, 8), (64, 8), (64, 2), (32, 3),
+                                     (1, 4), (1, 1), (1, 3), (1, 6), (1, 8), (1, 2)])
 def test_ensemble_bit_exact(cuda_device, tile, tb):
     sizes = [64, 128, 32, 100, 64, 256, 48]   # includes sizes that are not tile multiples
     F = [0.02, 0.03, 0.04, 0.05, 0.06, 0.035, 0.045]
