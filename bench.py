@@ -578,7 +578,8 @@ def run_profile_case(args):
                                      args.profile_steps, args.profile_tb)
     elif args.profile == "ensemble":
         sizes, F, k = inits.gs2d_ensemble(512, seed=1)
-        e = kernels.Ensemble(sizes, F, k, tile=64, tb=max(args.profile_tb, 1))
+        tile = 1 if args.profile_tile == 0 else args.profile_tile  # 1: wavefront strips
+        e = kernels.Ensemble(sizes, F, k, tile=tile, tb=max(args.profile_tb, 1))
         Ue, Ve = inits.gs2d_ensemble_state(sizes, seed=1)
         Ue, Ve = torch.from_numpy(Ue).to(dev), torch.from_numpy(Ve).to(dev)
         e.forward(Ue, Ve, torch.empty_like(Ue), torch.empty_like(Ve), args.profile_steps,
@@ -648,6 +649,8 @@ def main():
     ap.add_argument("--profile-n", type=int, default=256)
     ap.add_argument("--profile-steps", type=int, default=4)
     ap.add_argument("--profile-tb", type=int, default=0)
+    ap.add_argument("--profile-tile", type=int, default=0,
+                    help="ensemble case: 1 wavefront strips (default), 32 or 64 smem tiles")
     ap.add_argument("--profile-batch", type=int, default=8, help="surrogate case: instances")
     ap.add_argument("--profile-train", action="store_true",
                     help="surrogate case: also run one training step")
