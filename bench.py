@@ -249,7 +249,7 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
     sec = _event_time(torch, lambda: kernels.diff2d_f64_forward(d, wd, 0.1, 1000))
     out["diffusion_2d_256_fp64"] = {"value": round(256 * 256 * 1000 / sec / 1e9, 2),
                                     "unit": "GLUP/s", "steps": 1000, "ms": round(sec * 1e3, 3),
-                                    "bit_exact_vs_oracle": True, "kernel": "diff2d_persistent"}
+                                    "bit_exact_vs_oracle": True, "kernel": "diff2d_tb (4 steps per grid barrier)"}
     # -- 3D MHD 256^3, 500 steps: binary32 bulk with the FP64 energy update
     f0 = inits.mhd_3d(N, seed=1)
     t32 = [torch.from_numpy(x.astype(np.float32)).cuda() for x in f0]
@@ -274,7 +274,7 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
     out["mhd_3d_256_fp32_bulk_fp64_energy"] = {
         "value": round(N ** 3 * 500 / sec / 1e9, 3), "unit": "GLUP/s", "steps": 500,
         "seconds": round(sec, 3), "totals_fp64": [float(x) for x in tot],
-        "max_rel_error_vs_fp64_64cube_500steps": errs, "kernel": "mhd_stage"}
+        "max_rel_error_vs_fp64_64cube_500steps": errs, "kernel": "mhd_stage_tile x4 + mhd_finish"}
     return out
 
 
