@@ -413,6 +413,20 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def aggregate_replicas(dev_s: float, e2e_s: float, lups_per_rank: float, ws: int, device="cuda"):
+    """Whole-job throughput of N independent replicas: the slowest rank's
+    device and end-to-end times (MAX over ranks), all ranks' lattice updates.
+    Returns (value GLUP/s, e2e GLUP/s, dev_s, e2e_s) on every rank."""
+    import torch
+
+    times = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    dev_s, e2e_s = times.tolist()
+    lups = lups_per_rank * ws
+    return lups / dev_s / 1e9, lups / e2e_s / 1e9, dev_s, e2e_s
+
+
 def run_engine(args):
     import numpy as np
     import torch
@@ -474,13 +488,7 @@ def run_engine(args):
         prog.forward()
         U_final = prog.state["U"].copy()
 
-    times = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
-    if ws > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    dev_s, e2e_s = times.tolist()
-    lups = float(N ** 3) * M * args.steps * ws
-    value = lups / dev_s / 1e9
-    e2e = lups / e2e_s / 1e9
+    value, e2e, dev_s, e2e_s = aggregate_replicas(dev_s, e2e_s, float(N ** 3) * M * args.steps, ws)
     if rank != 0:
         if ws > 1:
             torch.distributed.destroy_process_group()
