@@ -125,3 +125,30 @@ def test_navigator_layout_matches_header(tmp_path):
     vals = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()))
     assert vals[0] == ctypes.sizeof(nav)
     assert vals[1:] == [getattr(nav, f).offset for f in fields]
+
+
+def test_argument_validation_of_the_other_entry_points(core_lib):
+    fake = ctypes.c_void_p(0x1000)
+    snap = ctypes.c_void_p()
+    shape = (ctypes.c_int * 3)(8, 8, 8)
+    assert core_lib.fm_snapshot_create(ctypes.byref(snap), 0, shape, 8) == 1
+    assert core_lib.fm_snapshot_create(ctypes.byref(snap), 3, shape, 3) == 1
+    bad = (ctypes.c_int * 3)(8, 0, 8)
+    assert core_lib.fm_snapshot_create(ctypes.byref(snap), 3, bad, 8) == 1
+    assert core_lib.fm_snapshot_plane_elems(None, 0) == -1
+    assert core_lib.fm_snapshot_begin(None, fake, 0, 0, None) == 1
+    fields = (ctypes.c_void_p * 9)(*([0x1000] * 9))
+    assert core_lib.fm_mhd_forward_f32(4, fields, fake, 1, None) == 1  # n >= 5
+    assert core_lib.fm_mhd_forward_f64(16, fields, None, 1, None) == 1
+    ens = ctypes.c_void_p()
+    sizes = (ctypes.c_int * 1)(64)
+    F = (ctypes.c_double * 1)(0.04)
+    k = (ctypes.c_double * 1)(0.06)
+    assert core_lib.fm_gs2d_ensemble_create(ctypes.byref(ens), 1, sizes, F, k, 2e-5, 1e-5, 1.0,
+                                            0.01, 128, 2) == 1
+    assert core_lib.fm_gs2d_ensemble_create(ctypes.byref(ens), 1, sizes, F, k, 2e-5, 1e-5, 1.0,
+                                            0.01, 1, 9) == 1
+    err = ctypes.c_void_p(0x2000)
+    assert core_lib.fm_conv3x3_fwd_bf16(1, 8, 8, 48, fake, fake, None, None, None, 0, None, fake,
+                                        None, err, None) == 1  # cout 32 or 64
+    assert core_lib.fm_diff2d_f64_forward_noalloc(2048, 1024, fake, 0.1, 1, None) == 1  # > 2^20
