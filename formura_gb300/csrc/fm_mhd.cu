@@ -422,120 +422,6 @@ __global__ void __launch_bounds__(128)
   reinterpret_cast<R *>(S.p[7])[c] = (R)(widen(nv[7]) + heat);
 }
 
-// mhd_finish_march: the same finishing step with every face flux computed
-// once.  The flux at a face is the same function of the same four values for
-// the cell on either side (face(u[i-1], u[i], u[i+1], u[i+2]) is cell i's
-// "+1/2" and cell i+1's "-1/2" flux), so it can be shared exactly:
-//   x: each thread marches along x over a chunk of planes and carries the
-//      flux at x+1/2 into the next plane as its x-1/2 flux (5-value window);
-//   y, z: per plane the CTA stages the field over its 32 (z) x 8 (y) tile plus
-//      a 2-point periodic halo into shared memory and computes the fluxes of
-//      the tile's faces (9 x 32 in y, 8 x 33 in z) once into shared memory.
-// Fields are processed one at a time in the order 1..6, 8, 7, 0: the
-// numerical heat (with s, field 7) reads the new velocities and fields of
-// 1..6 back from S, and the step's input density from S before field 0 is
-// overwritten.  Per cell: w = N_f; w = (w + f_{x-1/2}) - f_{x+1/2}; then y,
-// then z — the order of mhd_finish, so results are bit-identical with it.
-template <typename R>
-__global__ void __launch_bounds__(256)
-    mhd_finish_march(Fields N, Fields S, int n, int xchunk, int ntiles_yz, int ntiles,
-                     MhdC<R> k) {
-  __shared__ R su[kRY][kRZ];
-  __shared__ R sfy[kTY + 1][kTZ];
-  __shared__ R sfz[kTY][kTZ + 1];
-  const int tz = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const size_t sx = (size_t)n * n, sy = (size_t)n;
-  const int ntz = (n + kTZ - 1) / kTZ;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int tyz = t % ntiles_yz;
-    const int z0 = (tyz % ntz) * kTZ, y0 = (tyz / ntz) * kTY;
-    const int x0 = (t / ntiles_yz) * xchunk;
-    const int x1 = min(x0 + xchunk, n);
-    const int y = y0 + ty, z = z0 + tz;
-    const bool own = y < n && z < n;
-    const size_t yz = own ? (size_t)y * sy + z : 0;
-    for (int oi = 0; oi < NF; ++oi) {
-      const int f = oi < 6 ? oi + 1 : (oi == 6 ? 8 : (oi == 7 ? 7 : 0));  // 1..6, 8, 7, 0
-      const R *uf = reinterpret_cast<const R *>(N.p[f]);
-      R win[5];
-      R fxm = R(0);
-      if (own) {
-#pragma unroll
-        for (int d = 0; d < 4; ++d) {
-          int q = (x0 - 2 + d) % n;
-          q = q < 0 ? q + n : q;
-          win[d + 1] = __ldg(uf + (size_t)q * sx + yz);
-        }
-        fxm = face<R>(win[1], win[2], win[3], win[4]);  // flux at x0 - 1/2
-      }
-      for (int x = x0; x < x1; ++x) {
-        // stage plane x of field f (tile + 2-point halo in y and z)
-        for (int pt = threadIdx.x; pt < kNP; pt += 256) {
-          const int ry = pt / kRZ, rz = pt - ry * kRZ;
-          int gy = (y0 - kH + ry) % n;
-          gy = gy < 0 ? gy + n : gy;
-          int gz = (z0 - kH + rz) % n;
-          gz = gz < 0 ? gz + n : gz;
-          su[ry][rz] = __ldg(uf + (size_t)x * sx + (size_t)gy * sy + gz);
-        }
-        __syncthreads();
-        // y faces of rows y0-1 .. y0+kTY-1 (the face above each row), z faces
-        for (int q = threadIdx.x; q < (kTY + 1) * kTZ + kTY * (kTZ + 1); q += 256) {
-          if (q < (kTY + 1) * kTZ) {
-            const int r = q / kTZ, c = q - r * kTZ;  // face between rows r-1 and r (tile rows)
-            const int cz = c + kH;
-            sfy[r][c] = face<R>(su[r][cz], su[r + 1][cz], su[r + 2][cz], su[r + 3][cz]);
-          } else {
-            const int q2 = q - (kTY + 1) * kTZ;
-            const int r = q2 / (kTZ + 1), c = q2 - r * (kTZ + 1);
-            const int ry = r + kH;
-            sfz[r][c] = face<R>(su[ry][c], su[ry][c + 1], su[ry][c + 2], su[ry][c + 3]);
-          }
-        }
-        __syncthreads();
-        if (own) {
-          // x window: win[0..4] = u[x-2 .. x+2]
-          int q = (x + 2) % n;
-          win[0] = win[1];
-          win[1] = win[2];
-          win[2] = win[3];
-          win[3] = win[4];
-          win[4] = __ldg(uf + (size_t)q * sx + yz);
-          const R fxp = face<R>(win[1], win[2], win[3], win[4]);
-          const size_t c = (size_t)x * sx + yz;
-          R w = su[ty + kH][tz + kH];
-          w = (w + fxm) - fxp;
-          w = (w + sfy[ty][tz]) - sfy[ty + 1][tz];
-          w = (w + sfz[ty][tz]) - sfz[ty][tz + 1];
-          fxm = fxp;
-          R *out = reinterpret_cast<R *>(S.p[f]);
-          if (f == 0) {
-            out[c] = vmax(w, R(-0.9));
-          } else if (f == 7) {
-            // numerical_heat (3d-mhd-rk4.fmr:141-143), always in FP64; the new
-            // velocities and fields were written to S by fields 1..6; dens = the
-            // step's input density perturbation, still in S (field 0 comes last)
-            const R r[3] = {ld<R>(N.p[1], c), ld<R>(N.p[2], c), ld<R>(N.p[3], c)};
-            const R b[3] = {ld<R>(N.p[4], c), ld<R>(N.p[5], c), ld<R>(N.p[6], c)};
-            const R nn[3] = {reinterpret_cast<const R *>(S.p[1])[c],
-                             reinterpret_cast<const R *>(S.p[2])[c],
-                             reinterpret_cast<const R *>(S.p[3])[c]};
-            const R nm[3] = {reinterpret_cast<const R *>(S.p[4])[c],
-                             reinterpret_cast<const R *>(S.p[5])[c],
-                             reinterpret_cast<const R *>(S.p[6])[c]};
-            const double heat =
-                numerical_heat<R>(r, b, nn, nm, reinterpret_cast<const R *>(S.p[0])[c]);
-            out[c] = (R)(widen(w) + heat);
-          } else {
-            out[c] = w;
-          }
-        }
-        __syncthreads();
-      }
-    }
-  }
-}
-
 // The flux at the face between ua and ub from the slopes at both cells: the
 // expression of face() with slope(um, ua, ub) = sla and slope(ua, ub, u2) = slb.
 template <typename R>
@@ -792,10 +678,11 @@ int mhd_forward(int n, R *const *fields, R *work, int steps, cudaStream_t s) {
     else
       mhd_stage<R><<<grid, 128, 0, s>>>(in, S, out, n, kk);
   };
-  // 2 shared slopes and faces, all fields per plane; 1 x-march one field at a time;
-  // 0 per-point.  Measured at 256^3 (GLUP/s of the whole step, 0/1/2): float
-  // 3.13/2.75/2.49, double 0.129/0.155/0.171 — the shared-memory forms pay for
-  // their staging and barriers at 2 CTAs per SM unless the arithmetic is FP64.
+  // 2 shared slopes and faces, all fields per plane; 0 per-point.  Measured at
+  // 256^3 (GLUP/s of the whole step, 0/2): float 3.13/2.49, double 0.129/0.171
+  // — the shared-memory form pays for its staging and barriers at 2 CTAs per
+  // SM unless the arithmetic is FP64.  (A form marching one field at a time,
+  // 2.75/0.155, was slower than both.)
   const int finish_kernel = fm::tune_get("mhd.finish", sizeof(R) == 8 ? 2 : 0);
   const size_t fsmem = sizeof(FinishSmem<R>);
   if (finish_kernel == 2)
@@ -821,8 +708,6 @@ int mhd_forward(int n, R *const *fields, R *work, int steps, cudaStream_t s) {
     stage(A, B, k1);
     if (finish_kernel == 2)
       mhd_finish_v2<R><<<fgrid, 256, fsmem, s>>>(B, S, n, xchunk, ntiles_yz, ntiles, k1);
-    else if (finish_kernel == 1)
-      mhd_finish_march<R><<<fgrid, 256, 0, s>>>(B, S, n, xchunk, ntiles_yz, ntiles, k1);
     else
       mhd_finish<R><<<grid, 128, 0, s>>>(B, S, n, k1);
   }

@@ -384,8 +384,7 @@ void fm_snapshot_destroy(fm_snapshot *s);
  *                      kernel (default), 0 per-point kernel
  *   "mhd.finish"       artificial-viscosity kernel of fm_mhd_forward_*: 2 x-marching kernel
  *                      computing each slope and face flux once, all fields per plane
- *                      (default for f64), 1 the same one field at a time, 0 per-point
- *                      kernel (default for f32)
+ *                      (default for f64), 0 per-point kernel (default for f32)
  *   "mhd.xchunk"       x planes per tile of the x-marching kernel (0 = automatic)
  *   "conv.kernel"      fm_conv3x3_fwd_bf16 with 64 output channels: 1 weight-resident
  *                      persistent kernel (default; falls back to 0 when its staged region
