@@ -26,8 +26,6 @@ from __future__ import annotations
 
 import dataclasses
 import math
-import struct
-from fractions import Fraction
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np

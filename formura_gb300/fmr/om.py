@@ -172,7 +172,7 @@ class Evaluator:
             return Grid(self.norm_offset(t.offsets), elem_of(inner))
         raise FmrSemanticError("type %r is not a node type" % (t,))
 
-    def cast(self, t: Union[P.TypeE, NodeType, "TupleTypeV"], v: Value) -> Value:
+    def cast(self, t: Union[P.TypeE, NodeType], v: Value) -> Value:
         if isinstance(t, (P.TopT, P.FunT)):
             return v
         if isinstance(t, P.TupleT):

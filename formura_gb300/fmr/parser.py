@@ -27,7 +27,7 @@ from __future__ import annotations
 import dataclasses
 import unicodedata
 from fractions import Fraction
-from typing import List, Optional, Sequence, Tuple, Union
+from typing import List, Optional, Tuple, Union
 
 KEYWORDS = {"begin", "end", "function", "returns", "let", "in", "fun", "dimension", "axes",
             "if", "then", "else", "const", "extern", "manifest",

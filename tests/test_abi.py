@@ -3,7 +3,6 @@ arguments before touching the device, and fails loudly without a GPU."""
 import ctypes
 import re
 import subprocess
-from pathlib import Path
 
 import pytest
 

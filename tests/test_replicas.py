@@ -2,7 +2,6 @@
 rank, whole-job throughput = all ranks' lattice updates over the slowest
 rank's time.  Checked here with world_size 2 on CPU (gloo, 127.0.0.1); the
 reference arm runs on rank 0 only."""
-import json
 import os
 import socket
 import subprocess
