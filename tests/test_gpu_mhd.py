@@ -94,11 +94,13 @@ def test_mhd_kernel_variants_agree(cuda_device, n, dtype):
     outs = []
     L = _lib.lib()
     try:
-        for kern, fin, xc in ((0, 0, 0), (1, 2, 0), (1, 2, 5), (1, 2, 3), (0, 2, 1)):
+        for kern, fin, xc in ((0, 0, 0), (1, 2, 0), (1, 2, 5), (1, 2, 3), (0, 2, 1), (2, 0, 16),
+                              (2, 0, 5), (2, 2, 1)):
             L.fm_tune_clear()
             L.fm_tune_set(b"mhd.stage", kern)
             L.fm_tune_set(b"mhd.finish", fin)
             L.fm_tune_set(b"mhd.xchunk", xc)
+            L.fm_tune_set(b"mhd.stage_xchunk", xc if xc else 16)
             t = [torch.from_numpy(x).to(dtype).to(cuda_device) for x in f0]
             kernels.mhd_forward(t, torch.empty(18 * n ** 3, dtype=dtype, device=cuda_device), 3)
             outs.append([x.cpu().numpy() for x in t])
