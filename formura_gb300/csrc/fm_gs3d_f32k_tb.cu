@@ -110,6 +110,9 @@ __global__ void __launch_bounds__(kE *kE, 1)
       pcu[k] = __ldg(cU + g);
       pcv[k] = __ldg(cV + g);
     }
+    // unrolled by 6 = lcm(3-plane windows, 2 shared-memory parities): the window
+    // rotation becomes register renaming instead of moves (210 -> 228 GLUP/s at T = 3)
+#pragma unroll 6
     for (int i = x0 - T; i < x1 + T; ++i) {
       const int par = i & 1;
       // ---- level 0: plane i from the prefetch queue; queue plane i+kPF
