@@ -187,12 +187,19 @@ __global__ void __launch_bounds__(256)
   const int tz = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int z0 = blockIdx.x * kTZ, y0 = blockIdx.y * kTY, x = blockIdx.z;
   const size_t sx = (size_t)n * n, sy = (size_t)n;
+  const bool big = n >= kRZ;  // one conditional add/subtract wraps every region coordinate
   for (int pt = threadIdx.x; pt < kNP; pt += 256) {
     const int ry = pt / kRZ, rz = pt - ry * kRZ;
-    int gy = (y0 - kH + ry) % n;
-    gy = gy < 0 ? gy + n : gy;
-    int gz = (z0 - kH + rz) % n;
-    gz = gz < 0 ? gz + n : gz;
+    int gy = y0 - kH + ry, gz = z0 - kH + rz;
+    if (big) {
+      gy = gy < 0 ? gy + n : (gy >= n ? gy - n : gy);
+      gz = gz < 0 ? gz + n : (gz >= n ? gz - n : gz);
+    } else {
+      gy %= n;
+      gy = gy < 0 ? gy + n : gy;
+      gz %= n;
+      gz = gz < 0 ? gz + n : gz;
+    }
     const size_t i = (size_t)x * sx + (size_t)gy * sy + gz;
     const R dn = ld<R>(Q.p[0], i);
     const R v[3] = {ld<R>(Q.p[1], i), ld<R>(Q.p[2], i), ld<R>(Q.p[3], i)};
