@@ -33,6 +33,10 @@ def _random_state(prog, rng):
     ("fmr-features.fmr", dict(intra_node_shape=[7, 33], monitor_interval=3)),
     ("gray-scott-3d.fmr", dict(intra_node_shape=[16, 24, 40], monitor_interval=5)),
     ("diffusion-2d.fmr", dict(intra_node_shape=[64, 48], monitor_interval=7)),
+    ("fmr-1d-float.fmr", {}),
+    ("fmr-1d-float.fmr", dict(intra_node_shape=[7], monitor_interval=5)),
+    ("fmr-3d-advection.fmr", {}),
+    ("fmr-3d-advection.fmr", dict(intra_node_shape=[5, 3, 33], monitor_interval=4)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)
@@ -72,3 +76,17 @@ def test_generated_gs3d_equals_hand_kernel(cuda_device, tmp_path):
     assert np.array_equal(prog.state["V"], V.cpu().numpy())
     tot = prog.conserved_totals()
     np.testing.assert_allclose(tot, [prog.state["U"].sum(), prog.state["V"].sum()], rtol=1e-12)
+
+
+def test_generated_program_with_device_libm_within_tolerance(cuda_device, tmp_path):
+    """`**` and extern exp on grid values run on the device's pow/exp, which
+    are not bit-identical with the host's libm: agreement to 1e-12 relative."""
+    p = load_program(EX / "fmr-libm.fmr")
+    prog = load_lib(p, outdir=tmp_path)
+    prog.init()
+    a0 = np.random.default_rng(5).random(p.shape)
+    prog.state["a"][...] = a0
+    prog.forward()
+    prog.forward()
+    want = fmr_c.FmrOracle(p.fmr_source, p.shape).run({"a": a0}, 2 * p.steps_per_forward)["a"]
+    np.testing.assert_allclose(prog.state["a"], want, rtol=1e-12, atol=1e-14)
