@@ -275,6 +275,18 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
         "value": round(N ** 3 * 500 / sec / 1e9, 3), "unit": "GLUP/s", "steps": 500,
         "seconds": round(sec, 3), "totals_fp64": [float(x) for x in tot],
         "max_rel_error_vs_fp64_64cube_500steps": errs, "kernel": "mhd_stage_tile x4 + mhd_finish"}
+    # -- 3D MHD 256^3 all-FP64 (bit-exact with the oracle), 10 steps
+    t64 = [torch.from_numpy(x).cuda() for x in f0]
+    w64 = torch.empty(18 * N ** 3, dtype=torch.float64, device="cuda")
+    kernels.mhd_forward([x.clone() for x in t64], w64, 1)
+    sec64 = _event_time(torch, lambda: kernels.mhd_forward(t64, w64, 10))
+    del t64, w64
+    out["mhd_3d_256_fp64"] = {
+        "value": round(N ** 3 * 10 / sec64 / 1e9, 4), "unit": "GLUP/s", "steps": 10,
+        "seconds": round(sec64, 3), "bit_exact_vs_oracle": True,
+        "kernel": "mhd_stage_tile<double, 1> x4 + mhd_finish_v2<double, 1> "
+                  "(exact binary64 scalings, constant products, divisions, fmax/fmin on the "
+                  "integer pipes)"}
     return out
 
 
@@ -594,11 +606,11 @@ def run_profile_case(args):
                   use_graph=False)
         e.status()
         e.close()
-    elif args.profile == "mhd":
+    elif args.profile in ("mhd", "mhd_f64"):
+        dt = torch.float64 if args.profile == "mhd_f64" else torch.float32
         f0 = inits.mhd_3d(n, seed=1)
-        t = [torch.from_numpy(x.astype("float32")).to(dev) for x in f0]
-        kernels.mhd_forward(t, torch.empty(18 * n ** 3, dtype=torch.float32, device=dev),
-                            args.profile_steps)
+        t = [torch.from_numpy(x).to(dt).to(dev) for x in f0]
+        kernels.mhd_forward(t, torch.empty(18 * n ** 3, dtype=dt, device=dev), args.profile_steps)
     elif args.profile == "diff2d":
         d0 = inits.diffusion_2d(n, n, seed=1)
         d = torch.from_numpy(d0).to(dev)
@@ -651,7 +663,7 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
     ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",
-                                          "mhd", "diff2d", "surrogate", "fmr_gs3d"],
+                                          "mhd", "mhd_f64", "diff2d", "surrogate", "fmr_gs3d"],
                     default=None,
                     help="run a small case of one kernel for an ncu capture, then exit")
     ap.add_argument("--profile-n", type=int, default=256)

@@ -1,6 +1,6 @@
-// fm_softfp.cuh — correctly rounded binary64 division by a constant and
-// binary64 multiplication computed on the INTEGER pipes, with no FP64
-// instruction on the fast path.
+// fm_softfp.cuh — correctly rounded binary64 division (by a constant, or by a
+// run-time divisor), multiplication and scaling by powers of two computed on
+// the INTEGER pipes, with no FP64 instruction on the fast path.
 //
 // Why: a GB300 SM retires 2 FP64 lanes per clock against 64 integer-ALU and
 // 64 IMAD lanes, and the FP64 stencils of this library are FP64-pipe-bound
@@ -25,6 +25,7 @@
 // the bit-exactness checks run on the CPU against the host's IEEE arithmetic.
 #pragma once
 
+#include <math.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -141,7 +142,10 @@ inline DivConstS make_div_const_s(double d) {
   return c;
 }
 
-FM_SOFT_HD double div_const_s(double x, const DivConstS &c) {
+// The quotient step for a prepared divisor c; the result's sign is x's XOR
+// dsign, and dnormal says whether the divisor is a normal number (a zero,
+// subnormal, infinite or NaN divisor takes the slow path with c.d).
+FM_SOFT_HD double div_core(double x, const DivConstS &c, uint32_t dsign, bool dnormal) {
   const uint32_t xh = hi_word(x), xl = lo_word(x);
   const uint32_t ex = (xh >> 20) & 0x7ffu;
   const uint32_t mxh = (xh & 0x000fffffu) | 0x00100000u;
@@ -163,15 +167,122 @@ FM_SOFT_HD double div_const_s(double x, const DivConstS &c) {
   const int64_t diff = (int64_t)(sx - prod);
   const uint64_t Qr = Q + (diff > 0 ? 1ull : 0ull);
   const int E = (int)ex - c.ed + 1022 + (int)A;
-  // pack: (E-1) << 52 plus Q (implicit bit included), sign of x
-  const uint32_t rh = (((uint32_t)(E - 1) << 20) + (uint32_t)(Qr >> 32)) | (xh & 0x80000000u);
+  // pack: (E-1) << 52 plus Q (implicit bit included), the quotient's sign
+  const uint32_t sign = (xh ^ dsign) & 0x80000000u;
+  const uint32_t rh = (((uint32_t)(E - 1) << 20) + (uint32_t)(Qr >> 32)) | sign;
   double q = from_words(rh, (uint32_t)Qr);
   const bool zero = ((xh << 1) | xl) == 0u;
   const bool ok = (ex - 1u) < 2046u && (uint32_t)(E - 1) < 2046u;
-  if (zero) q = x;
-  if (!(ok || zero)) q = div_slow(x, c.d);
+  if (zero) q = from_words(sign, 0u);
+  if (!((ok || zero) && dnormal)) q = div_slow(x, c.d);
   return q;
 }
+
+FM_SOFT_HD double div_const_s(double x, const DivConstS &c) { return div_core(x, c, 0u, true); }
+
+// ---------------------------------------------------------------------------
+// Division by a divisor known only at run time: the same quotient step after
+// computing R = ceil(2^115/md) on the integer pipes —
+//   R0: 24 bits from a binary32 reciprocal of md's top 24 bits (relative
+//       error < 2^-22.4: 2^-24 from the rounding, < 2^-23 from the truncation);
+//   R1, R2: two Newton-Raphson steps R + R*(2^115 - md*R)/2^115 in fixed
+//       point (errors 2^-44.7 relative, then below one unit plus the floors:
+//       ceil(2^115/md) - R2 is 0 or 1);
+//   exact correction: D = 2^115 - md*R2 (its magnitude < 2^55, so the low 64
+//       bits of md*R2 give it) decides R2 + 1.
+// Two upward and one downward correction steps are applied for margin.
+FM_SOFT_HD void umul128(uint64_t a, uint64_t b, uint64_t &hi, uint64_t &lo) {
+#if defined(__CUDA_ARCH__)
+  lo = a * b;
+  hi = __umul64hi(a, b);
+#else
+  const unsigned __int128 p = (unsigned __int128)a * b;
+  lo = (uint64_t)p;
+  hi = (uint64_t)(p >> 64);
+#endif
+}
+
+// floor(a * b / 2^64) for a signed a and an unsigned b (the result fits)
+FM_SOFT_HD int64_t smulhi(int64_t a, uint64_t b) {
+  uint64_t hi, lo;
+  umul128((uint64_t)a, b, hi, lo);
+  return (int64_t)(hi - (a < 0 ? b : 0ull));
+}
+
+// (2^115 - (p_hi:p_lo)) >> k as a signed 64-bit value, for 2^115 - p of
+// magnitude below 2^(63+k)
+FM_SOFT_HD int64_t resid115(uint64_t p_hi, uint64_t p_lo, int k) {
+  const uint64_t e_lo = 0ull - p_lo;
+  const uint64_t e_hi = (1ull << 51) - p_hi - (p_lo != 0ull ? 1ull : 0ull);
+  return (int64_t)((e_hi << (64 - k)) | (e_lo >> k));
+}
+
+FM_SOFT_HD uint64_t recip115(uint64_t md) {
+  const uint32_t top = (uint32_t)(md >> 29);  // [2^23, 2^24)
+  float f;
+  {
+    const uint32_t fb = 0x3f800000u | (top & 0x7fffffu);  // top * 2^-23, exactly
+    memcpy(&f, &fb, 4);
+  }
+#if defined(__CUDA_ARCH__)
+  const float rf = __frcp_rn(f);
+#else
+  const float rf = 1.0f / f;
+#endif
+  uint32_t rb;
+  memcpy(&rb, &rf, 4);
+  const uint32_t mr = (rb & 0x7fffffu) | 0x800000u;
+  const int s = 40 + (int)(rb >> 23) - 127;  // rf in (0.5, 1]: 39, or 40 for rf == 1
+  const uint64_t R0 = (uint64_t)mr << s;
+  uint64_t h, l;
+  umul128(md, mr, h, l);
+  const int64_t e0 = resid115((h << s) | (l >> (64 - s)), l << s, 51);
+  const uint64_t R1 = R0 + (uint64_t)smulhi(e0, R0);
+  umul128(md, R1, h, l);
+  const int64_t e1 = resid115(h, l, 20);
+  uint64_t R = R1 + (uint64_t)(smulhi(e1, R1) >> 31);
+  int64_t D = (int64_t)(0ull - md * R);
+  if (D > 0) {
+    ++R;
+    D -= (int64_t)md;
+  }
+  if (D > 0) {
+    ++R;
+    D -= (int64_t)md;
+  }
+  if (D <= -(int64_t)md) --R;
+  return R;
+}
+
+// A divisor prepared at run time (any value; non-normal ones take the slow
+// path in div_var_s).  Several divisions by one value share the reciprocal.
+struct DivVarS {
+  DivConstS c;
+  uint32_t sign;
+  bool normal;
+};
+
+FM_SOFT_HD DivVarS prep_div_s(double d) {
+  DivVarS v;
+  const uint32_t dh = hi_word(d), dl = lo_word(d);
+  const uint64_t md = ((uint64_t)((dh & 0x000fffffu) | 0x00100000u) << 32) | dl;
+  const uint64_t R = recip115(md);
+  v.c.r_hi = (uint32_t)(R >> 32);
+  v.c.r_lo = (uint32_t)R;
+  v.c.md_hi = (uint32_t)(md >> 32);
+  v.c.md_lo = (uint32_t)md;
+  v.c.ed = (int)((dh >> 20) & 0x7ffu);
+  v.c.d = d;
+  v.sign = dh & 0x80000000u;
+  v.normal = ((uint32_t)v.c.ed - 1u) < 2046u;
+  return v;
+}
+
+FM_SOFT_HD double div_var_s(double x, const DivVarS &v) {
+  return div_core(x, v.c, v.sign, v.normal);
+}
+
+FM_SOFT_HD double div_s(double x, double y) { return div_var_s(x, prep_div_s(y)); }
 
 // ---------------------------------------------------------------------------
 // Multiplication.  With x = mx*2^(ex-1075), y = my*2^(ey-1075): the exact
@@ -270,6 +381,77 @@ FM_SOFT_HD double mul_s(double x, double y) {
   if (zfin) r = from_words(sign, 0u);
   if (!(ok || zfin)) r = mul_slow(x, y);
   return r;
+}
+
+// ---------------------------------------------------------------------------
+// x * 2^k, exactly, for a small |k|: a normal x whose scaled exponent stays in
+// [1, 2046] only has its exponent field moved; zero is unchanged; results that
+// would be subnormal or overflow, subnormal x, Inf and NaN take the FP64
+// multiplication out of line.
+#if defined(__CUDA_ARCH__)
+static __device__ __noinline__ double scale_slow(double x, double f) { return __dmul_rn(x, f); }
+#elif defined(FM_SOFT_SLOW_SENTINEL)
+inline double scale_slow(double, double) { return sentinel(); }
+#else
+inline double scale_slow(double x, double f) { return x * f; }
+#endif
+
+FM_SOFT_HD double scale_pow2(double x, int k) {
+  const uint32_t xh = hi_word(x), xl = lo_word(x);
+  const int e = (int)((xh >> 20) & 0x7ffu);
+  double r = from_words(xh + ((uint32_t)k << 20), xl);
+  const bool zero = ((xh << 1) | xl) == 0u;
+  if (zero) r = x;
+  else if (e == 0 || e == 0x7ff || e + k < 1 || e + k > 2046)
+    r = scale_slow(x, k >= 0 ? (double)(1ull << k) : 1.0 / (double)(1ull << -k));
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// fmax, fmin and x <= 0 on the integer pipes.  For operands that are not NaN,
+// and not a +0/-0 pair (whose result the hardware instruction decides), the
+// order of binary64 values is the order of their bit patterns read as signed
+// 64-bit integers after the magnitude bits of negative values are inverted
+// (-0 below +0).  NaN operands and +0/-0 pairs take fmax/fmin out of line.
+#if defined(__CUDA_ARCH__)
+static __device__ __noinline__ double max_slow(double a, double b) { return fmax(a, b); }
+static __device__ __noinline__ double min_slow(double a, double b) { return fmin(a, b); }
+#elif defined(FM_SOFT_SLOW_SENTINEL)
+inline double max_slow(double, double) { return sentinel(); }
+inline double min_slow(double, double) { return sentinel(); }
+#else
+inline double max_slow(double a, double b) { return fmax(a, b); }
+inline double min_slow(double a, double b) { return fmin(a, b); }
+#endif
+
+FM_SOFT_HD uint64_t bits64(double x) { return ((uint64_t)hi_word(x) << 32) | lo_word(x); }
+FM_SOFT_HD int64_t order_key(uint64_t b) {
+  return (int64_t)(b ^ ((uint64_t)((int64_t)b >> 63) >> 1));
+}
+FM_SOFT_HD bool minmax_special(uint64_t a, uint64_t b) {
+  const bool nan = (a << 1) > 0xffe0000000000000ull || (b << 1) > 0xffe0000000000000ull;
+  const bool mixed_zeros = ((a | b) << 1) == 0ull && a != b;
+  return nan || mixed_zeros;
+}
+
+FM_SOFT_HD double max_s(double x, double y) {
+  const uint64_t a = bits64(x), b = bits64(y);
+  double r = order_key(a) >= order_key(b) ? x : y;
+  if (minmax_special(a, b)) r = max_slow(x, y);
+  return r;
+}
+
+FM_SOFT_HD double min_s(double x, double y) {
+  const uint64_t a = bits64(x), b = bits64(y);
+  double r = order_key(a) <= order_key(b) ? x : y;
+  if (minmax_special(a, b)) r = min_slow(x, y);
+  return r;
+}
+
+// x <= 0 (false for NaN)
+FM_SOFT_HD bool le_zero_s(double x) {
+  const uint64_t a = bits64(x);
+  return (a << 1) <= 0xffe0000000000000ull && ((a >> 63) != 0ull || (a << 1) == 0ull);
 }
 
 }  // namespace soft

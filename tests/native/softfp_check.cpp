@@ -19,6 +19,30 @@ void softfp_mul(const double *x, const double *y, long n, double *out) {
   for (long i = 0; i < n; ++i) out[i] = fm::soft::mul_s(x[i], y[i]);
 }
 
+void softfp_scale_pow2(const double *x, long n, int k, double *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::scale_pow2(x[i], k);
+}
+
+void softfp_div(const double *x, const double *y, long n, double *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::div_s(x[i], y[i]);
+}
+
+void softfp_recip115(const unsigned long long *md, long n, unsigned long long *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::recip115(md[i]);
+}
+
+void softfp_max(const double *x, const double *y, long n, double *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::max_s(x[i], y[i]);
+}
+
+void softfp_min(const double *x, const double *y, long n, double *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::min_s(x[i], y[i]);
+}
+
+void softfp_le_zero(const double *x, long n, unsigned char *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::le_zero_s(x[i]) ? 1 : 0;
+}
+
 void softfp_div_reciprocal_words(double d, unsigned *r_hi, unsigned *r_lo) {
   const fm::soft::DivConstS c = fm::soft::make_div_const_s(d);
   *r_hi = c.r_hi;

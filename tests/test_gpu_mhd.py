@@ -49,6 +49,21 @@ def test_mhd_f64_strong_perturbation_bit_exact(cuda_device):
         assert np.array_equal(g, w), name
 
 
+def test_mhd_f64_signed_zeros_bit_exact(cuda_device):
+    """Fields that are exactly +0 or -0 everywhere (vy = -0, Bz = +0, Psi = -0)
+    make the Kronecker-delta term -(0*Psi) + x and the products of zeros
+    produce signed zeros; compared bit for bit, the sign of zero included."""
+    n = 12
+    f0 = [np.array(f) for f in inits.mhd_3d(n, seed=7)]
+    f0[2] = np.full((n, n, n), -0.0)
+    f0[6] = np.zeros((n, n, n))
+    f0[8] = np.full((n, n, n), -0.0)
+    _, got = gpu_run(f0, 2, torch.float64)
+    want = oracle.mhd_f64(f0, 2)
+    for name, g, w in zip(inits.MHD_FIELDS, got, want):
+        assert np.array_equal(g.view(np.int64), np.ascontiguousarray(w).view(np.int64)), name
+
+
 def test_mhd_f32_error_against_f64(cuda_device):
     n, steps = 32, 40
     f0 = inits.mhd_3d(n, seed=5)
@@ -82,25 +97,28 @@ def test_mhd_totals_conserve_mass(cuda_device):
 @pytest.mark.parametrize("n", [12, 40])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
 def test_mhd_kernel_variants_agree(cuda_device, n, dtype):
-    """The shared-memory stage kernel (mhd.stage = 1, default) and the
-    per-point one (0), the x-marching finish kernel sharing slopes and faces of
-    all fields per plane (mhd.finish = 2; several x chunks) and the per-point
-    one (0)
-    evaluate the same expressions: identical bits, also for sizes that are not
-    multiples of the 32 x 8 tile."""
+    """The stage kernels (mhd.stage: 2 x-marching with a register ring, 1
+    shared-memory tiled, 0 per-point), the finish kernels (mhd.finish: 2
+    x-marching sharing slopes and faces of all fields per plane, several x
+    chunks; 0 per-point) and, for FP64, the integer-pipe arithmetic
+    (mhd.soft = 1, 2) against the FP64 instructions (0) evaluate the same
+    expressions: identical bits, also for sizes that are not multiples of the
+    32 x 8 tile."""
     from formura_gb300 import _lib
 
     f0 = inits.mhd_3d(n, seed=11, amp=0.05)
     outs = []
     L = _lib.lib()
     try:
-        for kern, fin, xc in ((0, 0, 0), (1, 2, 0), (1, 2, 5), (1, 2, 3), (0, 2, 1), (2, 0, 16),
-                              (2, 0, 5), (2, 2, 1)):
+        for kern, fin, xc, soft in ((0, 0, 0, 0), (1, 2, 0, 1), (1, 2, 5, 0), (1, 2, 3, 1),
+                                    (0, 2, 1, 1), (2, 0, 16, 1), (2, 0, 5, 0), (2, 2, 1, 1),
+                                    (2, 2, 16, 0), (2, 2, 16, 2), (1, 0, 0, 2), (0, 2, 4, 2)):
             L.fm_tune_clear()
             L.fm_tune_set(b"mhd.stage", kern)
             L.fm_tune_set(b"mhd.finish", fin)
             L.fm_tune_set(b"mhd.xchunk", xc)
             L.fm_tune_set(b"mhd.stage_xchunk", xc if xc else 16)
+            L.fm_tune_set(b"mhd.soft", soft)
             t = [torch.from_numpy(x).to(dtype).to(cuda_device) for x in f0]
             kernels.mhd_forward(t, torch.empty(18 * n ** 3, dtype=dtype, device=cuda_device), 3)
             outs.append([x.cpu().numpy() for x in t])

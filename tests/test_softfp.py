@@ -28,6 +28,15 @@ def _build(tmp_path_factory, name, defines=()):
     L.softfp_div_const.argtypes = [dp, ctypes.c_long, ctypes.c_double, dp]
     L.softfp_mul_const.argtypes = [dp, ctypes.c_long, ctypes.c_double, dp]
     L.softfp_mul.argtypes = [dp, dp, ctypes.c_long, dp]
+    L.softfp_scale_pow2.argtypes = [dp, ctypes.c_long, ctypes.c_int, dp]
+    L.softfp_div.argtypes = [dp, dp, ctypes.c_long, dp]
+    L.softfp_max.argtypes = [dp, dp, ctypes.c_long, dp]
+    L.softfp_min.argtypes = [dp, dp, ctypes.c_long, dp]
+    L.softfp_le_zero.argtypes = [dp, ctypes.c_long, ctypes.POINTER(ctypes.c_ubyte)]
+    up = ctypes.POINTER(ctypes.c_ulonglong)
+    L.softfp_recip115.argtypes = [up, ctypes.c_long, up]
+    L.softfp_div_reciprocal_words.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_uint),
+                                              ctypes.POINTER(ctypes.c_uint)]
     return L
 
 
@@ -141,3 +150,108 @@ def test_mul_matches_ieee(lib):
     ok, bad = same_bits(got, want, normal(xs) & normal(ys))
     assert ok, (xs[bad[:5]], ys[bad[:5]], got[bad[:5]], want[bad[:5]])
 
+
+@pytest.mark.parametrize("k", [-1, 1, 3, -4])
+def test_scale_pow2_matches_ieee(lib, k):
+    rng = np.random.default_rng(k + 10)
+    x = np.concatenate([random_doubles(rng, 200_000), random_doubles(rng, 50_000, -1022, 1023),
+                        SPECIALS, np.ldexp(1.0, np.arange(-1074, 1024))])
+    with np.errstate(all="ignore"):
+        want = x * (2.0 ** k)
+    got = np.empty_like(x)
+    lib.softfp_scale_pow2(_p(x), x.size, k, _p(got))
+    ok, bad = same_bits(got, want, normal(x))
+    assert ok, (k, x[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+def _ceil_recip115(md):
+    """ceil(2^115 / md) in Python integers."""
+    return [-((-(1 << 115)) // int(m)) for m in md]
+
+
+def test_recip115_is_exact(lib):
+    """The run-time reciprocal (binary32 seed, two fixed-point Newton steps,
+    exact correction) equals ceil(2^115/md) for every significand tried: random
+    ones, both ends of the binade, and the neighbourhoods of powers of two and
+    of the points where the binary32 seed changes."""
+    rng = np.random.default_rng(115)
+    lo, hi = 1 << 52, 1 << 53
+    md = [int(v) for v in rng.integers(lo, hi, 200_000, dtype=np.uint64)]
+    md += list(range(lo, lo + 2000)) + list(range(hi - 2000, hi))
+    for t in rng.integers(1 << 23, 1 << 24, 300):       # seed boundaries: top 24 bits change
+        base = int(t) << 29
+        md += [base - 1, base, base + 1, base + (1 << 28), base + (1 << 29) - 1]
+    for k in range(1, 53):                               # 2^52 (1 + 2^-k) and neighbours
+        m = lo + (lo >> k)
+        md += [m - 1, m, m + 1]
+    md = [m for m in md if lo <= m < hi]
+    a = np.array(md, dtype=np.uint64)
+    out = np.empty_like(a)
+    lib.softfp_recip115(a.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), a.size,
+                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)))
+    want = np.array(_ceil_recip115(md), dtype=np.uint64)
+    bad = np.flatnonzero(out != want)
+    assert bad.size == 0, (a[bad[:5]], out[bad[:5]], want[bad[:5]])
+    # the host-prepared constant (long division) gives the same words
+    for d in (0.01, 3.0, 1.0, 0.7, 12.0 / 256):
+        rh, rl = ctypes.c_uint(), ctypes.c_uint()
+        lib.softfp_div_reciprocal_words(d, ctypes.byref(rh), ctypes.byref(rl))
+        m = (int(np.float64(d).view(np.uint64)) & ((1 << 52) - 1)) | (1 << 52)
+        assert (rh.value << 32) | rl.value == _ceil_recip115([m])[0]
+
+
+def test_div_matches_ieee(lib):
+    """x / y with both operands varying: random operands over wide and full
+    exponent ranges, both signs, quotients at binade boundaries (x = y * 2^k
+    and neighbours), and every pair of the special values."""
+    rng = np.random.default_rng(23)
+    n = 600_000
+    x = random_doubles(rng, n)
+    y = random_doubles(rng, n)
+    k = 100_000
+    t = y[:k] * 2.0 ** rng.integers(-10, 10, k)
+    step = rng.integers(-1, 2, k)
+    x[:k] = np.where(step > 0, np.nextafter(t, np.inf), np.where(step < 0, np.nextafter(t, -np.inf), t))
+    xs = np.concatenate([x, random_doubles(rng, 100_000, -1022, 1023),
+                         np.repeat(SPECIALS, SPECIALS.size)])
+    ys = np.concatenate([y, random_doubles(rng, 100_000, -1022, 1023),
+                         np.tile(SPECIALS, SPECIALS.size)])
+    with np.errstate(all="ignore"):
+        want = xs / ys
+    got = np.empty_like(xs)
+    lib.softfp_div(_p(xs), _p(ys), xs.size, _p(got))
+    ok, bad = same_bits(got, want, normal(xs) & normal(ys) & (ys != 0))
+    assert ok, (xs[bad[:5]], ys[bad[:5]], got[bad[:5]], want[bad[:5]])
+
+
+@pytest.mark.parametrize("op", ["max", "min"])
+def test_minmax_matches_fmax_fmin(lib, op):
+    """fmax/fmin on the integer pipes: random pairs, pairs that are equal or
+    adjacent, and every pair of the special values; the fast path must take
+    every pair except NaNs and +0/-0 pairs."""
+    rng = np.random.default_rng(31)
+    n = 300_000
+    x = random_doubles(rng, n, -1022, 1023)
+    y = random_doubles(rng, n, -1022, 1023)
+    y[:50_000] = x[:50_000]
+    y[50_000:100_000] = np.nextafter(x[50_000:100_000], np.where(rng.random(50_000) < 0.5, np.inf, -np.inf))
+    y[100_000:150_000] = -x[100_000:150_000]
+    xs = np.concatenate([x, np.repeat(SPECIALS, SPECIALS.size)])
+    ys = np.concatenate([y, np.tile(SPECIALS, SPECIALS.size)])
+    want = np.fmax(xs, ys) if op == "max" else np.fmin(xs, ys)
+    got = np.empty_like(xs)
+    getattr(lib, "softfp_" + op)(_p(xs), _p(ys), xs.size, _p(got))
+    special = np.isnan(xs) | np.isnan(ys) | ((xs == 0) & (ys == 0) & (np.signbit(xs) != np.signbit(ys)))
+    g64, w64 = got.view(np.uint64), want.view(np.uint64)
+    fast_ok = (g64 == w64) | (np.isnan(got) & np.isnan(want) & (g64 != SENTINEL))
+    assert np.all(fast_ok[~special])
+    assert np.all(fast_ok[special] | (g64[special] == SENTINEL))
+
+
+def test_le_zero_matches_ieee(lib):
+    rng = np.random.default_rng(37)
+    x = np.concatenate([random_doubles(rng, 100_000, -1022, 1023), SPECIALS, -SPECIALS])
+    got = np.empty(x.size, dtype=np.uint8)
+    lib.softfp_le_zero(_p(x), x.size, got.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
+    with np.errstate(invalid="ignore"):
+        assert np.array_equal(got.astype(bool), x <= 0)
