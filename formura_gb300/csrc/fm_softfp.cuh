@@ -448,6 +448,24 @@ FM_SOFT_HD double min_s(double x, double y) {
   return r;
 }
 
+// IEEE comparisons on the same keys: unordered (a NaN operand) is false for
+// <, <=, == and true for !=; +0 and -0 compare equal.  No slow path.
+FM_SOFT_HD bool unordered_s(uint64_t a, uint64_t b) {
+  return (a << 1) > 0xffe0000000000000ull || (b << 1) > 0xffe0000000000000ull;
+}
+FM_SOFT_HD bool lt_s(double x, double y) {
+  const uint64_t a = bits64(x), b = bits64(y);
+  return !unordered_s(a, b) && ((a | b) << 1) != 0ull && order_key(a) < order_key(b);
+}
+FM_SOFT_HD bool le_s(double x, double y) {
+  const uint64_t a = bits64(x), b = bits64(y);
+  return !unordered_s(a, b) && (((a | b) << 1) == 0ull || order_key(a) <= order_key(b));
+}
+FM_SOFT_HD bool eq_s(double x, double y) {
+  const uint64_t a = bits64(x), b = bits64(y);
+  return !unordered_s(a, b) && (a == b || ((a | b) << 1) == 0ull);
+}
+
 // x <= 0 (false for NaN)
 FM_SOFT_HD bool le_zero_s(double x) {
   const uint64_t a = bits64(x);

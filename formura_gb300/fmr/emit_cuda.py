@@ -12,11 +12,16 @@ Arithmetic keeps the C semantics of the reference's generated code
 the node's C type, ``**`` -> ``pow``, ``>?``/``<?`` -> right-folded
 ``fmax``/``fmin`` chains, ``<%`` -> ``fmin(0, fmax(..)) + fmax(0, fmin(..))``,
 ``if`` -> ``?:``, extern functions called on doubles.  The file is compiled
-with ``--fmad=false``, so no multiply-add is contracted.  Two exact
-substitutions are made (bit-identical results, see csrc/fm_softfp.cuh):
-a division by a positive normal constant runs as ``fm::soft::div_const_s``
-and a multiplication of a double by a nonzero normal double constant as
-``fm::soft::mul_const_s``, both on the integer pipes.
+with ``--fmad=false``, so no multiply-add is contracted.  Exact
+substitutions of binary64 operations by integer-pipe forms (bit-identical
+results, csrc/fm_softfp.cuh), because the FP64 pipe is the scarce one:
+  * x * 2^k and x / 2^k (a power-of-two constant): ``scale_pow2``;
+  * x / d for another positive normal constant: ``div_const_s``;
+  * x * y for another nonzero normal constant: ``mul_const_s``;
+  * x / y for a run-time y: ``div_var_s``, one ``prep_div_s`` reciprocal
+    per divisor node shared by all its quotients;
+  * ``fmax``/``fmin`` chains (``>?``, ``<?``, ``<%``) and ``< <= > >= == !=``
+    of two doubles: ``max_s``/``min_s`` and the ordered-key comparisons.
 """
 from __future__ import annotations
 
@@ -58,6 +63,21 @@ def _normal_double(v) -> bool:
     return math.isfinite(a) and a >= 2.2250738585072014e-308
 
 
+def _pow2_exponent(v):
+    """k if v == 2**k for an integer |k| <= 62, else None."""
+    if not isinstance(v, float) or not math.isfinite(v) or v <= 0:
+        return None
+    m, e = math.frexp(v)
+    if m != 0.5 or abs(e - 1) > 62:
+        return None
+    return e - 1
+
+
+CMP_SOFT = {"<": "fm::soft::lt_s(a%d, a%d)", "<=": "fm::soft::le_s(a%d, a%d)",
+            ">": "fm::soft::lt_s(a%d, a%d)", ">=": "fm::soft::le_s(a%d, a%d)",
+            "==": "fm::soft::eq_s(a%d, a%d)", "!=": "!fm::soft::eq_s(a%d, a%d)"}
+
+
 def _wrap_name(ax: int, c: int) -> str:
     if c == 0:
         return AXVARS[ax]
@@ -66,9 +86,9 @@ def _wrap_name(ax: int, c: int) -> str:
 
 class LevelEmitter:
     def __init__(self, mmp: MM.MMProgram, level: MM.Level, li: int, soft_div: bool,
-                 soft_mul: bool):
+                 soft_mul: bool, soft_cmp: bool = True):
         self.mmp, self.level, self.li = mmp, level, li
-        self.soft_div, self.soft_mul = soft_div, soft_mul
+        self.soft_div, self.soft_mul, self.soft_cmp = soft_div, soft_mul, soft_cmp
         self.shape = mmp.shape
         self.dim = mmp.dim
 
@@ -124,6 +144,7 @@ class LevelEmitter:
             else:
                 w("    const int %s = ((%s + %d) %% %d + %d) %% %d;" % (v, AXVARS[a], c, n, n, n))
         const_vals: Dict[int, object] = {}
+        prepared = set()  # divisor nodes whose reciprocal is prepared
         for i, m in enumerate(L.micro):
             t = m.ctype
             name = "a%d" % i
@@ -148,18 +169,38 @@ class LevelEmitter:
             elif k == "bin":
                 op, a, b = m.args
                 ta, tb = L.micro[a].ctype, L.micro[b].ctype
+                dd = t == "double" and ta == "double" and tb == "double"
                 if op == "**":
                     w("    const %s %s = pow((double)a%d, (double)a%d);" % (t, name, a, b))
-                elif (op == "/" and self.soft_div and t == "double" and ta == "double" and
-                      b in const_vals and _normal_double(const_vals[b]) and const_vals[b] > 0):
+                elif (op == "/" and self.soft_div and dd and b in const_vals and
+                      _pow2_exponent(const_vals[b]) is not None):
+                    w("    const %s %s = fm::soft::scale_pow2(a%d, %d);" %
+                      (t, name, a, -_pow2_exponent(const_vals[b])))
+                elif (op == "/" and self.soft_div and dd and b in const_vals and
+                      _normal_double(const_vals[b]) and const_vals[b] > 0):
                     w("    const %s %s = fm::soft::div_const_s(a%d, fm::soft::DivConstS%s);" %
                       (t, name, a, div_const_fields(const_vals[b])))
+                elif op == "/" and self.soft_div and dd and b not in const_vals:
+                    if b not in prepared:
+                        prepared.add(b)
+                        w("    const fm::soft::DivVarS dv%d = fm::soft::prep_div_s(a%d);" % (b, b))
+                    w("    const %s %s = fm::soft::div_var_s(a%d, dv%d);" % (t, name, a, b))
+                elif (op == "*" and self.soft_mul and dd and
+                      (b in const_vals or a in const_vals) and
+                      _pow2_exponent(const_vals[b] if b in const_vals else const_vals[a])
+                      is not None):
+                    x, c = (a, b) if b in const_vals else (b, a)
+                    w("    const %s %s = fm::soft::scale_pow2(a%d, %d);" %
+                      (t, name, x, _pow2_exponent(const_vals[c])))
                 elif (op == "*" and self.soft_mul and t == "double" and
                       ((b in const_vals and ta == "double" and _normal_double(const_vals[b])) or
                        (a in const_vals and tb == "double" and _normal_double(const_vals[a])))):
                     x, c = (a, b) if b in const_vals else (b, a)
                     w("    const %s %s = fm::soft::mul_const_s(a%d, fm::soft::MulConstS%s);" %
                       (t, name, x, mul_const_fields(const_vals[c])))
+                elif (op in CMP_SOFT and self.soft_cmp and ta == "double" and tb == "double"):
+                    x, y = (b, a) if op in (">", ">=") else (a, b)
+                    w("    const %s %s = %s;" % (t, name, CMP_SOFT[op] % (x, y)))
                 else:
                     w("    const %s %s = (a%d %s a%d);" % (t, name, a, op, b))
             elif k == "ite":
@@ -175,12 +216,16 @@ class LevelEmitter:
                         acc = "%s(%s, %s)" % (fn, it, acc)
                     return acc
 
+                soft = self.soft_cmp and t == "double" and all(
+                    L.micro[x].ctype == "double" for x in xs)
+                fmax_, fmin_ = ("fm::soft::max_s", "fm::soft::min_s") if soft else ("fmax", "fmin")
                 if op == ">?":
-                    e = chain("fmax", names)
+                    e = chain(fmax_, names)
                 elif op == "<?":
-                    e = chain("fmin", names)
+                    e = chain(fmin_, names)
                 else:
-                    e = "fmin(0.0, %s) + fmax(0.0, %s)" % (chain("fmax", names), chain("fmin", names))
+                    e = "%s(0.0, %s) + %s(0.0, %s)" % (fmin_, chain(fmax_, names), fmax_,
+                                                       chain(fmin_, names))
                 w("    const %s %s = %s;" % (t, name, e))
             else:
                 raise MM.OM.FmrSemanticError("cannot emit %s" % k)
@@ -195,13 +240,14 @@ class LevelEmitter:
         return "\n".join(src), state_names, arr_ids, L.arrays
 
 
-def emit_kernels(mmp: MM.MMProgram, soft_div: bool = True, soft_mul: bool = True):
+def emit_kernels(mmp: MM.MMProgram, soft_div: bool = True, soft_mul: bool = True,
+                 soft_cmp: bool = True):
     """Kernel source and, per level, (kernel name, state names read, arrays
     read, arrays written)."""
     parts = []
     levels = []
     for li, L in enumerate(mmp.levels):
-        src, sn, ar, aw = LevelEmitter(mmp, L, li, soft_div, soft_mul).emit()
+        src, sn, ar, aw = LevelEmitter(mmp, L, li, soft_div, soft_mul, soft_cmp).emit()
         parts.append(src)
         levels.append(("fmr_level_%d" % li, sn, ar, aw))
     return "\n".join(parts), levels

@@ -43,6 +43,13 @@ void softfp_le_zero(const double *x, long n, unsigned char *out) {
   for (long i = 0; i < n; ++i) out[i] = fm::soft::le_zero_s(x[i]) ? 1 : 0;
 }
 
+void softfp_cmp(const double *x, const double *y, long n, unsigned char *out) {
+  // bit 0: <, bit 1: <=, bit 2: ==
+  for (long i = 0; i < n; ++i)
+    out[i] = (fm::soft::lt_s(x[i], y[i]) ? 1 : 0) | (fm::soft::le_s(x[i], y[i]) ? 2 : 0) |
+             (fm::soft::eq_s(x[i], y[i]) ? 4 : 0);
+}
+
 void softfp_div_reciprocal_words(double d, unsigned *r_hi, unsigned *r_lo) {
   const fm::soft::DivConstS c = fm::soft::make_div_const_s(d);
   *r_hi = c.r_hi;

@@ -189,6 +189,28 @@ def test_generated_program_compiles(tmp_path):
         assert (" %s\n" % name) in syms, name
 
 
+@pytest.mark.skipif(shutil.which("nvcc") is None and not Path("/usr/local/cuda/bin/nvcc").exists(),
+                    reason="nvcc not available")
+def test_generated_integer_pipe_forms_compile(tmp_path):
+    """fmr-limiter.fmr has run-time divisions (one divisor shared by two
+    quotients), comparisons of doubles, power-of-two scalings and fmax/fmin
+    chains: each is emitted in its integer-pipe form and the file compiles."""
+    from formura_gb300.fmr.emit_cuda import emit_kernels
+
+    p = load_program(EX / "fmr-limiter.fmr")
+    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)))
+    for form in ("prep_div_s", "div_var_s", "scale_pow2", "max_s", "min_s", "lt_s", "le_s",
+                 "eq_s", "mul_const_s"):
+        assert "fm::soft::" + form in kern, form
+    # the divisor 1 + a*a is prepared once for its two quotients (w and g)
+    import collections
+    import re
+    uses = collections.Counter(re.findall(r"div_var_s\(a\d+, (dv\d+)\)", kern))
+    assert max(uses.values()) == 2 and kern.count("prep_div_s(") == len(uses)
+    assert "fmax(" not in kern and "fmin(" not in kern and " / " not in kern
+    backend.build_program(p, outdir=tmp_path)
+
+
 CURRENT_SYNTAX_EXAMPLES = [
     "2d-mhd-dc.fmr", "2d-mhd.fmr", "3d-localsun.fmr", "3d-mhd-lessM.fmr", "3d-mhd-rk4.fmr",
     "3d-mhd.fmr", "av-mhd.fmr", "champion.fmr", "diffusion.fmr", "finalist.fmr",

@@ -37,6 +37,8 @@ def _random_state(prog, rng):
     ("fmr-1d-float.fmr", dict(intra_node_shape=[7], monitor_interval=5)),
     ("fmr-3d-advection.fmr", {}),
     ("fmr-3d-advection.fmr", dict(intra_node_shape=[5, 3, 33], monitor_interval=4)),
+    ("fmr-limiter.fmr", {}),
+    ("fmr-limiter.fmr", dict(intra_node_shape=[9, 17], monitor_interval=6)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)

@@ -33,6 +33,7 @@ def _build(tmp_path_factory, name, defines=()):
     L.softfp_max.argtypes = [dp, dp, ctypes.c_long, dp]
     L.softfp_min.argtypes = [dp, dp, ctypes.c_long, dp]
     L.softfp_le_zero.argtypes = [dp, ctypes.c_long, ctypes.POINTER(ctypes.c_ubyte)]
+    L.softfp_cmp.argtypes = [dp, dp, ctypes.c_long, ctypes.POINTER(ctypes.c_ubyte)]
     up = ctypes.POINTER(ctypes.c_ulonglong)
     L.softfp_recip115.argtypes = [up, ctypes.c_long, up]
     L.softfp_div_reciprocal_words.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_uint),
@@ -255,3 +256,21 @@ def test_le_zero_matches_ieee(lib):
     lib.softfp_le_zero(_p(x), x.size, got.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
     with np.errstate(invalid="ignore"):
         assert np.array_equal(got.astype(bool), x <= 0)
+
+
+def test_comparisons_match_ieee(lib):
+    rng = np.random.default_rng(41)
+    n = 200_000
+    x = random_doubles(rng, n, -1022, 1023)
+    y = random_doubles(rng, n, -1022, 1023)
+    y[:40_000] = x[:40_000]
+    y[40_000:80_000] = np.nextafter(x[40_000:80_000], np.inf)
+    y[80_000:120_000] = -x[80_000:120_000]
+    xs = np.concatenate([x, np.repeat(SPECIALS, SPECIALS.size), np.repeat(-SPECIALS, SPECIALS.size)])
+    ys = np.concatenate([y, np.tile(SPECIALS, SPECIALS.size), np.tile(SPECIALS, SPECIALS.size)])
+    got = np.empty(xs.size, dtype=np.uint8)
+    lib.softfp_cmp(_p(xs), _p(ys), xs.size, got.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
+    with np.errstate(invalid="ignore"):
+        assert np.array_equal((got & 1) != 0, xs < ys)
+        assert np.array_equal((got & 2) != 0, xs <= ys)
+        assert np.array_equal((got & 4) != 0, xs == ys)
