@@ -45,6 +45,12 @@
 #include "fm_softfp.cuh"
 #include "fm_tune.h"
 
+// CTAs per SM the full-row kernel is compiled for at RY = 2: 3 (80 registers);
+// 4 (64 registers, 56 bytes of spills) measured 18.7 against 19.5 GLUP/s
+#ifndef FM_GS64_ROW_MINB
+#define FM_GS64_ROW_MINB 3
+#endif
+
 namespace {
 
 struct Gs64 {
@@ -114,7 +120,7 @@ __device__ __forceinline__ void gs_cell(double u, double v, double fxu_m, double
 // default with DIV = 3, 19.3 GLUP/s at 256^3 against 18.1 for RY = 4); the CTA covers a full periodic z row, so no flux is computed
 // twice along z.  Tiles: (ny/RY) y blocks x ceil(nx/xchunk) x chunks.
 template <int DIV, int MUL, int RY>
-__global__ void __launch_bounds__(256, RY >= 4 ? 2 : 3)
+__global__ void __launch_bounds__(256, RY >= 4 ? 2 : FM_GS64_ROW_MINB)
     gs3d_f64_row(const double *__restrict__ U, const double *__restrict__ V,
                  double *__restrict__ Un, double *__restrict__ Vn, int nx, int ny, int nz,
                  int xchunk, int ntiles, Gs64 c) {
