@@ -37,13 +37,30 @@ typedef __nv_bfloat16 bf16;
 constexpr int CIN = 64;
 constexpr int kTM = 128;
 
+// erf(z) by Abramowitz & Stegun, Handbook of Mathematical Functions, 7.1.26
+// (|error| <= 1.5e-7, far below the bf16 rounding of the activations): one
+// reciprocal, a degree-5 polynomial and one exponential, without the range
+// branches of a full-precision erff.  `e` returns exp(-z^2), which the GELU
+// derivative reuses.
+__device__ __forceinline__ float erf_as(float z, float &e) {
+  const float az = fabsf(z);
+  const float t = __fdividef(1.0f, fmaf(0.3275911f, az, 1.0f));
+  const float poly =
+      t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 1.061405429f, -1.453152027f), 1.421413741f),
+                       -0.284496736f),
+               0.254829592f);
+  e = __expf(-az * az);
+  return copysignf(fmaf(-poly, e, 1.0f), z);
+}
+// GELU(x) = x * Phi(x) = 0.5 x (1 + erf(x / sqrt 2)); GELU'(x) = Phi(x) + x phi(x)
 __device__ __forceinline__ float gelu(float x) {
-  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+  float e;
+  return 0.5f * x * (1.0f + erf_as(x * 0.70710678118654752f, e));
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
-  return cdf + x * pdf;
+  float e;  // exp(-x^2 / 2)
+  const float cdf = 0.5f * (1.0f + erf_as(x * 0.70710678118654752f, e));
+  return cdf + x * (0.39894228040143268f * e);
 }
 
 struct ConvArgs {
@@ -217,8 +234,11 @@ __global__ void __launch_bounds__(128) conv3x3_fwd(ConvArgs a) {
 //   * regions are double-buffered with cp.async (prefetch of tile i+1 while the
 //     tensor core works on tile i);
 //   * two TMEM accumulators (2 x 64 columns): the epilogue of tile i-1 runs
-//     while the MMAs of tile i are in flight.
-constexpr int kResThreads = 128;
+//     while the MMAs of tile i are in flight;
+//   * eight warps: warp w reads TMEM lanes 32*(w%4).. (its 32 positions) and
+//     columns 32*(w/4).. (its 32 channels), so the epilogue, which bounds the
+//     kernel, is spread over twice the warps of the four TMEM lane quarters.
+constexpr int kResThreads = 256;
 
 __host__ __device__ __forceinline__ int res_region_len(int Wp) { return kTM + 2 * (Wp + 1); }
 
@@ -229,9 +249,16 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
   extern __shared__ __align__(1024) uint8_t dsm[];
   uint8_t *sw = dsm;                          // weights
   uint8_t *sreg = dsm + kWBytes;              // 2 region buffers of 8*plane bytes
+  // 3 buffers of a tile's residual input (when there is one), 128 positions x
+  // 8 chunks of 16 B, chunk q of position p at slot p*8 + (q ^ (p & 7))
+  // (conflict-free 16-byte reads); tile t uses buffer t % 3
+  uint8_t *sres = sreg + 2 * 8 * (size_t)plane;
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t s_tmem;
+  __shared__ float s_bias[NT];
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lane quarter, channel half
+  if (tid < NT) s_bias[tid] = a.bias ? a.bias[tid] : 0.0f;
   const int H = a.H, W = a.W, Wp = W + 2;
   const int rlen = res_region_len(Wp);
   const long long img = (long long)(H + 2) * Wp;  // positions per padded image
@@ -269,11 +296,29 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
     }
     cp_async_commit();
   };
+  // the residual rows of tile `it` (its own cp.async group); issued after the
+  // barrier of an iteration, so its buffer's previous reader (the epilogue of
+  // tile it-3, two iterations earlier) has finished
+  auto stage_res = [&](int it) {
+    const int tile = blockIdx.x + it * gridDim.x;
+    const int b = tile / ntile_img, tl = tile % ntile_img;
+    const long long j0 = (long long)(Wp + 1) + (long long)tl * kTM;
+    const bf16 *rbase = a.resid + (size_t)b * img * NT;
+    uint8_t *rdst = sres + (size_t)(it % 3) * kTM * NT * 2;
+    for (int v = tid; v < kTM * 8; v += kResThreads) {
+      const int pos = v >> 3, q = v & 7;
+      const long long j = j0 + pos;
+      const bool ok = j < img;
+      cp_async16(rdst + (pos * 8 + (q ^ (pos & 7))) * 16, rbase + (size_t)(ok ? j : 0) * NT + q * 8,
+                 ok);
+    }
+    cp_async_commit();
+  };
 
   auto epilogue = [&](int it, int acc) {
     const int tile = blockIdx.x + it * gridDim.x;
     const int b = tile / ntile_img, tl = tile % ntile_img;
-    const long long j = (long long)(Wp + 1) + (long long)tl * kTM + warp * 32 + (tid & 31);
+    const long long j = (long long)(Wp + 1) + (long long)tl * kTM + quarter * 32 + (tid & 31);
     const int py = (int)(j / Wp), px = (int)(j % Wp);
     const bool interior = py >= 1 && py <= H && px >= 1 && px <= W;
     const int y = py - 1, xx = px - 1;
@@ -283,22 +328,37 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
     if (xx == 0) pxs[1] = W + 1;
     if (xx == W - 1) pxs[1] = 0;
     const size_t pin = (size_t)b * img + (size_t)j;
+    // this thread's 32 channels of the gate and residual inputs (64 B each), loaded
+    // as 16-byte vectors before the accumulator is read so that their latency overlaps
+    uint4 gv[4], rv[4];
+    if (interior && a.gate) {
+      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * (NT / 2));
 #pragma unroll
-    for (int c0 = 0; c0 < NT; c0 += 16) {
+      for (int q = 0; q < 4; ++q) gv[q] = __ldg(g4 + q);
+    }
+    if (interior && a.resid) {  // staged with the region
+      const int p = quarter * 32 + (tid & 31);
+      const uint4 *r4 = reinterpret_cast<const uint4 *>(sres + (size_t)(it % 3) * kTM * NT * 2);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) rv[q] = r4[p * 8 + ((chalf * 4 + q) ^ (p & 7))];
+    }
+#pragma unroll
+    for (int cc = 0; cc < NT / 2; cc += 16) {
+      const int c0 = chalf * (NT / 2) + cc;
       float v[16];
-      tmem_ld16(tmem + (uint32_t)(acc * 64) + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      tmem_ld16(tmem + (uint32_t)(acc * 64) + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
       if (!interior) continue;
       if (a.bias) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] += __ldg(a.bias + c0 + i);
+        for (int i = 0; i < 16; ++i) v[i] += s_bias[c0 + i];
       }
       if (a.gate) {
-        const bf16 *g = a.gate + pin * NT + c0;
+        const bf16 *g = reinterpret_cast<const bf16 *>(&gv[cc / 8]);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] *= gelu_grad(__bfloat162float(g[i]));
       }
       if (a.resid) {
-        const bf16 *rr = a.resid + pin * NT + c0;
+        const bf16 *rr = reinterpret_cast<const bf16 *>(&rv[cc / 8]);
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] += __bfloat162float(rr[i]);
       }
@@ -341,7 +401,10 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
   const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / gridDim.x + 1 : 0;
   uint32_t ph[2] = {0u, 0u};
   bool ok = true;
-  if (my_tiles > 0) stage(0, 0);
+  if (my_tiles > 0) {
+    stage(0, 0);
+    if (a.resid) stage_res(0);
+  }
   for (int it = 0; it < my_tiles; ++it) {
     const int buf = it & 1;
     if (it >= 1) {
@@ -377,6 +440,7 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
       }
       mma_commit(&bar[buf]);
     }
+    if (a.resid && it + 1 < my_tiles) stage_res(it + 1);
     if (it >= 1 && ok) epilogue(it - 1, buf ^ 1);
   }
   if (my_tiles > 0) {
@@ -558,7 +622,8 @@ int launch_fwd_res(const ConvArgs &a, cudaStream_t s) {
   const int Wp = a.W + 2;
   const int rlen = res_region_len(Wp);
   const int plane = ((rlen * 16 + 127) / 128) * 128;
-  const size_t smem = (size_t)9 * 64 * CIN * 2 + 2 * 8 * (size_t)plane;
+  const size_t smem = (size_t)9 * 64 * CIN * 2 + 2 * 8 * (size_t)plane +
+                      (a.resid ? 3 * (size_t)kTM * 64 * 2 : 0);
   int dev = 0, optin = 0;
   FM_TRY_CUDA(cudaGetDevice(&dev));
   FM_TRY_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
