@@ -73,6 +73,9 @@ class Program:
     mpi_grid_shape: Optional[Sequence[int]] = None
     axes: Optional[Sequence[str]] = None
     fmr_source: Optional[str] = None  # form "fmr": the program text
+    # form "fmr": cells per thread along axis 0 in the generated kernels (values shared by
+    # consecutive cells carried in registers); 0 = automatic (up to 16, keeping ~150k threads)
+    march_chunk: int = 0
 
     @property
     def dim(self) -> int:
@@ -273,7 +276,7 @@ def _fmr_parts(p: Program):
     from .fmr.emit_cuda import emit_kernels
 
     mmp = p.compiled()
-    kern, levels = emit_kernels(mmp)
+    kern, levels = emit_kernels(mmp, march_chunk=p.march_chunk)
     states = [n for n, _ in mmp.state]
     sidx = {n: i for i, n in enumerate(states)}
     arrays = sorted(mmp.arrays.values(), key=lambda a: a.node)

@@ -27,7 +27,7 @@ from __future__ import annotations
 
 import math
 import struct
-from typing import Dict, List, Sequence, Tuple
+from typing import Dict, List, Optional, Sequence, Tuple
 
 from . import mm as MM
 
@@ -86,9 +86,10 @@ def _wrap_name(ax: int, c: int) -> str:
 
 class LevelEmitter:
     def __init__(self, mmp: MM.MMProgram, level: MM.Level, li: int, soft_div: bool,
-                 soft_mul: bool, soft_cmp: bool = True):
+                 soft_mul: bool, soft_cmp: bool = True, march_chunk: int = 0):
         self.mmp, self.level, self.li = mmp, level, li
         self.soft_div, self.soft_mul, self.soft_cmp = soft_div, soft_mul, soft_cmp
+        self.march_chunk = march_chunk
         self.shape = mmp.shape
         self.dim = mmp.dim
 
@@ -98,6 +99,244 @@ class LevelEmitter:
         for a in range(1, self.dim):
             e = "(%s * %d + %s)" % (e, self.shape[a], parts[a])
         return e
+
+    def _emit_ops(self, which, alias: Dict[int, str], w, ind: str) -> None:
+        """C statements for the micro ops in `which` (topological order), one
+        `const` temporary a<i> each; an op in `alias` is bound to that C
+        expression (a value carried from the previous cell) instead."""
+        L = self.level
+        const_vals: Dict[int, object] = {}
+        for i, m in enumerate(L.micro):
+            if m.kind == "const":
+                const_vals[i] = m.args[0]
+        prepared = set()  # divisor nodes whose reciprocal is prepared
+        for i in which:
+            m = L.micro[i]
+            if i in alias:
+                w(ind + "const %s a%d = %s;" % (m.ctype, i, alias[i]))
+                continue
+            t = m.ctype
+            name = "a%d" % i
+            k = m.kind
+            if k == "const":
+                const_vals[i] = m.args[0]
+                w(ind + "const %s %s = %s;" % (t, name, MM.c_literal(m.args[0], t)))
+            elif k == "loadS":
+                w(ind + "const %s %s = s_%s[%s];" % (t, name, m.args[1], self.idx_expr(m.args[0])))
+            elif k == "loadM":
+                arr = self.mmp.arrays[m.args[1]]
+                w(ind + "const %s %s = r_%s[%s];" % (t, name, arr.name, self.idx_expr(m.args[0])))
+            elif k == "index":
+                w(ind + "const %s %s = (%s)%s;" % (t, name, t, AXVARS[m.args[0]]))
+            elif k == "uni":
+                op, a = m.args
+                if op.startswith("external-call/"):
+                    f = op.split("/", 1)[1]
+                    w(ind + "const %s %s = %s((double)a%d);" % (t, name, f, a))
+                else:
+                    w(ind + "const %s %s = (%sa%d);" % (t, name, op, a))
+            elif k == "bin":
+                op, a, b = m.args
+                ta, tb = L.micro[a].ctype, L.micro[b].ctype
+                dd = t == "double" and ta == "double" and tb == "double"
+                if op == "**":
+                    w(ind + "const %s %s = pow((double)a%d, (double)a%d);" % (t, name, a, b))
+                elif (op == "/" and self.soft_div and dd and b in const_vals and
+                      _pow2_exponent(const_vals[b]) is not None):
+                    w(ind + "const %s %s = fm::soft::scale_pow2(a%d, %d);" %
+                      (t, name, a, -_pow2_exponent(const_vals[b])))
+                elif (op == "/" and self.soft_div and dd and b in const_vals and
+                      _normal_double(const_vals[b]) and const_vals[b] > 0):
+                    w(ind + "const %s %s = fm::soft::div_const_s(a%d, fm::soft::DivConstS%s);" %
+                      (t, name, a, div_const_fields(const_vals[b])))
+                elif op == "/" and self.soft_div and dd and b not in const_vals:
+                    if b not in prepared:
+                        prepared.add(b)
+                        w(ind + "const fm::soft::DivVarS dv%d = fm::soft::prep_div_s(a%d);" % (b, b))
+                    w(ind + "const %s %s = fm::soft::div_var_s(a%d, dv%d);" % (t, name, a, b))
+                elif (op == "*" and self.soft_mul and dd and
+                      (b in const_vals or a in const_vals) and
+                      _pow2_exponent(const_vals[b] if b in const_vals else const_vals[a])
+                      is not None):
+                    x, c = (a, b) if b in const_vals else (b, a)
+                    w(ind + "const %s %s = fm::soft::scale_pow2(a%d, %d);" %
+                      (t, name, x, _pow2_exponent(const_vals[c])))
+                elif (op == "*" and self.soft_mul and t == "double" and
+                      ((b in const_vals and ta == "double" and _normal_double(const_vals[b])) or
+                       (a in const_vals and tb == "double" and _normal_double(const_vals[a])))):
+                    x, c = (a, b) if b in const_vals else (b, a)
+                    w(ind + "const %s %s = fm::soft::mul_const_s(a%d, fm::soft::MulConstS%s);" %
+                      (t, name, x, mul_const_fields(const_vals[c])))
+                elif (op in CMP_SOFT and self.soft_cmp and ta == "double" and tb == "double"):
+                    x, y = (b, a) if op in (">", ">=") else (a, b)
+                    w(ind + "const %s %s = %s;" % (t, name, CMP_SOFT[op] % (x, y)))
+                else:
+                    w(ind + "const %s %s = (a%d %s a%d);" % (t, name, a, op, b))
+            elif k == "ite":
+                c, a, b = m.args
+                w(ind + "const %s %s = (a%d ? a%d : a%d);" % (t, name, c, a, b))
+            elif k == "nary":
+                op, xs = m.args
+                names = ["(double)a%d" % x for x in xs]
+
+                def chain(fn, items):
+                    acc = items[-1]
+                    for it in reversed(items[:-1]):
+                        acc = "%s(%s, %s)" % (fn, it, acc)
+                    return acc
+
+                soft = self.soft_cmp and t == "double" and all(
+                    L.micro[x].ctype == "double" for x in xs)
+                fmax_, fmin_ = ("fm::soft::max_s", "fm::soft::min_s") if soft else ("fmax", "fmin")
+                if op == ">?":
+                    e = chain(fmax_, names)
+                elif op == "<?":
+                    e = chain(fmin_, names)
+                else:
+                    e = "%s(0.0, %s) + %s(0.0, %s)" % (fmin_, chain(fmax_, names), fmax_,
+                                                       chain(fmin_, names))
+                w(ind + "const %s %s = %s;" % (t, name, e))
+            else:
+                raise MM.OM.FmrSemanticError("cannot emit %s" % k)
+
+    # -- marching along axis 0 ------------------------------------------------------------
+    def _shifted(self) -> Dict[int, int]:
+        """For each micro op i, the op j whose value at cell x equals op i's at
+        cell x+1 along axis 0 (i itself for values that do not depend on the
+        position along axis 0), where the level has one."""
+        L = self.level
+        index = {(m.kind, m.args, m.ctype): i for i, m in enumerate(L.micro)}
+        memo: Dict[int, Optional[int]] = {}
+
+        def sh(i: int) -> Optional[int]:
+            if i in memo:
+                return memo[i]
+            m = L.micro[i]
+            k, args = m.kind, m.args
+            r: Optional[int] = None
+            if k in ("const", "imm"):
+                r = i
+            elif k == "index":
+                r = None if args[0] == 0 else i
+            elif k in ("loadS", "loadM"):
+                c = (args[0][0] + 1,) + tuple(args[0][1:])
+                r = index.get((k, (c, args[1]), m.ctype))
+            else:
+                ops = MM._Builder._operands(k, args)
+                new = [sh(j) for j in ops]
+                if all(j is not None for j in new):
+                    if k == "uni":
+                        a2 = (args[0], new[0])
+                    elif k == "bin":
+                        a2 = (args[0], new[0], new[1])
+                    elif k == "ite":
+                        a2 = tuple(new)
+                    else:  # nary
+                        a2 = (args[0], tuple(new))
+                    r = index.get((k, a2, m.ctype))
+            memo[i] = r
+            return r
+
+        out = {}
+        for i in range(len(L.micro)):
+            j = sh(i)
+            if j is not None and L.micro[i].kind not in ("const", "imm"):
+                out[i] = j
+        return out
+
+    def _march_plan(self):
+        """(ops the loop body needs, carried ops {i: j}): op i is taken from op
+        j's value at the previous cell; everything else is computed."""
+        L = self.level
+        carried_all = self._shifted()
+        need = set()
+        carried = {}
+        stack = [a.root for a in L.arrays]
+        need.update(stack)
+        while stack:
+            i = stack.pop()
+            if i in carried_all:
+                j = carried_all[i]
+                carried[i] = j
+                if j not in need:
+                    need.add(j)
+                    stack.append(j)
+            else:
+                for j in MM._Builder._operands(L.micro[i].kind, L.micro[i].args):
+                    if j not in need:
+                        need.add(j)
+                        stack.append(j)
+        return need, carried
+
+    def _wrap_lines(self, w, ind: str, axes) -> None:
+        needed = set()
+        for m in self.level.micro:
+            if m.kind in ("loadS", "loadM"):
+                for a, c in enumerate(m.args[0]):
+                    if c and a in axes:
+                        needed.add((a, c))
+        for a, c in sorted(needed):
+            n = self.shape[a]
+            v = _wrap_name(a, c)
+            if abs(c) < n:
+                if c > 0:
+                    w(ind + "const int %s = %s + %d >= %d ? %s + %d : %s + %d;" %
+                      (v, AXVARS[a], c, n, AXVARS[a], c - n, AXVARS[a], c))
+                else:
+                    w(ind + "const int %s = %s - %d < 0 ? %s + %d : %s - %d;" %
+                      (v, AXVARS[a], -c, AXVARS[a], n + c, AXVARS[a], -c))
+            else:
+                w(ind + "const int %s = ((%s + %d) %% %d + %d) %% %d;" % (v, AXVARS[a], c, n, n, n))
+
+    def _march_body(self, need, carried, chunk: int):
+        """Kernel body: each thread takes one column (a cell of axes 1..d-1) and a
+        chunk of `chunk` cells along axis 0; the first cell evaluates every op,
+        the following ones take the carried ops from the previous cell (same
+        operations on the same values: bit-identical)."""
+        L = self.level
+        ncol = 1
+        for n in self.shape[1:]:
+            ncol *= n
+        n0 = self.shape[0]
+        nchunk = (n0 + chunk - 1) // chunk
+        body: List[str] = []
+        w = body.append
+        w("    const long long col = item %% %dll;" % ncol)
+        w("    const int x0 = (int)(item / %dll) * %d;" % (ncol, chunk))
+        w("    const int x1 = x0 + %d < %d ? x0 + %d : %d;" % (chunk, n0, chunk, n0))
+        w("    size_t rest = (size_t)col;")
+        for a in reversed(range(1, self.dim)):
+            if a == 1:
+                w("    const int %s = (int)rest;" % AXVARS[a])
+            else:
+                w("    const int %s = (int)(rest %% %du); rest /= %du;" % (AXVARS[a], self.shape[a],
+                                                                       self.shape[a]))
+        self._wrap_lines(w, "    ", set(range(1, self.dim)))
+        live_carry = sorted(i for i in carried if i in need)
+        for i in live_carry:
+            w("    %s h%d;" % (L.micro[i].ctype, i))  # value held from the previous cell
+        # first cell of the chunk: every op
+        w("    {")
+        w("      const int c0 = x0;")
+        w("      const size_t idx = (size_t)c0 * %dull + (size_t)col;" % ncol)
+        self._wrap_lines(w, "      ", {0})
+        self._emit_ops(range(len(L.micro)), {}, w, "      ")
+        for arr in L.arrays:
+            w("      w_%s[idx] = a%d;" % (arr.name, arr.root))
+        for i in live_carry:
+            w("      h%d = a%d;" % (i, carried[i]))
+        w("    }")
+        # the rest of the chunk
+        w("    for (int c0 = x0 + 1; c0 < x1; ++c0) {")
+        w("      const size_t idx = (size_t)c0 * %dull + (size_t)col;" % ncol)
+        self._wrap_lines(w, "      ", {0})
+        self._emit_ops(sorted(need), {i: "h%d" % i for i in live_carry}, w, "      ")
+        for arr in L.arrays:
+            w("      w_%s[idx] = a%d;" % (arr.name, arr.root))
+        for i in live_carry:
+            w("      h%d = a%d;" % (i, carried[i]))
+        w("    }")
+        return body, ncol * nchunk
 
     def emit(self) -> Tuple[str, List[str], List[int], List[MM.Array]]:
         L = self.level
@@ -115,6 +354,24 @@ class LevelEmitter:
         ncells = 1
         for n in self.shape:
             ncells *= n
+        kname = "fmr_level_%d" % self.li
+        # automatic (march_chunk = 0): chunks of up to 16 cells that leave ~150k
+        # threads (the generated MHD program at 64^3 ran slower with chunks of 3 and
+        # 53k threads than with one cell per thread; at 256^3 chunks of 16 gain 12-14 %)
+        if self.march_chunk > 0:
+            chunk = min(self.march_chunk, self.shape[0])
+        else:
+            chunk = min(16, self.shape[0], max(1, ncells // 150000))
+        if chunk > 1 and self.dim >= 2:
+            need, carried = self._march_plan()
+            if any(i in need for i in carried):
+                body, nitems = self._march_body(need, carried, chunk)
+                src = ["__global__ void __launch_bounds__(256) %s(%s) {" % (kname, ", ".join(params)),
+                       "  for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;"
+                       " item < %dll; item += (long long)gridDim.x * blockDim.x) {" % nitems]
+                src += body
+                src += ["  }", "}", ""]
+                return "\n".join(src), state_names, arr_ids, L.arrays
         body: List[str] = []
         w = body.append
         # coordinates
@@ -143,95 +400,9 @@ class LevelEmitter:
                       (v, AXVARS[a], -c, AXVARS[a], n + c, AXVARS[a], -c))
             else:
                 w("    const int %s = ((%s + %d) %% %d + %d) %% %d;" % (v, AXVARS[a], c, n, n, n))
-        const_vals: Dict[int, object] = {}
-        prepared = set()  # divisor nodes whose reciprocal is prepared
-        for i, m in enumerate(L.micro):
-            t = m.ctype
-            name = "a%d" % i
-            k = m.kind
-            if k == "const":
-                const_vals[i] = m.args[0]
-                w("    const %s %s = %s;" % (t, name, MM.c_literal(m.args[0], t)))
-            elif k == "loadS":
-                w("    const %s %s = s_%s[%s];" % (t, name, m.args[1], self.idx_expr(m.args[0])))
-            elif k == "loadM":
-                arr = self.mmp.arrays[m.args[1]]
-                w("    const %s %s = r_%s[%s];" % (t, name, arr.name, self.idx_expr(m.args[0])))
-            elif k == "index":
-                w("    const %s %s = (%s)%s;" % (t, name, t, AXVARS[m.args[0]]))
-            elif k == "uni":
-                op, a = m.args
-                if op.startswith("external-call/"):
-                    f = op.split("/", 1)[1]
-                    w("    const %s %s = %s((double)a%d);" % (t, name, f, a))
-                else:
-                    w("    const %s %s = (%sa%d);" % (t, name, op, a))
-            elif k == "bin":
-                op, a, b = m.args
-                ta, tb = L.micro[a].ctype, L.micro[b].ctype
-                dd = t == "double" and ta == "double" and tb == "double"
-                if op == "**":
-                    w("    const %s %s = pow((double)a%d, (double)a%d);" % (t, name, a, b))
-                elif (op == "/" and self.soft_div and dd and b in const_vals and
-                      _pow2_exponent(const_vals[b]) is not None):
-                    w("    const %s %s = fm::soft::scale_pow2(a%d, %d);" %
-                      (t, name, a, -_pow2_exponent(const_vals[b])))
-                elif (op == "/" and self.soft_div and dd and b in const_vals and
-                      _normal_double(const_vals[b]) and const_vals[b] > 0):
-                    w("    const %s %s = fm::soft::div_const_s(a%d, fm::soft::DivConstS%s);" %
-                      (t, name, a, div_const_fields(const_vals[b])))
-                elif op == "/" and self.soft_div and dd and b not in const_vals:
-                    if b not in prepared:
-                        prepared.add(b)
-                        w("    const fm::soft::DivVarS dv%d = fm::soft::prep_div_s(a%d);" % (b, b))
-                    w("    const %s %s = fm::soft::div_var_s(a%d, dv%d);" % (t, name, a, b))
-                elif (op == "*" and self.soft_mul and dd and
-                      (b in const_vals or a in const_vals) and
-                      _pow2_exponent(const_vals[b] if b in const_vals else const_vals[a])
-                      is not None):
-                    x, c = (a, b) if b in const_vals else (b, a)
-                    w("    const %s %s = fm::soft::scale_pow2(a%d, %d);" %
-                      (t, name, x, _pow2_exponent(const_vals[c])))
-                elif (op == "*" and self.soft_mul and t == "double" and
-                      ((b in const_vals and ta == "double" and _normal_double(const_vals[b])) or
-                       (a in const_vals and tb == "double" and _normal_double(const_vals[a])))):
-                    x, c = (a, b) if b in const_vals else (b, a)
-                    w("    const %s %s = fm::soft::mul_const_s(a%d, fm::soft::MulConstS%s);" %
-                      (t, name, x, mul_const_fields(const_vals[c])))
-                elif (op in CMP_SOFT and self.soft_cmp and ta == "double" and tb == "double"):
-                    x, y = (b, a) if op in (">", ">=") else (a, b)
-                    w("    const %s %s = %s;" % (t, name, CMP_SOFT[op] % (x, y)))
-                else:
-                    w("    const %s %s = (a%d %s a%d);" % (t, name, a, op, b))
-            elif k == "ite":
-                c, a, b = m.args
-                w("    const %s %s = (a%d ? a%d : a%d);" % (t, name, c, a, b))
-            elif k == "nary":
-                op, xs = m.args
-                names = ["(double)a%d" % x for x in xs]
-
-                def chain(fn, items):
-                    acc = items[-1]
-                    for it in reversed(items[:-1]):
-                        acc = "%s(%s, %s)" % (fn, it, acc)
-                    return acc
-
-                soft = self.soft_cmp and t == "double" and all(
-                    L.micro[x].ctype == "double" for x in xs)
-                fmax_, fmin_ = ("fm::soft::max_s", "fm::soft::min_s") if soft else ("fmax", "fmin")
-                if op == ">?":
-                    e = chain(fmax_, names)
-                elif op == "<?":
-                    e = chain(fmin_, names)
-                else:
-                    e = "%s(0.0, %s) + %s(0.0, %s)" % (fmin_, chain(fmax_, names), fmax_,
-                                                       chain(fmin_, names))
-                w("    const %s %s = %s;" % (t, name, e))
-            else:
-                raise MM.OM.FmrSemanticError("cannot emit %s" % k)
+        self._emit_ops(range(len(L.micro)), {}, w, "    ")
         for arr in L.arrays:
             w("    w_%s[idx] = a%d;" % (arr.name, arr.root))
-        kname = "fmr_level_%d" % self.li
         src = ["__global__ void __launch_bounds__(256) %s(%s) {" % (kname, ", ".join(params)),
                "  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < %dll;"
                " idx += (long long)gridDim.x * blockDim.x) {" % ncells]
@@ -241,13 +412,16 @@ class LevelEmitter:
 
 
 def emit_kernels(mmp: MM.MMProgram, soft_div: bool = True, soft_mul: bool = True,
-                 soft_cmp: bool = True):
+                 soft_cmp: bool = True, march_chunk: int = 0):
     """Kernel source and, per level, (kernel name, state names read, arrays
-    read, arrays written)."""
+    read, arrays written).  A thread evaluates a chunk of cells along axis 0
+    and carries the values a cell shares with the next one: march_chunk cells
+    (1: one cell per thread), or with 0 up to 16 while ~150k threads remain."""
     parts = []
     levels = []
     for li, L in enumerate(mmp.levels):
-        src, sn, ar, aw = LevelEmitter(mmp, L, li, soft_div, soft_mul, soft_cmp).emit()
+        src, sn, ar, aw = LevelEmitter(mmp, L, li, soft_div, soft_mul, soft_cmp,
+                                       march_chunk).emit()
         parts.append(src)
         levels.append(("fmr_level_%d" % li, sn, ar, aw))
     return "\n".join(parts), levels

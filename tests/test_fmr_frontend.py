@@ -198,7 +198,7 @@ def test_generated_integer_pipe_forms_compile(tmp_path):
     from formura_gb300.fmr.emit_cuda import emit_kernels
 
     p = load_program(EX / "fmr-limiter.fmr")
-    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)))
+    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)), march_chunk=1)
     for form in ("prep_div_s", "div_var_s", "scale_pow2", "max_s", "min_s", "lt_s", "le_s",
                  "eq_s", "mul_const_s"):
         assert "fm::soft::" + form in kern, form
@@ -209,6 +209,28 @@ def test_generated_integer_pipe_forms_compile(tmp_path):
     assert max(uses.values()) == 2 and kern.count("prep_div_s(") == len(uses)
     assert "fmax(" not in kern and "fmin(" not in kern and " / " not in kern
     backend.build_program(p, outdir=tmp_path)
+
+
+def test_marching_kernels_carry_shared_values():
+    """In the x-marching form a thread evaluates a chunk of cells along axis 0;
+    values a cell shares with the next one (loads at x+1 that become loads at
+    x, the face flux at x+1/2 that becomes the one at x-1/2) are carried in
+    registers, so the loop body of gray-scott-3d evaluates fewer loads and
+    divisions than its first cell."""
+    from formura_gb300.fmr.emit_cuda import emit_kernels
+
+    p = load_program(EX / "gray-scott-3d.fmr")
+    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)))
+    first, loop = kern.split("for (int c0 = x0 + 1;")
+    first = first[first.index("const int c0 = x0;"):]
+    count = lambda text, s: text.count(s)
+    assert count(loop, "s_U[") + count(loop, "s_V[") == 10   # 14 in the first cell
+    assert count(first, "s_U[") + count(first, "s_V[") == 14
+    assert count(loop, "div_const_s") == count(first, "div_const_s") - 2
+    assert "h0 = a" in loop and "= h0;" in loop
+    # one cell per thread when asked
+    flat, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)), march_chunk=1)
+    assert "x0" not in flat
 
 
 CURRENT_SYNTAX_EXAMPLES = [

@@ -39,6 +39,14 @@ def _random_state(prog, rng):
     ("fmr-3d-advection.fmr", dict(intra_node_shape=[5, 3, 33], monitor_interval=4)),
     ("fmr-limiter.fmr", {}),
     ("fmr-limiter.fmr", dict(intra_node_shape=[9, 17], monitor_interval=6)),
+    # the x-marching kernels (values carried between consecutive cells along x),
+    # chunks that divide the axis and chunks that do not
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[16, 24, 40], monitor_interval=5, march_chunk=4)),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[19, 8, 16], monitor_interval=3, march_chunk=5)),
+    ("fmr-3d-advection.fmr", dict(march_chunk=6)),
+    ("fmr-features.fmr", dict(march_chunk=7)),
+    ("fmr-limiter.fmr", dict(march_chunk=3)),
+    ("diffusion-2d.fmr", dict(intra_node_shape=[64, 48], monitor_interval=7, march_chunk=16)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)
