@@ -23,7 +23,11 @@
 // split-K GEMM: M = (tap, ci) rows (576, in 5 tiles of 128), N = co,
 // K = pixels; each CTA accumulates a pixel range in TMEM and adds its tile
 // to the fp32 gradient with atomics.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <mutex>
 
 #include "fm_common.cuh"
 #include "fm_tc.cuh"
@@ -342,11 +346,14 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
 #pragma unroll
       for (int q = 0; q < 4; ++q) rv[q] = r4[p * 8 + ((chalf * 4 + q) ^ (p & 7))];
     }
+    float vv[32];
+    tmem_ld32(tmem + (uint32_t)(acc * 64) + ((uint32_t)(quarter * 32) << 16) +
+                  (uint32_t)(chalf * (NT / 2)),
+              vv);
 #pragma unroll
     for (int cc = 0; cc < NT / 2; cc += 16) {
       const int c0 = chalf * (NT / 2) + cc;
-      float v[16];
-      tmem_ld16(tmem + (uint32_t)(acc * 64) + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, v);
+      float *v = vv + cc;
       if (!interior) continue;
       if (a.bias) {
 #pragma unroll
@@ -452,6 +459,266 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
   if (!ok && tid == 0) atomicExch(a.err, 1);
   fence_before_sync();
   __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// ---------------------------------------------------------------------------
+// conv3x3_fwd_tma: conv3x3_fwd_res with its staging on TMA and its steps
+// chained by mbarriers instead of CTA-wide barriers.
+//   * a tile's region (8 channel-group planes, as above) arrives by 16 tiled
+//     TMA copies (a plane per channel group, in two boxes of at most 256
+//     positions), its residual rows by one TMA copy with the 128-byte swizzle
+//     (position p's 16-byte chunk q lands at chunk q ^ (p % 8): conflict-free
+//     reads); each completes on its buffer's mbarrier by transaction count;
+//   * thread 0 issues a tile's MMAs as soon as its region has landed and the
+//     epilogue of the tile two back has released the accumulator (acc_empty,
+//     one arrival per warp), so the MMAs of tile t+1 run under the epilogue of
+//     tile t, and the region of tile t+2 is requested as soon as the MMAs of
+//     tile t have finished reading region buffer t % 2;
+//   * weights stay resident (loaded once with cp.async), two TMEM accumulators.
+// Same MMA sequence and epilogue as conv3x3_fwd_res: identical results.
+__global__ void __launch_bounds__(kResThreads, 1)
+    conv3x3_fwd_tma(ConvArgs a, int ntile_img, int ntiles, int plane, int rlen, int r1,
+                    const __grid_constant__ CUtensorMap tm_x1,
+                    const __grid_constant__ CUtensorMap tm_x2,
+                    const __grid_constant__ CUtensorMap tm_r) {
+  constexpr int NT = 64;
+  constexpr int kWBytes = 9 * NT * CIN * 2;
+  constexpr uint32_t kResBytes = kTM * NT * 2;  // 16 KB of residual rows per tile
+  extern __shared__ __align__(1024) uint8_t dsm[];
+  uint8_t *sw = dsm;
+  uint8_t *sreg = dsm + kWBytes;
+  uint8_t *sres = dsm + (((size_t)kWBytes + 16 * (size_t)plane + 1023) & ~(size_t)1023);
+  __shared__ __align__(8) uint64_t full_x[2], full_r[2], mma_done[2], acc_empty[2];
+  __shared__ uint32_t s_tmem;
+  __shared__ float s_bias[NT];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3, chalf = warp >> 2;
+  if (tid < NT) s_bias[tid] = a.bias ? a.bias[tid] : 0.0f;
+  const int H = a.H, W = a.W, Wp = W + 2;
+  const long long img = (long long)(H + 2) * Wp;
+  if (warp == 0) tmem_alloc(&s_tmem, 128);
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&full_x[b], 1);
+      mbar_init(&full_r[b], 1);
+      mbar_init(&mma_done[b], 1);
+      mbar_init(&acc_empty[b], kResThreads / 32);
+    }
+  }
+  for (int v = tid; v < 9 * NT * 8; v += kResThreads) {
+    const int tap = v / (NT * 8), rem = v % (NT * 8);
+    const int r = rem >> 3, kk = (rem & 7) * 8;
+    cp_async16(sw + tap * (NT * CIN * 2) + kmajor_off(r, kk, CIN),
+               a.w + ((size_t)r * 9 + tap) * CIN + kk, true);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  fence_proxy_async_smem();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  const uint32_t idesc = idesc_bf16_f32(kTM, NT);
+  const int my_tiles =
+      ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / gridDim.x + 1 : 0;
+
+  auto tile_pos = [&](int it, int &b, long long &j0) {
+    const int tile = blockIdx.x + it * gridDim.x;
+    b = tile / ntile_img;
+    j0 = (long long)(Wp + 1) + (long long)(tile % ntile_img) * kTM;
+  };
+  // (thread 0) region of tile `it` into region buffer it % 2
+  auto issue_x = [&](int it) {
+    int b;
+    long long j0;
+    tile_pos(it, b, j0);
+    const int r0 = (int)(j0 - (Wp + 1));
+    uint64_t *bar = &full_x[it & 1];
+    uint8_t *dst = sreg + (size_t)(it & 1) * 8 * plane;
+    mbar_arrive_expect_tx(bar, (uint32_t)(8 * rlen * 16));
+    for (int kg = 0; kg < 8; ++kg) {
+      tma_load_3d(dst + (size_t)kg * plane, &tm_x1, kg * 8, r0, b, bar);
+      if (rlen > r1) tma_load_3d(dst + (size_t)kg * plane + (size_t)r1 * 16, &tm_x2, kg * 8, r0 + r1, b, bar);
+    }
+  };
+  // (thread 0) residual rows of tile `it` into residual buffer it % 2
+  auto issue_r = [&](int it) {
+    int b;
+    long long j0;
+    tile_pos(it, b, j0);
+    uint64_t *bar = &full_r[it & 1];
+    mbar_arrive_expect_tx(bar, kResBytes);
+    tma_load_3d(sres + (size_t)(it & 1) * kResBytes, &tm_r, 0, (int)j0, b, bar);
+  };
+
+  bool ok = true;
+  // bookkeeping for the clean-up: the last tile issued per buffer (-1: none)
+  int last_x[2] = {-1, -1}, last_r[2] = {-1, -1}, last_mma[2] = {-1, -1};
+  if (tid == 0) {
+    for (int it = 0; it < 2 && it < my_tiles; ++it) {
+      issue_x(it);
+      last_x[it & 1] = it;
+      if (a.resid) {
+        issue_r(it);
+        last_r[it & 1] = it;
+      }
+    }
+  }
+
+  auto epilogue = [&](int t) {
+    const int bt = t & 1;
+    const uint32_t pt = (uint32_t)(t >> 1) & 1u;
+    __syncwarp();
+    bool good = mbar_wait(&mma_done[bt], pt);
+    fence_after_sync();
+    // region buffer bt is free: request tile t+2's region
+    if (tid == 0 && good && ok && t + 2 < my_tiles) {
+      issue_x(t + 2);
+      last_x[bt] = t + 2;
+    }
+    if (a.resid && good) good = mbar_wait(&full_r[bt], pt);
+    ok = __all_sync(0xffffffffu, ok && good);  // warp-uniform from here on
+    int b;
+    long long j0;
+    tile_pos(t, b, j0);
+    const long long j = j0 + quarter * 32 + lane;
+    const int py = (int)(j / Wp), px = (int)(j % Wp);
+    const bool interior = ok && py >= 1 && py <= H && px >= 1 && px <= W;
+    const int y = py - 1, xx = px - 1;
+    int pys[2] = {py, -1}, pxs[2] = {px, -1};
+    if (y == 0) pys[1] = H + 1;
+    if (y == H - 1) pys[1] = 0;
+    if (xx == 0) pxs[1] = W + 1;
+    if (xx == W - 1) pxs[1] = 0;
+    const size_t pin = (size_t)b * img + (size_t)j;
+    uint4 gv[4], rv[4];
+    if (interior && a.gate) {
+      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * (NT / 2));
+#pragma unroll
+      for (int q = 0; q < 4; ++q) gv[q] = __ldg(g4 + q);
+    }
+    if (interior && a.resid) {
+      const int p = quarter * 32 + lane;
+      const uint4 *r4 = reinterpret_cast<const uint4 *>(sres + (size_t)bt * kResBytes);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) rv[q] = r4[p * 8 + ((chalf * 4 + q) ^ (p & 7))];
+    }
+    float vv[32];
+    tmem_ld32(tmem + (uint32_t)(bt * 64) + ((uint32_t)(quarter * 32) << 16) +
+                  (uint32_t)(chalf * (NT / 2)),
+              vv);
+#pragma unroll
+    for (int cc = 0; cc < NT / 2; cc += 16) {
+      const int c0 = chalf * (NT / 2) + cc;
+      float *v = vv + cc;
+      if (!interior) continue;
+      if (a.bias) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += s_bias[c0 + i];
+      }
+      if (a.gate) {
+        const bf16 *g = reinterpret_cast<const bf16 *>(&gv[cc / 8]);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] *= gelu_grad(__bfloat162float(g[i]));
+      }
+      if (a.resid) {
+        const bf16 *rr = reinterpret_cast<const bf16 *>(&rv[cc / 8]);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] += __bfloat162float(rr[i]);
+      }
+      __align__(16) bf16 zb[16], yb[16];
+      if (a.z_out) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) zb[i] = __float2bfloat16_rn(v[i]);
+      }
+      if (a.act == 1) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) yb[i] = __float2bfloat16_rn(v[i]);
+#pragma unroll
+      for (int iy = 0; iy < 2; ++iy) {
+        if (pys[iy] < 0) continue;
+#pragma unroll
+        for (int ix = 0; ix < 2; ++ix) {
+          if (pxs[ix] < 0) continue;
+          const size_t q = (((size_t)b * (H + 2) + pys[iy]) * Wp + pxs[ix]) * NT + c0;
+          if (a.z_out) {
+            reinterpret_cast<uint4 *>(a.z_out + q)[0] = reinterpret_cast<const uint4 *>(zb)[0];
+            reinterpret_cast<uint4 *>(a.z_out + q)[1] = reinterpret_cast<const uint4 *>(zb)[1];
+          }
+          if (a.y_out) {
+            reinterpret_cast<uint4 *>(a.y_out + q)[0] = reinterpret_cast<const uint4 *>(yb)[0];
+            reinterpret_cast<uint4 *>(a.y_out + q)[1] = reinterpret_cast<const uint4 *>(yb)[1];
+          }
+        }
+      }
+      if (a.y_f32) {
+        float *dst = a.y_f32 + (((size_t)b * H + y) * W + xx) * NT + c0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) dst[i] = v[i];
+      }
+    }
+    // this warp is done with accumulator bt and residual buffer bt
+    fence_before_sync();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&acc_empty[bt]);
+    if (tid == 0 && ok && a.resid && t + 2 < my_tiles) {
+      if (!mbar_wait(&acc_empty[bt], pt)) ok = false;
+      if (ok) {
+        issue_r(t + 2);
+        last_r[bt] = t + 2;
+      }
+    }
+  };
+
+  for (int it = 0; it < my_tiles && ok; ++it) {
+    const int bb = it & 1;
+    if (tid == 0) {
+      if (!mbar_wait(&full_x[bb], (uint32_t)(it >> 1) & 1u)) ok = false;
+      if (ok && it >= 2 && !mbar_wait(&acc_empty[bb], (uint32_t)((it - 2) >> 1) & 1u)) ok = false;
+      fence_after_sync();
+      if (ok) {
+        const uint32_t reg = smem_u32(sreg + (size_t)bb * 8 * plane);
+        const uint32_t wbase = smem_u32(sw);
+#pragma unroll 1
+        for (int tap = 0; tap < 9; ++tap) {
+          const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+          const uint32_t a_off = (uint32_t)((Wp + 1) + dy * Wp + dx) * 16u;
+#pragma unroll
+          for (int s = 0; s < CIN / 16; ++s) {
+            const uint64_t ad = smem_desc(reg + a_off + (uint32_t)(2 * s) * (uint32_t)plane,
+                                          (uint32_t)plane, 128);
+            const uint64_t bd = smem_desc(wbase + tap * (NT * CIN * 2) + s * 256, 128,
+                                          (CIN / 8) * 128);
+            mma_bf16(tmem + (uint32_t)(bb * 64), ad, bd, idesc, (tap | s) != 0);
+          }
+        }
+        mma_commit(&mma_done[bb]);
+        last_mma[bb] = it;
+      }
+    }
+    if (it >= 1) epilogue(it - 1);
+    // a failed wait of thread 0 stops its whole warp at the same point (the
+    // epilogue's TMEM loads are warp-collective)
+    ok = __all_sync(0xffffffffu, ok);
+  }
+  if (my_tiles > 0 && ok) epilogue(my_tiles - 1);
+  // clean-up: nothing may still be writing shared memory or TMEM when the CTA
+  // ends — wait (bounded) for the last TMA copies and MMAs issued per buffer
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b) {
+      if (last_x[b] >= 0) mbar_wait(&full_x[b], (uint32_t)(last_x[b] >> 1) & 1u);
+      if (last_r[b] >= 0) mbar_wait(&full_r[b], (uint32_t)(last_r[b] >> 1) & 1u);
+      if (last_mma[b] >= 0) mbar_wait(&mma_done[b], (uint32_t)(last_mma[b] >> 1) & 1u);
+    }
+    if (!ok) atomicExch(a.err, 1);
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
   if (warp == 0) tmem_dealloc(tmem, 128);
 }
 
@@ -645,6 +912,108 @@ int launch_fwd_res(const ConvArgs &a, cudaStream_t s) {
 }
 }  // namespace
 
+namespace {
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  }
+  return fn;
+}
+
+// A 3D tiled tensor map over a padded NHWC bf16 tensor viewed as
+// [B][(H+2)*(W+2) positions][64 channels]; box = {bc channels, bp positions, 1}.
+bool encode_positions_map_uncached(CUtensorMap *m, const void *base, long long img, int B, int bc,
+                                   int bp, bool swizzle128) {
+  auto enc = tensor_map_encoder();
+  if (!enc || ((uintptr_t)base & 15u)) return false;
+  cuuint64_t dims[3] = {64, (cuuint64_t)img, (cuuint64_t)B};
+  cuuint64_t strides[2] = {128, (cuuint64_t)img * 128};
+  cuuint32_t box[3] = {(cuuint32_t)bc, (cuuint32_t)bp, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The encoded maps of recent (buffer, shape, box) combinations: a network step
+// runs the same layers on the same buffers, and encoding costs microseconds of
+// host time per map.
+bool encode_positions_map(CUtensorMap *m, const void *base, long long img, int B, int bc, int bp,
+                          bool swizzle128) {
+  struct Entry {
+    const void *base;
+    long long img;
+    int B, bc, bp;
+    bool sw;
+    CUtensorMap map;
+  };
+  constexpr int kEntries = 64;
+  static Entry cache[kEntries];
+  static int used = 0, next = 0;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  for (int i = 0; i < used; ++i) {
+    const Entry &e = cache[i];
+    if (e.base == base && e.img == img && e.B == B && e.bc == bc && e.bp == bp && e.sw == swizzle128) {
+      *m = e.map;
+      return true;
+    }
+  }
+  if (!encode_positions_map_uncached(m, base, img, B, bc, bp, swizzle128)) return false;
+  Entry &e = cache[next];
+  e = Entry{base, img, B, bc, bp, swizzle128, *m};
+  next = (next + 1) % kEntries;
+  used = used < kEntries ? used + 1 : kEntries;
+  return true;
+}
+
+int launch_fwd_tma(const ConvArgs &a, cudaStream_t s) {
+  const int Wp = a.W + 2;
+  const int rlen = res_region_len(Wp);
+  const int r1 = std::min(rlen, 192);  // first box: a multiple of 8 positions (128-byte aligned)
+  if (rlen - r1 > 256) return FM_ERR_UNSUPPORTED;
+  const int plane = ((rlen * 16 + 127) / 128) * 128;
+  const size_t smem = (((size_t)9 * 64 * CIN * 2 + 16 * (size_t)plane + 1023) & ~(size_t)1023) +
+                      2 * (size_t)kTM * 64 * 2;
+  int dev = 0, optin = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  FM_TRY_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (smem > (size_t)optin) return FM_ERR_UNSUPPORTED;
+  const long long img = (long long)(a.H + 2) * Wp;
+  CUtensorMap tx1, tx2, tr;
+  if (!encode_positions_map(&tx1, a.x, img, a.B, 8, r1, false)) return FM_ERR_UNSUPPORTED;
+  if (!encode_positions_map(&tx2, a.x, img, a.B, 8, rlen > r1 ? rlen - r1 : 8, false))
+    return FM_ERR_UNSUPPORTED;
+  tr = tx1;
+  if (a.resid && !encode_positions_map(&tr, a.resid, img, a.B, 64, kTM, true))
+    return FM_ERR_UNSUPPORTED;
+  FM_TRY_CUDA(cudaFuncSetAttribute(conv3x3_fwd_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  int sms = 0;
+  int st = fm::device_sm_count(&sms);
+  if (st) return st;
+  const long long span = (long long)a.H * Wp - 2;
+  const int ntile_img = (int)((span + kTM - 1) / kTM);
+  const long long ntiles = (long long)ntile_img * a.B;
+  if (ntiles > (1ll << 30) || img * (long long)a.B > (1ll << 31)) return FM_ERR_UNSUPPORTED;
+  const int grid = (int)std::min<long long>(ntiles, sms);
+  conv3x3_fwd_tma<<<grid, kResThreads, smem, s>>>(a, ntile_img, (int)ntiles, plane, rlen, r1, tx1,
+                                                  tx2, tr);
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+}  // namespace
+
 extern "C" int fm_conv3x3_fwd_bf16(int B, int H, int W, int cout, const void *x_pad,
                                    const void *w, const float *bias, const void *gate_pad,
                                    const void *resid_pad, int act, void *z_pad_out,
@@ -670,7 +1039,12 @@ extern "C" int fm_conv3x3_fwd_bf16(int B, int H, int W, int cout, const void *x_
   a.act = act;
   a.err = err_device;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  if (cout == 64 && fm::tune_get("conv.kernel", 1) == 1) {
+  const int kern = fm::tune_get("conv.kernel", 1);
+  if (cout == 64 && kern == 2) {
+    const int st = launch_fwd_tma(a, s);
+    if (st != FM_ERR_UNSUPPORTED) return st;
+  }
+  if (cout == 64 && kern >= 1) {
     const int st = launch_fwd_res(a, s);
     if (st != FM_ERR_UNSUPPORTED) return st;
   }

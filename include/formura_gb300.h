@@ -394,9 +394,9 @@ void fm_snapshot_destroy(fm_snapshot *s);
  *   "mhd.xchunk"       x planes per tile of the x-marching kernel (0 = automatic)
  *   "conv.kernel"      fm_conv3x3_fwd_bf16 with 64 output channels: 1 weight-resident
  *                      persistent kernel (default; falls back to 0 when its staged region
- *                      does not fit in shared memory), 0 per-tap gather kernel
- *                      (B*H*W % 128 == 0).  The two accumulate in different orders, so
- *                      their outputs may differ in the last FP32 bits.
+ *                      does not fit in shared memory), 2 the same with its regions and
+ *                      residual rows staged by TMA and its steps chained by mbarriers
+ *                      (falls back to 1), 0 per-tap gather kernel (B*H*W % 128 == 0).
  * fm_tune_clear() restores every default.
  */
 int fm_tune_set(const char *key, int value);

@@ -34,10 +34,11 @@ def bf16r(t):
     return t.to(torch.bfloat16).to(torch.float64)
 
 
-@pytest.fixture(params=[1, 0], ids=["resident", "gather"])
+@pytest.fixture(params=[2, 1, 0], ids=["tma", "resident", "gather"])
 def conv_kernel(request):
-    """Both forward-convolution kernels: the weight-resident shifted-descriptor
-    kernel (default) and the per-tap gather kernel."""
+    """The forward-convolution kernels: the weight-resident shifted-descriptor
+    kernel with TMA staging and mbarrier-chained steps, the same with cp.async
+    staging and a barrier per tile, and the per-tap gather kernel."""
     L = _lib.lib()
     L.fm_tune_set(b"conv.kernel", request.param)
     yield request.param
@@ -72,7 +73,8 @@ def test_conv_fwd_matches_cpu(cuda_device, conv_kernel, B, n):
 
 
 def test_conv_kernels_agree_bitwise(cuda_device):
-    """The two forward kernels issue the same MMA sequence: identical outputs."""
+    """The three forward kernels issue the same MMA sequence: identical outputs
+    (the TMA kernel staging the residual too)."""
     B, n = 2, 64
     g = torch.Generator().manual_seed(5)
     x = pad_periodic(torch.randn(B, n, n, C, generator=g)).to(torch.bfloat16).cuda().contiguous()
@@ -84,7 +86,7 @@ def test_conv_kernels_agree_bitwise(cuda_device):
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     outs = []
     try:
-        for k in (0, 1):
+        for k in (0, 1, 2):
             L.fm_tune_set(b"conv.kernel", k)
             y = torch.zeros(B, n + 2, n + 2, C, dtype=torch.bfloat16, device="cuda")
             z = torch.zeros_like(y)
