@@ -302,8 +302,15 @@ __global__ void __launch_bounds__(128)
             pv[k][q] = pv[k + 1][q];
           }
         if (i + kPF < iend) {
-          int x = (i + kPF) % n;
-          x = x < 0 ? x + n : x;
+          // i + kPF lies in [x0 - T + kPF, x1 + T + kPF): one conditional wrap
+          // for n >= 16 (T <= 8), the integer remainder only for smaller instances
+          int x = i + kPF;
+          if (n >= 16) {
+            x = x < 0 ? x + n : (x >= n ? x - n : x);
+          } else {
+            x %= n;
+            x = x < 0 ? x + n : x;
+          }
           const size_t r = (size_t)x * n;
           pu[kPF - 1][0] = __ldcg(Ui + r + yA);
           pu[kPF - 1][1] = __ldcg(Ui + r + yB);
