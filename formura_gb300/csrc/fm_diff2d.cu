@@ -156,13 +156,32 @@ __global__ void __launch_bounds__(256)
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
       const int x0 = (t / nty) * kDX, y0 = (t % nty) * kDY;
       const int rx = kDX + 2 * k, ry = kDY + 2 * k;
-      for (int q = threadIdx.x; q < rx * ry; q += 256) {
-        const int i = q / ry, j = q - i * ry;
-        int gx = (x0 - k + i) % nx;
-        gx = gx < 0 ? gx + nx : gx;
-        int gy = (y0 - k + j) % ny;
-        gy = gy < 0 ? gy + ny : gy;
-        buf[0][i][j] = __ldcg(src + (size_t)gx * ny + gy);
+      // the staged region spans [x0 - k, x0 + kDX + k): one conditional wrap per
+      // coordinate when the grid is at least that wide, the remainder otherwise
+      const bool near = nx >= kDX + 2 * K && ny >= kDY + 2 * K;
+      {
+        // (i, j) of q = threadIdx.x + 256 m, advanced without a division per cell
+        int i = threadIdx.x / ry, j = threadIdx.x - i * ry;
+        const int di = 256 / ry, dj = 256 - di * ry;
+        for (int q = threadIdx.x; q < rx * ry; q += 256) {
+          int gx = x0 - k + i, gy = y0 - k + j;
+          if (near) {
+            gx = gx < 0 ? gx + nx : (gx >= nx ? gx - nx : gx);
+            gy = gy < 0 ? gy + ny : (gy >= ny ? gy - ny : gy);
+          } else {
+            gx %= nx;
+            gx = gx < 0 ? gx + nx : gx;
+            gy %= ny;
+            gy = gy < 0 ? gy + ny : gy;
+          }
+          buf[0][i][j] = __ldcg(src + (size_t)gx * ny + gy);
+          i += di;
+          j += dj;
+          if (j >= ry) {
+            j -= ry;
+            ++i;
+          }
+        }
       }
       __syncthreads();
       for (int st = 1; st <= k; ++st) {
@@ -170,8 +189,16 @@ __global__ void __launch_bounds__(256)
         const int w = hy - lo;
         const double(*in)[RY] = buf[(st - 1) & 1];
         double(*out)[RY] = buf[st & 1];
+        const int di = 256 / w, dj = 256 - di * w;
+        int qi = threadIdx.x / w, qj = threadIdx.x - qi * w;
         for (int q = threadIdx.x; q < (hx - lo) * w; q += 256) {
-          const int i = lo + q / w, j = lo + q % w;
+          const int i = lo + qi, j = lo + qj;
+          qi += di;
+          qj += dj;
+          if (qj >= w) {
+            qj -= w;
+            ++qi;
+          }
           const double av = in[i][j];
           const double f_1 = half(av - in[i][j - 1]);
           const double f_0 = half(in[i][j + 1] - av);
@@ -187,9 +214,18 @@ __global__ void __launch_bounds__(256)
       }
       const double(*res)[RY] = buf[k & 1];
       const int rows = min(kDX, nx - x0), cols = min(kDY, ny - y0);
-      for (int q = threadIdx.x; q < rows * cols; q += 256) {
-        const int i = q / cols, j = q - i * cols;
-        __stcg(dst + (size_t)(x0 + i) * ny + (y0 + j), res[i + k][j + k]);
+      {
+        int i = threadIdx.x / cols, j = threadIdx.x - i * cols;
+        const int di = 256 / cols, dj = 256 - di * cols;
+        for (int q = threadIdx.x; q < rows * cols; q += 256) {
+          __stcg(dst + (size_t)(x0 + i) * ny + (y0 + j), res[i + k][j + k]);
+          i += di;
+          j += dj;
+          if (j >= cols) {
+            j -= cols;
+            ++i;
+          }
+        }
       }
       __syncthreads();
     }

@@ -125,7 +125,14 @@ __global__ void __launch_bounds__(kE *kE, 1)
         pcv[k] = pcv[k + 1];
       }
       if (i + kPF < x1 + T) {
-        const size_t g = (size_t)wrap_any(i + kPF, nx) * sx + col;
+        // i + kPF lies in [x0 - T + kPF, x1 + T + kPF): one conditional wrap when
+        // nx >= 8 (T <= 4), the integer remainder only for smaller grids
+        int ip = i + kPF;
+        if (nx >= 8)
+          ip = ip < 0 ? ip + nx : (ip >= nx ? ip - nx : ip);
+        else
+          ip = wrap_any(ip, nx);
+        const size_t g = (size_t)ip * sx + col;
         pu[kPF - 1] = __ldg(U + g);
         pv[kPF - 1] = __ldg(V + g);
         pcu[kPF - 1] = __ldg(cU + g);
