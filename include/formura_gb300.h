@@ -385,8 +385,7 @@ void fm_snapshot_destroy(fm_snapshot *s);
  *                      (default), 0 per-point kernel
  *   "mhd.soft"         exact binary64 operations of fm_mhd_forward_f64 on the integer pipes:
  *                      1 (default) scalings, products with constants, divisions, fmax/fmin;
- *                      2 also the products of two fields; 0 FP64 instructions only.  All
- *                      levels give identical bits
+ *                      0 FP64 instructions only.  Both give identical bits
  *   "mhd.stage_xchunk" x planes per tile of the x-marching stage kernel (default 16)
  *   "mhd.finish"       artificial-viscosity kernel of fm_mhd_forward_*: 2 x-marching kernel
  *                      computing each slope and face flux once, all fields per plane
