@@ -153,7 +153,7 @@ def cpu_baseline(seconds: float = 12.0):
     t = time.perf_counter()
     oracle.gs3d_f64(U0, V0, 2, **GS, fast=True)
     per = (time.perf_counter() - t) / 2
-    steps = max(2, min(200, int(seconds / max(per, 1e-6))))
+    steps = max(2, min(2000, int(seconds / max(per, 1e-6))))  # ~`seconds` of CPU work
     t = time.perf_counter()
     oracle.gs3d_f64(U0, V0, steps, **GS, fast=True)
     dt = time.perf_counter() - t
