@@ -29,6 +29,13 @@
 #include <algorithm>
 #include <mutex>
 
+// threads of the weight-resident convolution kernels: 128 per TMEM lane-quarter
+// group, each group taking 64 / (threads / 128) of the 64 output channels
+// (512 measured 0.653 against 0.640 ms per 8 x 512^2 network jump)
+#ifndef FM_CONV_THREADS
+#define FM_CONV_THREADS 256
+#endif
+
 #include "fm_common.cuh"
 #include "fm_tc.cuh"
 #include "fm_tune.h"
@@ -242,7 +249,8 @@ __global__ void __launch_bounds__(128) conv3x3_fwd(ConvArgs a) {
 //   * eight warps: warp w reads TMEM lanes 32*(w%4).. (its 32 positions) and
 //     columns 32*(w/4).. (its 32 channels), so the epilogue, which bounds the
 //     kernel, is spread over twice the warps of the four TMEM lane quarters.
-constexpr int kResThreads = 256;
+constexpr int kResThreads = FM_CONV_THREADS;
+constexpr int kCh = 64 / (kResThreads / 128);  // channels per epilogue warp
 
 __host__ __device__ __forceinline__ int res_region_len(int Wp) { return kTM + 2 * (Wp + 1); }
 
@@ -261,7 +269,7 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
   __shared__ uint32_t s_tmem;
   __shared__ float s_bias[NT];
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lane quarter, channel half
+  const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lane quarter, channel group
   if (tid < NT) s_bias[tid] = a.bias ? a.bias[tid] : 0.0f;
   const int H = a.H, W = a.W, Wp = W + 2;
   const int rlen = res_region_len(Wp);
@@ -334,25 +342,28 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
     const size_t pin = (size_t)b * img + (size_t)j;
     // this thread's 32 channels of the gate and residual inputs (64 B each), loaded
     // as 16-byte vectors before the accumulator is read so that their latency overlaps
-    uint4 gv[4], rv[4];
+    uint4 gv[kCh / 8], rv[kCh / 8];
     if (interior && a.gate) {
-      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * (NT / 2));
+      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * kCh);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) gv[q] = __ldg(g4 + q);
+      for (int q = 0; q < kCh / 8; ++q) gv[q] = __ldg(g4 + q);
     }
     if (interior && a.resid) {  // staged with the region
       const int p = quarter * 32 + (tid & 31);
       const uint4 *r4 = reinterpret_cast<const uint4 *>(sres + (size_t)(it % 3) * kTM * NT * 2);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) rv[q] = r4[p * 8 + ((chalf * 4 + q) ^ (p & 7))];
+      for (int q = 0; q < kCh / 8; ++q) rv[q] = r4[p * 8 + ((chalf * (kCh / 8) + q) ^ (p & 7))];
     }
-    float vv[32];
-    tmem_ld32(tmem + (uint32_t)(acc * 64) + ((uint32_t)(quarter * 32) << 16) +
-                  (uint32_t)(chalf * (NT / 2)),
-              vv);
+    float vv[kCh];
+    const uint32_t tcol = tmem + (uint32_t)(acc * 64) + ((uint32_t)(quarter * 32) << 16) +
+                          (uint32_t)(chalf * kCh);
+    if constexpr (kCh == 32)
+      tmem_ld32(tcol, *reinterpret_cast<float(*)[32]>(vv));
+    else
+      tmem_ld16(tcol, *reinterpret_cast<float(*)[16]>(vv));
 #pragma unroll
-    for (int cc = 0; cc < NT / 2; cc += 16) {
-      const int c0 = chalf * (NT / 2) + cc;
+    for (int cc = 0; cc < kCh; cc += 16) {
+      const int c0 = chalf * kCh + cc;
       float *v = vv + cc;
       if (!interior) continue;
       if (a.bias) {
@@ -493,7 +504,7 @@ __global__ void __launch_bounds__(kResThreads, 1)
   __shared__ uint32_t s_tmem;
   __shared__ float s_bias[NT];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int quarter = warp & 3, chalf = warp >> 2;
+  const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lane quarter, channel group
   if (tid < NT) s_bias[tid] = a.bias ? a.bias[tid] : 0.0f;
   const int H = a.H, W = a.W, Wp = W + 2;
   const long long img = (long long)(H + 2) * Wp;
@@ -592,25 +603,28 @@ __global__ void __launch_bounds__(kResThreads, 1)
     if (xx == 0) pxs[1] = W + 1;
     if (xx == W - 1) pxs[1] = 0;
     const size_t pin = (size_t)b * img + (size_t)j;
-    uint4 gv[4], rv[4];
+    uint4 gv[kCh / 8], rv[kCh / 8];
     if (interior && a.gate) {
-      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * (NT / 2));
+      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * kCh);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) gv[q] = __ldg(g4 + q);
+      for (int q = 0; q < kCh / 8; ++q) gv[q] = __ldg(g4 + q);
     }
     if (interior && a.resid) {
       const int p = quarter * 32 + lane;
       const uint4 *r4 = reinterpret_cast<const uint4 *>(sres + (size_t)bt * kResBytes);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) rv[q] = r4[p * 8 + ((chalf * 4 + q) ^ (p & 7))];
+      for (int q = 0; q < kCh / 8; ++q) rv[q] = r4[p * 8 + ((chalf * (kCh / 8) + q) ^ (p & 7))];
     }
-    float vv[32];
-    tmem_ld32(tmem + (uint32_t)(bt * 64) + ((uint32_t)(quarter * 32) << 16) +
-                  (uint32_t)(chalf * (NT / 2)),
-              vv);
+    float vv[kCh];
+    const uint32_t tcol = tmem + (uint32_t)(bt * 64) + ((uint32_t)(quarter * 32) << 16) +
+                          (uint32_t)(chalf * kCh);
+    if constexpr (kCh == 32)
+      tmem_ld32(tcol, *reinterpret_cast<float(*)[32]>(vv));
+    else
+      tmem_ld16(tcol, *reinterpret_cast<float(*)[16]>(vv));
 #pragma unroll
-    for (int cc = 0; cc < NT / 2; cc += 16) {
-      const int c0 = chalf * (NT / 2) + cc;
+    for (int cc = 0; cc < kCh; cc += 16) {
+      const int c0 = chalf * kCh + cc;
       float *v = vv + cc;
       if (!interior) continue;
       if (a.bias) {
