@@ -214,17 +214,20 @@ __device__ __forceinline__ double div_const_r(double x, double d, double r) {
   return q;
 }
 
-// binary32 counterpart: Markstein's step with r = RN(1/d) in float.
+// binary32 counterpart: Markstein's step with r = RN(1/d) in float, for a
+// positive d.  For |x| in [2^-94, 2^93] no intermediate leaves the normal
+// range and the step gives x/d correctly rounded (with the sign of x); zero
+// returns x; anything else (subnormal, huge, Inf, NaN) takes the IEEE
+// division.  The range test is two float compares on |x|.
 __device__ __forceinline__ float div_const_f(float x, float d, float r) {
-  const unsigned bits = (unsigned)__float_as_int(x);
-  const unsigned ex = (bits >> 23) & 0xffu;
-  const bool zero = (bits << 1) == 0u;
-  const bool normal = (ex - 33u) <= (220u - 33u);
+  const float ax = fabsf(x);
   float q;
-  if (normal || zero) {
+  if (ax >= 0x1p-94f && ax <= 0x1p93f) {
     const float q0 = x * r;
     const float e = fmaf(-q0, d, x);
-    q = copysignf(fmaf(e, r, q0), x);
+    q = fmaf(e, r, q0);
+  } else if (ax == 0.0f) {
+    q = x;
   } else {
     q = __fdiv_rn(x, d);
   }
