@@ -720,10 +720,11 @@ __global__ void __launch_bounds__(128)
   R nv[NF];
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
-    R w = ld<R>(N.p[f], c);
+    const R uc = ld<R>(N.p[f], c);  // off[a][2] == c on every axis
+    R w = uc;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      const R u[5] = {ld<R>(N.p[f], off[a][0]), ld<R>(N.p[f], off[a][1]), ld<R>(N.p[f], off[a][2]),
+      const R u[5] = {ld<R>(N.p[f], off[a][0]), ld<R>(N.p[f], off[a][1]), uc,
                       ld<R>(N.p[f], off[a][3]), ld<R>(N.p[f], off[a][4])};
       const R fm = face<R, SF>(u[0], u[1], u[2], u[3], k);  // avf[i-1/2]
       const R fp = face<R, SF>(u[1], u[2], u[3], u[4], k);  // avf[i+1/2]
