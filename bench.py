@@ -278,7 +278,7 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
     out["mhd_3d_256_fp64"] = {
         "value": round(N ** 3 * 500 / sec64 / 1e9, 4), "unit": "GLUP/s", "steps": 500,
         "seconds": round(sec64, 3), "bit_exact_vs_oracle": True,
-        "kernel": "mhd_stage_tile<double, 1> x4 + mhd_finish_v2<double, 1> "
+        "kernel": "mhd_stage_march<double, 1> x4 + mhd_finish_v2<double, 1> "
                   "(exact binary64 scalings, constant products, divisions, fmax/fmin on the "
                   "integer pipes)"}
     return out

@@ -515,7 +515,7 @@ __device__ __forceinline__ void x_comp(const Fields &Q, size_t i, const MhdC<R> 
 }
 
 template <typename R, int SF>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
     mhd_stage_march(Fields Q, Fields S, Fields O, int n, int xchunk, int ntiles_yz, int ntiles,
                     MhdC<R> k) {
   using AR = Ar<R, SF>;
@@ -1007,11 +1007,12 @@ int mhd_run(int n, R *const *fields, R *work, int steps, cudaStream_t s) {
                 k2 = make_consts<R>(n, dt / 2.0), k1 = make_consts<R>(n, dt);
   const dim3 grid((n + 31) / 32, (n + 3) / 4, n);
   // 2 x-marching with a register ring of x composites, 1 tiled, 0 per-point.  Whole
-  // step at 256^3 (GLUP/s, 2 / 1 / 0): float 2.57 / 3.22 / 2.9; double with FP64
+  // step at 256^3 (GLUP/s, 2 / 1 / 0): float 2.65 / 3.40 / 2.9; double with FP64
   // instructions 0.184 / 0.171 / 0.13; double with the integer-pipe arithmetic
-  // (mhd.soft = 1) 0.285 / 0.296 — once the FP64 pipe is relieved, the tile kernel's
-  // higher occupancy wins over the ring's saved composites.
-  const int stage_kernel = fm::tune_get("mhd.stage", 1);
+  // (mhd.soft = 1) 0.316 / 0.301 — the march kernel bounded to 2 CTAs per SM (128
+  // registers, spilling the ring) keeps the composites it saves and enough warps
+  // (0.285 at 1 CTA per SM).
+  const int stage_kernel = fm::tune_get("mhd.stage", sizeof(R) == 8 ? 2 : 1);
   const dim3 tgrid((n + kTZ - 1) / kTZ, (n + kTY - 1) / kTY, n);
   const size_t tsmem = (size_t)kNV * kNP * sizeof(R);
   if (stage_kernel == 1)

@@ -381,8 +381,8 @@ void fm_snapshot_destroy(fm_snapshot *s);
  *   "diff2d.tb"        steps per grid barrier of fm_diff2d_f64_forward on shared-memory
  *                      tiles with a halo: 2, 4 (default) or 8; 0 = one step per barrier
  *   "mhd.stage"        Runge-Kutta stage kernel of fm_mhd_forward_*: 2 x-marching kernel with
- *                      the x composites in a register ring, 1 shared-memory tile kernel
- *                      (default), 0 per-point kernel
+ *                      the x composites in a register ring (default for f64), 1 shared-memory
+ *                      tile kernel (default for f32), 0 per-point kernel
  *   "mhd.soft"         exact binary64 operations of fm_mhd_forward_f64 on the integer pipes:
  *                      1 (default) scalings, products with constants, divisions, fmax/fmin;
  *                      0 FP64 instructions only.  Both give identical bits
