@@ -281,8 +281,10 @@ constexpr int kTZ = 32, kTY = 8, kH = 2, kRZ = kTZ + 2 * kH, kRY = kTY + 2 * kH;
 constexpr int kNP = kRZ * kRY;  // 432 points
 constexpr int kNV = 20;
 
+// binary32: 5 CTAs per SM (48 registers, 24 bytes spilled) measured 3.51 against 3.43
+// GLUP/s at 4 (64 registers)
 template <typename R, int SF>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1)
     mhd_stage_tile(Fields Q, Fields S, Fields O, int n, MhdC<R> k) {
   using AR = Ar<R, SF>;
   extern __shared__ __align__(16) unsigned char mhd_smem[];
