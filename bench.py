@@ -141,7 +141,7 @@ def read_profile_traffic():
     return None
 
 
-def cpu_baseline(seconds: float = 12.0):
+def cpu_baseline(seconds: float = 18.0):
     """The oracle's speed build (OpenMP, all host cores) on 256^3 x S steps."""
     import numpy as np
 
