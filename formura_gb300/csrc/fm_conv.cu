@@ -229,6 +229,109 @@ __global__ void __launch_bounds__(128) conv3x3_fwd(ConvArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// The epilogue of one tile of the weight-resident kernels, for this warp's 32
+// positions (its TMEM lane quarter) and kCh channels (its channel group):
+//   v = acc + bias (* gelu'(gate)) (+ residual);  z_out <- v;  y <- act(v)
+// stored bf16 into the padded output (with the periodic halo copies of border
+// cells) and/or fp32 unpadded.  `tacc` is the accumulator's TMEM address,
+// `res_rows` the tile's staged residual rows (128-byte swizzled) or null;
+// `valid` false only loads the accumulator (the TMEM load is warp-collective).
+constexpr int kConvThreads = FM_CONV_THREADS;
+constexpr int kCh = 64 / (kConvThreads / 128);  // channels per epilogue warp
+__device__ __forceinline__ void conv_tile_epilogue(const ConvArgs &a, int b, long long j0,
+                                                   uint32_t tacc, const uint8_t *res_rows,
+                                                   const float *s_bias, int quarter, int chalf,
+                                                   bool valid) {
+  constexpr int NT = 64;
+  const int lane = threadIdx.x & 31;
+  const int H = a.H, W = a.W, Wp = W + 2;
+  const long long img = (long long)(H + 2) * Wp;
+  const long long j = j0 + quarter * 32 + lane;
+  const int py = (int)(j / Wp), px = (int)(j % Wp);
+  const bool interior = valid && py >= 1 && py <= H && px >= 1 && px <= W;
+  const int y = py - 1, xx = px - 1;
+  int pys[2] = {py, -1}, pxs[2] = {px, -1};
+  if (y == 0) pys[1] = H + 1;
+  if (y == H - 1) pys[1] = 0;
+  if (xx == 0) pxs[1] = W + 1;
+  if (xx == W - 1) pxs[1] = 0;
+  const size_t pin = (size_t)b * img + (size_t)j;
+  // this thread's channels of the gate and residual inputs, loaded as 16-byte
+  // vectors before the accumulator is read so that their latency overlaps
+  uint4 gv[kCh / 8], rv[kCh / 8];
+  if (interior && a.gate) {
+    const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * kCh);
+#pragma unroll
+    for (int q = 0; q < kCh / 8; ++q) gv[q] = __ldg(g4 + q);
+  }
+  if (interior && res_rows) {
+    const int p = quarter * 32 + lane;
+    const uint4 *r4 = reinterpret_cast<const uint4 *>(res_rows);
+#pragma unroll
+    for (int q = 0; q < kCh / 8; ++q) rv[q] = r4[p * 8 + ((chalf * (kCh / 8) + q) ^ (p & 7))];
+  }
+  float vv[kCh];
+  const uint32_t tcol = tacc + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(chalf * kCh);
+  if constexpr (kCh == 32)
+    tmem_ld32(tcol, *reinterpret_cast<float(*)[32]>(vv));
+  else
+    tmem_ld16(tcol, *reinterpret_cast<float(*)[16]>(vv));
+#pragma unroll
+  for (int cc = 0; cc < kCh; cc += 16) {
+    const int c0 = chalf * kCh + cc;
+    float *v = vv + cc;
+    if (!interior) continue;
+    if (a.bias) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] += s_bias[c0 + i];
+    }
+    if (a.gate) {
+      const bf16 *g = reinterpret_cast<const bf16 *>(&gv[cc / 8]);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] *= gelu_grad(__bfloat162float(g[i]));
+    }
+    if (res_rows) {
+      const bf16 *rr = reinterpret_cast<const bf16 *>(&rv[cc / 8]);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] += __bfloat162float(rr[i]);
+    }
+    __align__(16) bf16 zb[16], yb[16];
+    if (a.z_out) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) zb[i] = __float2bfloat16_rn(v[i]);
+    }
+    if (a.act == 1) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 16; ++i) yb[i] = __float2bfloat16_rn(v[i]);
+#pragma unroll
+    for (int iy = 0; iy < 2; ++iy) {
+      if (pys[iy] < 0) continue;
+#pragma unroll
+      for (int ix = 0; ix < 2; ++ix) {
+        if (pxs[ix] < 0) continue;
+        const size_t q = (((size_t)b * (H + 2) + pys[iy]) * Wp + pxs[ix]) * NT + c0;
+        if (a.z_out) {
+          reinterpret_cast<uint4 *>(a.z_out + q)[0] = reinterpret_cast<const uint4 *>(zb)[0];
+          reinterpret_cast<uint4 *>(a.z_out + q)[1] = reinterpret_cast<const uint4 *>(zb)[1];
+        }
+        if (a.y_out) {
+          reinterpret_cast<uint4 *>(a.y_out + q)[0] = reinterpret_cast<const uint4 *>(yb)[0];
+          reinterpret_cast<uint4 *>(a.y_out + q)[1] = reinterpret_cast<const uint4 *>(yb)[1];
+        }
+      }
+    }
+    if (a.y_f32) {
+      float *dst = a.y_f32 + (((size_t)b * H + y) * W + xx) * NT + c0;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) dst[i] = v[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // conv3x3_fwd_res: the persistent, weight-resident form for cout = 64.
 //
 // Output positions are indexed in the FLATTENED PADDED image,
@@ -249,8 +352,7 @@ __global__ void __launch_bounds__(128) conv3x3_fwd(ConvArgs a) {
 //   * eight warps: warp w reads TMEM lanes 32*(w%4).. (its 32 positions) and
 //     columns 32*(w/4).. (its 32 channels), so the epilogue, which bounds the
 //     kernel, is spread over twice the warps of the four TMEM lane quarters.
-constexpr int kResThreads = FM_CONV_THREADS;
-constexpr int kCh = 64 / (kResThreads / 128);  // channels per epilogue warp
+constexpr int kResThreads = kConvThreads;
 
 __host__ __device__ __forceinline__ int res_region_len(int Wp) { return kTM + 2 * (Wp + 1); }
 
@@ -329,91 +431,10 @@ __global__ void __launch_bounds__(kResThreads, 1) conv3x3_fwd_res(ConvArgs a, in
 
   auto epilogue = [&](int it, int acc) {
     const int tile = blockIdx.x + it * gridDim.x;
-    const int b = tile / ntile_img, tl = tile % ntile_img;
-    const long long j = (long long)(Wp + 1) + (long long)tl * kTM + quarter * 32 + (tid & 31);
-    const int py = (int)(j / Wp), px = (int)(j % Wp);
-    const bool interior = py >= 1 && py <= H && px >= 1 && px <= W;
-    const int y = py - 1, xx = px - 1;
-    int pys[2] = {py, -1}, pxs[2] = {px, -1};
-    if (y == 0) pys[1] = H + 1;
-    if (y == H - 1) pys[1] = 0;
-    if (xx == 0) pxs[1] = W + 1;
-    if (xx == W - 1) pxs[1] = 0;
-    const size_t pin = (size_t)b * img + (size_t)j;
-    // this thread's 32 channels of the gate and residual inputs (64 B each), loaded
-    // as 16-byte vectors before the accumulator is read so that their latency overlaps
-    uint4 gv[kCh / 8], rv[kCh / 8];
-    if (interior && a.gate) {
-      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * kCh);
-#pragma unroll
-      for (int q = 0; q < kCh / 8; ++q) gv[q] = __ldg(g4 + q);
-    }
-    if (interior && a.resid) {  // staged with the region
-      const int p = quarter * 32 + (tid & 31);
-      const uint4 *r4 = reinterpret_cast<const uint4 *>(sres + (size_t)(it % 3) * kTM * NT * 2);
-#pragma unroll
-      for (int q = 0; q < kCh / 8; ++q) rv[q] = r4[p * 8 + ((chalf * (kCh / 8) + q) ^ (p & 7))];
-    }
-    float vv[kCh];
-    const uint32_t tcol = tmem + (uint32_t)(acc * 64) + ((uint32_t)(quarter * 32) << 16) +
-                          (uint32_t)(chalf * kCh);
-    if constexpr (kCh == 32)
-      tmem_ld32(tcol, *reinterpret_cast<float(*)[32]>(vv));
-    else
-      tmem_ld16(tcol, *reinterpret_cast<float(*)[16]>(vv));
-#pragma unroll
-    for (int cc = 0; cc < kCh; cc += 16) {
-      const int c0 = chalf * kCh + cc;
-      float *v = vv + cc;
-      if (!interior) continue;
-      if (a.bias) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] += s_bias[c0 + i];
-      }
-      if (a.gate) {
-        const bf16 *g = reinterpret_cast<const bf16 *>(&gv[cc / 8]);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] *= gelu_grad(__bfloat162float(g[i]));
-      }
-      if (a.resid) {
-        const bf16 *rr = reinterpret_cast<const bf16 *>(&rv[cc / 8]);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] += __bfloat162float(rr[i]);
-      }
-      __align__(16) bf16 zb[16], yb[16];
-      if (a.z_out) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) zb[i] = __float2bfloat16_rn(v[i]);
-      }
-      if (a.act == 1) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
-      }
-#pragma unroll
-      for (int i = 0; i < 16; ++i) yb[i] = __float2bfloat16_rn(v[i]);
-#pragma unroll
-      for (int iy = 0; iy < 2; ++iy) {
-        if (pys[iy] < 0) continue;
-#pragma unroll
-        for (int ix = 0; ix < 2; ++ix) {
-          if (pxs[ix] < 0) continue;
-          const size_t q = (((size_t)b * (H + 2) + pys[iy]) * Wp + pxs[ix]) * NT + c0;
-          if (a.z_out) {
-            reinterpret_cast<uint4 *>(a.z_out + q)[0] = reinterpret_cast<const uint4 *>(zb)[0];
-            reinterpret_cast<uint4 *>(a.z_out + q)[1] = reinterpret_cast<const uint4 *>(zb)[1];
-          }
-          if (a.y_out) {
-            reinterpret_cast<uint4 *>(a.y_out + q)[0] = reinterpret_cast<const uint4 *>(yb)[0];
-            reinterpret_cast<uint4 *>(a.y_out + q)[1] = reinterpret_cast<const uint4 *>(yb)[1];
-          }
-        }
-      }
-      if (a.y_f32) {
-        float *dst = a.y_f32 + (((size_t)b * H + y) * W + xx) * NT + c0;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) dst[i] = v[i];
-      }
-    }
+    const long long j0 = (long long)(Wp + 1) + (long long)(tile % ntile_img) * kTM;
+    conv_tile_epilogue(a, tile / ntile_img, j0, tmem + (uint32_t)(acc * 64),
+                       a.resid ? sres + (size_t)(it % 3) * kTM * NT * 2 : nullptr, s_bias, quarter,
+                       chalf, true);
   };
 
   const int my_tiles = ntiles > (int)blockIdx.x ? (ntiles - 1 - (int)blockIdx.x) / gridDim.x + 1 : 0;
@@ -506,8 +527,7 @@ __global__ void __launch_bounds__(kResThreads, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lane quarter, channel group
   if (tid < NT) s_bias[tid] = a.bias ? a.bias[tid] : 0.0f;
-  const int H = a.H, W = a.W, Wp = W + 2;
-  const long long img = (long long)(H + 2) * Wp;
+  const int Wp = a.W + 2;
   if (warp == 0) tmem_alloc(&s_tmem, 128);
   if (tid == 0) {
     for (int b = 0; b < 2; ++b) {
@@ -593,88 +613,8 @@ __global__ void __launch_bounds__(kResThreads, 1)
     int b;
     long long j0;
     tile_pos(t, b, j0);
-    const long long j = j0 + quarter * 32 + lane;
-    const int py = (int)(j / Wp), px = (int)(j % Wp);
-    const bool interior = ok && py >= 1 && py <= H && px >= 1 && px <= W;
-    const int y = py - 1, xx = px - 1;
-    int pys[2] = {py, -1}, pxs[2] = {px, -1};
-    if (y == 0) pys[1] = H + 1;
-    if (y == H - 1) pys[1] = 0;
-    if (xx == 0) pxs[1] = W + 1;
-    if (xx == W - 1) pxs[1] = 0;
-    const size_t pin = (size_t)b * img + (size_t)j;
-    uint4 gv[kCh / 8], rv[kCh / 8];
-    if (interior && a.gate) {
-      const uint4 *g4 = reinterpret_cast<const uint4 *>(a.gate + pin * NT + chalf * kCh);
-#pragma unroll
-      for (int q = 0; q < kCh / 8; ++q) gv[q] = __ldg(g4 + q);
-    }
-    if (interior && a.resid) {
-      const int p = quarter * 32 + lane;
-      const uint4 *r4 = reinterpret_cast<const uint4 *>(sres + (size_t)bt * kResBytes);
-#pragma unroll
-      for (int q = 0; q < kCh / 8; ++q) rv[q] = r4[p * 8 + ((chalf * (kCh / 8) + q) ^ (p & 7))];
-    }
-    float vv[kCh];
-    const uint32_t tcol = tmem + (uint32_t)(bt * 64) + ((uint32_t)(quarter * 32) << 16) +
-                          (uint32_t)(chalf * kCh);
-    if constexpr (kCh == 32)
-      tmem_ld32(tcol, *reinterpret_cast<float(*)[32]>(vv));
-    else
-      tmem_ld16(tcol, *reinterpret_cast<float(*)[16]>(vv));
-#pragma unroll
-    for (int cc = 0; cc < kCh; cc += 16) {
-      const int c0 = chalf * kCh + cc;
-      float *v = vv + cc;
-      if (!interior) continue;
-      if (a.bias) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] += s_bias[c0 + i];
-      }
-      if (a.gate) {
-        const bf16 *g = reinterpret_cast<const bf16 *>(&gv[cc / 8]);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] *= gelu_grad(__bfloat162float(g[i]));
-      }
-      if (a.resid) {
-        const bf16 *rr = reinterpret_cast<const bf16 *>(&rv[cc / 8]);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] += __bfloat162float(rr[i]);
-      }
-      __align__(16) bf16 zb[16], yb[16];
-      if (a.z_out) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) zb[i] = __float2bfloat16_rn(v[i]);
-      }
-      if (a.act == 1) {
-#pragma unroll
-        for (int i = 0; i < 16; ++i) v[i] = gelu(v[i]);
-      }
-#pragma unroll
-      for (int i = 0; i < 16; ++i) yb[i] = __float2bfloat16_rn(v[i]);
-#pragma unroll
-      for (int iy = 0; iy < 2; ++iy) {
-        if (pys[iy] < 0) continue;
-#pragma unroll
-        for (int ix = 0; ix < 2; ++ix) {
-          if (pxs[ix] < 0) continue;
-          const size_t q = (((size_t)b * (H + 2) + pys[iy]) * Wp + pxs[ix]) * NT + c0;
-          if (a.z_out) {
-            reinterpret_cast<uint4 *>(a.z_out + q)[0] = reinterpret_cast<const uint4 *>(zb)[0];
-            reinterpret_cast<uint4 *>(a.z_out + q)[1] = reinterpret_cast<const uint4 *>(zb)[1];
-          }
-          if (a.y_out) {
-            reinterpret_cast<uint4 *>(a.y_out + q)[0] = reinterpret_cast<const uint4 *>(yb)[0];
-            reinterpret_cast<uint4 *>(a.y_out + q)[1] = reinterpret_cast<const uint4 *>(yb)[1];
-          }
-        }
-      }
-      if (a.y_f32) {
-        float *dst = a.y_f32 + (((size_t)b * H + y) * W + xx) * NT + c0;
-#pragma unroll
-        for (int i = 0; i < 16; ++i) dst[i] = v[i];
-      }
-    }
+    conv_tile_epilogue(a, b, j0, tmem + (uint32_t)(bt * 64),
+                       a.resid ? sres + (size_t)bt * kResBytes : nullptr, s_bias, quarter, chalf, ok);
     // this warp is done with accumulator bt and residual buffer bt
     fence_before_sync();
     __syncwarp();
