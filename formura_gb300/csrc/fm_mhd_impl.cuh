@@ -209,6 +209,63 @@ __device__ __forceinline__ AxisQ<R> axis_q(const Fields &Q, size_t i, int a, con
   return q;
 }
 
+// the tile of the staged stage kernels: 32 (z) x 8 (y) cells and a 2-cell halo
+constexpr int kTZ = 32, kTY = 8, kH = 2, kRZ = kTZ + 2 * kH, kRY = kTY + 2 * kH;
+constexpr int kNP = kRZ * kRY;  // 432 points
+constexpr int kNV = 20;
+
+// One point of the staged region of the tiled stage kernels: the 20 y/z-derivative
+// quantities (d v_y, d v_z, v_y, v_z, P, B_y B_c, B_z B_c, E_cy, E_cz, s, B_y, B_z)
+// of point i, stored at index pt of each quantity's plane in shared memory.
+template <typename R, int SF>
+__device__ __forceinline__ void stage_point(const Fields &Q, size_t i, const MhdC<R> &k, R *sv,
+                                            int pt) {
+  using AR = Ar<R, SF>;
+  const R dn = ld<R>(Q.p[0], i);
+  const R v[3] = {ld<R>(Q.p[1], i), ld<R>(Q.p[2], i), ld<R>(Q.p[3], i)};
+  const R B[3] = {ld<R>(Q.p[4], i), ld<R>(Q.p[5], i), ld<R>(Q.p[6], i)};
+  const R s = ld<R>(Q.p[7], i), Psi = ld<R>(Q.p[8], i);
+  const R d = k.dens0 + dn;
+  const R b2 = (AR::mul(B[0], B[0]) + AR::mul(B[1], B[1])) + AR::mul(B[2], B[2]);
+  sv[0 * kNP + pt] = AR::mul(d, v[1]);
+  sv[1 * kNP + pt] = AR::mul(d, v[2]);
+  sv[2 * kNP + pt] = v[1];
+  sv[3 * kNP + pt] = v[2];
+  sv[4 * kNP + pt] = (AR::cmul(k.dp_ddens, k.dp_ddens_s, d) + AR::cmul(k.dp_ds, k.dp_ds_s, s)) + AR::cmul(k.c8, k.c8s, b2);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    sv[(5 + c) * kNP + pt] = AR::mul(B[1], B[c]);
+    sv[(8 + c) * kNP + pt] = AR::mul(B[2], B[c]);
+    sv[(11 + c) * kNP + pt] = AR::zp_add(Psi, AR::mul(v[c], B[1])) - AR::mul(v[1], B[c]);
+    sv[(14 + c) * kNP + pt] = AR::zp_add(Psi, AR::mul(v[c], B[2])) - AR::mul(v[2], B[c]);
+  }
+  sv[17 * kNP + pt] = s;
+  sv[18 * kNP + pt] = B[1];
+  sv[19 * kNP + pt] = B[2];
+}
+
+// f = ddt_sys (3d-mhd-rk4.fmr:83-101) from the 33 derivatives, the velocity, Psi
+// and the prepared divisor dens (the expressions and order of the generated code).
+template <typename R, int SF>
+__device__ __forceinline__ void assemble_f(const R (&dm)[3], const R (&dv)[3], const R (&dP)[3],
+                                           const R (&dBB)[3][3], const R (&dE)[3][3],
+                                           const R (&ds)[3], const R (&dB)[3], const R (&v)[3],
+                                           R Psi, const typename Ar<R, SF>::Den &dd,
+                                           const MhdC<R> &k, R (&f)[NF]) {
+  using AR = Ar<R, SF>;
+  f[0] = -(((dm[0]) + (dm[1])) + (dm[2]));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const R A = (AR::mul(v[0], dv[i]) + AR::mul(v[1], dv[i])) + AR::mul(v[2], dv[i]);
+    const R Y = ((dBB[0][i]) + (dBB[1][i])) + (dBB[2][i]);
+    f[1 + i] = ((-A) - AR::div(dP[i], dd)) + AR::div(AR::cmul(k.c4, k.c4s, Y), dd);
+    f[4 + i] = ((dE[i][0]) + (dE[i][1])) + (dE[i][2]);
+  }
+  f[7] = (AR::mul(v[0], ds[0]) + AR::mul(v[1], ds[1])) + AR::mul(v[2], ds[2]);
+  const R divB = ((dB[0]) + (dB[1])) + (dB[2]);
+  f[8] = (-AR::cmul(k.c_h2, k.c_h2s, divB)) - AR::cmul(k.ch2_cp2, k.ch2_cp2s, Psi);
+}
+
 template <typename R, int SF>
 __global__ void __launch_bounds__(128)
     mhd_stage(Fields Q, Fields S, Fields O, int n, MhdC<R> k) {
@@ -251,17 +308,7 @@ __global__ void __launch_bounds__(128)
   const R dens = k.dens0 + dn;
   const typename AR::Den dd = AR::prep(dens);
   R f[NF];
-  f[0] = -(((dm[0]) + (dm[1])) + (dm[2]));
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const R A = (AR::mul(v[0], dv[i]) + AR::mul(v[1], dv[i])) + AR::mul(v[2], dv[i]);
-    const R Y = ((dBB[0][i]) + (dBB[1][i])) + (dBB[2][i]);
-    f[1 + i] = ((-A) - AR::div(dP[i], dd)) + AR::div(AR::cmul(k.c4, k.c4s, Y), dd);
-    f[4 + i] = ((dE[i][0]) + (dE[i][1])) + (dE[i][2]);
-  }
-  f[7] = (AR::mul(v[0], ds[0]) + AR::mul(v[1], ds[1])) + AR::mul(v[2], ds[2]);
-  const R divB = ((dB[0]) + (dB[1])) + (dB[2]);
-  f[8] = (-AR::cmul(k.c_h2, k.c_h2s, divB)) - AR::cmul(k.ch2_cp2, k.ch2_cp2s, Psi);
+  assemble_f<R, SF>(dm, dv, dP, dBB, dE, ds, dB, v, Psi, dd, k, f);
 #pragma unroll
   for (int q = 0; q < NF; ++q)
     reinterpret_cast<R *>(O.p[q])[c] = ld<R>(S.p[q], c) + AR::cmul(k.dt_c, k.dts, f[q]);
@@ -277,9 +324,6 @@ __global__ void __launch_bounds__(128)
 // evaluate the composites at x-2 .. x+2 as mhd_stage does.  Every value is
 // the same IEEE expression as in axis_q, so results are bit-identical with
 // mhd_stage (and, for R = double, with the all-FP64 program).
-constexpr int kTZ = 32, kTY = 8, kH = 2, kRZ = kTZ + 2 * kH, kRY = kTY + 2 * kH;
-constexpr int kNP = kRZ * kRY;  // 432 points
-constexpr int kNV = 20;
 
 // binary32: 5 CTAs per SM (48 registers, 24 bytes spilled) measured 3.51 against 3.43
 // GLUP/s at 4 (64 registers)
@@ -306,27 +350,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1)
       gz = gz < 0 ? gz + n : gz;
     }
     const size_t i = (size_t)x * sx + (size_t)gy * sy + gz;
-    const R dn = ld<R>(Q.p[0], i);
-    const R v[3] = {ld<R>(Q.p[1], i), ld<R>(Q.p[2], i), ld<R>(Q.p[3], i)};
-    const R B[3] = {ld<R>(Q.p[4], i), ld<R>(Q.p[5], i), ld<R>(Q.p[6], i)};
-    const R s = ld<R>(Q.p[7], i), Psi = ld<R>(Q.p[8], i);
-    const R d = k.dens0 + dn;
-    const R b2 = (AR::mul(B[0], B[0]) + AR::mul(B[1], B[1])) + AR::mul(B[2], B[2]);
-    sv[0 * kNP + pt] = AR::mul(d, v[1]);
-    sv[1 * kNP + pt] = AR::mul(d, v[2]);
-    sv[2 * kNP + pt] = v[1];
-    sv[3 * kNP + pt] = v[2];
-    sv[4 * kNP + pt] = (AR::cmul(k.dp_ddens, k.dp_ddens_s, d) + AR::cmul(k.dp_ds, k.dp_ds_s, s)) + AR::cmul(k.c8, k.c8s, b2);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      sv[(5 + c) * kNP + pt] = AR::mul(B[1], B[c]);
-      sv[(8 + c) * kNP + pt] = AR::mul(B[2], B[c]);
-      sv[(11 + c) * kNP + pt] = AR::zp_add(Psi, AR::mul(v[c], B[1])) - AR::mul(v[1], B[c]);
-      sv[(14 + c) * kNP + pt] = AR::zp_add(Psi, AR::mul(v[c], B[2])) - AR::mul(v[2], B[c]);
-    }
-    sv[17 * kNP + pt] = s;
-    sv[18 * kNP + pt] = B[1];
-    sv[19 * kNP + pt] = B[2];
+    stage_point<R, SF>(Q, i, k, sv, pt);
   }
   __syncthreads();
   const int y = y0 + ty, z = z0 + tz;
@@ -437,17 +461,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 5 : 1)
     const R dens = k.dens0 + dn;
     const typename AR::Den dd = AR::prep(dens);
     R f[NF];
-    f[0] = -(((dm[0]) + (dm[1])) + (dm[2]));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const R A = (AR::mul(v[0], dv[i]) + AR::mul(v[1], dv[i])) + AR::mul(v[2], dv[i]);
-      const R Y = ((dBB[0][i]) + (dBB[1][i])) + (dBB[2][i]);
-      f[1 + i] = ((-A) - AR::div(dP[i], dd)) + AR::div(AR::cmul(k.c4, k.c4s, Y), dd);
-      f[4 + i] = ((dE[i][0]) + (dE[i][1])) + (dE[i][2]);
-    }
-    f[7] = (AR::mul(v[0], ds[0]) + AR::mul(v[1], ds[1])) + AR::mul(v[2], ds[2]);
-    const R divB = ((dB[0]) + (dB[1])) + (dB[2]);
-    f[8] = (-AR::cmul(k.c_h2, k.c_h2s, divB)) - AR::cmul(k.ch2_cp2, k.ch2_cp2s, Psi);
+    assemble_f<R, SF>(dm, dv, dP, dBB, dE, ds, dB, v, Psi, dd, k, f);
 #pragma unroll
     for (int q = 0; q < NF; ++q)
       reinterpret_cast<R *>(O.p[q])[c] = ld<R>(S.p[q], c) + AR::cmul(k.dt_c, k.dts, f[q]);
@@ -565,27 +579,7 @@ __global__ void __launch_bounds__(256, 2)
         if (spt[j] < 0) continue;
         const int pt = spt[j];
         const size_t i = px + soff[j];
-        const R dn = ld<R>(Q.p[0], i);
-        const R v[3] = {ld<R>(Q.p[1], i), ld<R>(Q.p[2], i), ld<R>(Q.p[3], i)};
-        const R B[3] = {ld<R>(Q.p[4], i), ld<R>(Q.p[5], i), ld<R>(Q.p[6], i)};
-        const R s = ld<R>(Q.p[7], i), Psi = ld<R>(Q.p[8], i);
-        const R d = k.dens0 + dn;
-        const R b2 = (AR::mul(B[0], B[0]) + AR::mul(B[1], B[1])) + AR::mul(B[2], B[2]);
-        sv[0 * kNP + pt] = AR::mul(d, v[1]);
-        sv[1 * kNP + pt] = AR::mul(d, v[2]);
-        sv[2 * kNP + pt] = v[1];
-        sv[3 * kNP + pt] = v[2];
-        sv[4 * kNP + pt] = (AR::cmul(k.dp_ddens, k.dp_ddens_s, d) + AR::cmul(k.dp_ds, k.dp_ds_s, s)) + AR::cmul(k.c8, k.c8s, b2);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          sv[(5 + c) * kNP + pt] = AR::mul(B[1], B[c]);
-          sv[(8 + c) * kNP + pt] = AR::mul(B[2], B[c]);
-          sv[(11 + c) * kNP + pt] = AR::zp_add(Psi, AR::mul(v[c], B[1])) - AR::mul(v[1], B[c]);
-          sv[(14 + c) * kNP + pt] = AR::zp_add(Psi, AR::mul(v[c], B[2])) - AR::mul(v[2], B[c]);
-        }
-        sv[17 * kNP + pt] = s;
-        sv[18 * kNP + pt] = B[1];
-        sv[19 * kNP + pt] = B[2];
+        stage_point<R, SF>(Q, i, k, sv, pt);
       }
       __syncthreads();
       if (own) {
@@ -640,17 +634,7 @@ __global__ void __launch_bounds__(256, 2)
         const R dens = k.dens0 + dn;
         const typename AR::Den dd = AR::prep(dens);
         R f[NF];
-        f[0] = -(((dm[0]) + (dm[1])) + (dm[2]));
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const R A = (AR::mul(v[0], dv[i]) + AR::mul(v[1], dv[i])) + AR::mul(v[2], dv[i]);
-          const R Y = ((dBB[0][i]) + (dBB[1][i])) + (dBB[2][i]);
-          f[1 + i] = ((-A) - AR::div(dP[i], dd)) + AR::div(AR::cmul(k.c4, k.c4s, Y), dd);
-          f[4 + i] = ((dE[i][0]) + (dE[i][1])) + (dE[i][2]);
-        }
-        f[7] = (AR::mul(v[0], ds[0]) + AR::mul(v[1], ds[1])) + AR::mul(v[2], ds[2]);
-        const R divB = ((dB[0]) + (dB[1])) + (dB[2]);
-        f[8] = (-AR::cmul(k.c_h2, k.c_h2s, divB)) - AR::cmul(k.ch2_cp2, k.ch2_cp2s, Psi);
+        assemble_f<R, SF>(dm, dv, dP, dBB, dE, ds, dB, v, Psi, dd, k, f);
 #pragma unroll
         for (int q = 0; q < NF; ++q)
           reinterpret_cast<R *>(O.p[q])[c] = ld<R>(S.p[q], c) + AR::cmul(k.dt_c, k.dts, f[q]);
