@@ -39,7 +39,7 @@ WORKLOAD = "gray_scott_3d"
 N = 256
 GS = dict(F=0.04, k=0.06, Du=2e-5, Dv=1e-5, dt=0.5, dx=0.01)
 # Algorithmic work per lattice-site update of the pearson-3d DAG (counted on the
-# constant-folded OM graph, division = 1 flop; see DESIGN.md): 46 flops, 32 B.
+# constant-folded OM graph, division = 1 flop): 46 flops, 32 B.
 FLOPS_PER_LUP = 46
 BYTES_PER_LUP = 32
 

@@ -1,6 +1,6 @@
 // fm_reduce.cu — deterministic FP64 sums for the conserved-total checks
 // (mass and energy drift), and FP64/FP32 pipe probes used to measure the
-// arithmetic roofline the stencil kernels are judged against.
+// arithmetic roofline the stencil kernels are measured against.
 //
 // The sum is a fixed two-level tree whose shape depends only on n: stage 1
 // gives each of G blocks a contiguous chunk (thread-strided, then a shared

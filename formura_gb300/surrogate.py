@@ -18,7 +18,7 @@ weight gradients on the tensor cores (the data gradient is the forward
 convolution with flipped, transposed weights; the weight gradient a split-K
 GEMM over pixels), Adam on FP32 master weights.
 
-The plain stencil remains the fallback and judge: see
+The plain stencil remains the fallback and the reference for its error: see
 :func:`formura_gb300.surrogate_run.run_with_surrogate`.
 """
 from __future__ import annotations

@@ -1,5 +1,5 @@
 """Training data, training loop and the surrogate-accelerated run with the
-plain stencil as fallback and judge.
+plain stencil as fallback and as the reference for its error.
 
 Training pairs come from the batched solver (the uneven-ensemble kernel of
 fm_gs2d.cu): a pool of periodic 2D Gray-Scott instances with F ~ U[0.02, 0.06],

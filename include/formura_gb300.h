@@ -120,7 +120,7 @@ int fm_gs3d_f32k_forward(int nx, int ny, int nz, float *U, float *V, float *cU,
  * regions of src/Formura/MPICxx/Cut.hs:240-281, as on-chip pipelines).
  * Arithmetic is the binary32 "fast form" (per-axis sums of differences,
  * explicit FMAs, constants Du/dx^2, Dv/dx^2, F+k rounded once to float):
- * results are bit-identical for every tb and are judged by their error against
+ * results are bit-identical for every tb and are scored by their error against
  * the FP64 run.  Same arrays as fm_gs3d_f32k_forward; any nx, ny, nz >= 1.
  */
 int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *V,
@@ -224,7 +224,7 @@ int fm_tc_gemm_bf16(int M, int N, int K, const void *A, const void *B, float *C,
 /*
  * No counterpart in the reference (a new form: a convolutional neural operator
  * that jumps 16 steps of the pearson-2d Gray-Scott program, with the plain
- * stencil as its fallback and judge).
+ * stencil as its fallback and as the reference for its error).
  *
  * Latent tensors are NHWC bf16 with a one-pixel periodic halo,
  * [B][H+2][W+2][64]; weights [cout][9][64] bf16 (tap t = (dy+1)*3 + dx+1).

@@ -67,7 +67,7 @@ void fo_gs3d_run_f32_kahan(int nx, int ny, int nz, float *U, float *V,
  *   dV = fmaf(cv, lapV, fmaf(-Fk, V, uvv))      cv = (float)(Dv/(dx*dx)), Fk = (float)(F+k)
  *   Kahan per field: y = fmaf(dt, dW, -cW); t = W + y; cW = (t - W) - y; W = t
  * It is not the generated DAG (that is fo_gs3d_run_f32_kahan); its accuracy is
- * judged against fo_gs3d_run_f64. */
+ * measured against fo_gs3d_run_f64. */
 void fo_gs3d_run_f32k_fast(int nx, int ny, int nz, float *U, float *V,
                            float *cU, float *cV, int steps, double F, double k,
                            double Du, double Dv, double dt, double dx);

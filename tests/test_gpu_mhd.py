@@ -1,7 +1,7 @@
 """GPU parity of the 3D MHD kernels (examples/3d-mhd-rk4.fmr form).
 
 FP64 path: bit-exact against the CPU oracle's restatement of the DAG.  FP32
-path (binary32 bulk, FP64 energy update): judged by its error against the
+path (binary32 bulk, FP64 energy update): scored by its error against the
 FP64 oracle, as the precision form asks; tolerance written below.
 """
 import numpy as np

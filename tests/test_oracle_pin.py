@@ -1,8 +1,7 @@
 """The oracle against the reference's own generated C, and its regression vectors.
 
 examples-generated/pearson.c is the only generated C the reference ships for a
-Jacobi stencil (SURVEY: the reference's tests hold no numerical golden
-vectors).  Its outputs, recorded in tests/golden/pearson_ref.json by
+Jacobi stencil (the reference's tests hold no numerical golden vectors).  Its outputs, recorded in tests/golden/pearson_ref.json by
 tests/golden/make_golden.py, pin the oracle's 2D Gray-Scott step bit for bit.
 """
 import hashlib
