@@ -152,7 +152,7 @@ def test_mul_matches_ieee(lib):
     assert ok, (xs[bad[:5]], ys[bad[:5]], got[bad[:5]], want[bad[:5]])
 
 
-@pytest.mark.parametrize("k", [-1, 1, 3, -4])
+@pytest.mark.parametrize("k", [-1, 1, 3, -4, 10, -10, 62, -62, 0])
 def test_scale_pow2_matches_ieee(lib, k):
     rng = np.random.default_rng(k + 10)
     x = np.concatenate([random_doubles(rng, 200_000), random_doubles(rng, 50_000, -1022, 1023),
