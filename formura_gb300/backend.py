@@ -76,6 +76,9 @@ class Program:
     # form "fmr": cells per thread along axis 0 in the generated kernels (values shared by
     # consecutive cells carried in registers); 0 = automatic (up to 16, keeping ~150k threads)
     march_chunk: int = 0
+    # form "fmr": cells per thread along axis 1 (2 = two adjacent cells sharing values, 1 = one,
+    # 0 = automatic per level); a pair needs 3+ axes and an even extent of axis 1
+    march_pair: int = 0
 
     @property
     def dim(self) -> int:
@@ -276,7 +279,7 @@ def _fmr_parts(p: Program):
     from .fmr.emit_cuda import emit_kernels
 
     mmp = p.compiled()
-    kern, levels = emit_kernels(mmp, march_chunk=p.march_chunk)
+    kern, levels = emit_kernels(mmp, march_chunk=p.march_chunk, march_pair=p.march_pair)
     states = [n for n, _ in mmp.state]
     sidx = {n: i for i, n in enumerate(states)}
     arrays = sorted(mmp.arrays.values(), key=lambda a: a.node)

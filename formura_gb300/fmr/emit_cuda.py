@@ -73,111 +73,125 @@ def _pow2_exponent(v):
     return e - 1
 
 
-CMP_SOFT = {"<": "fm::soft::lt_s(a%d, a%d)", "<=": "fm::soft::le_s(a%d, a%d)",
-            ">": "fm::soft::lt_s(a%d, a%d)", ">=": "fm::soft::le_s(a%d, a%d)",
-            "==": "fm::soft::eq_s(a%d, a%d)", "!=": "!fm::soft::eq_s(a%d, a%d)"}
+CMP_SOFT = {"<": "fm::soft::lt_s(%s, %s)", "<=": "fm::soft::le_s(%s, %s)",
+            ">": "fm::soft::lt_s(%s, %s)", ">=": "fm::soft::le_s(%s, %s)",
+            "==": "fm::soft::eq_s(%s, %s)", "!=": "!fm::soft::eq_s(%s, %s)"}
 
 
-def _wrap_name(ax: int, c: int) -> str:
+def _wrap_name(ax: int, c: int, lane: str = "") -> str:
+    """Variable holding the wrapped coordinate x_ax + c; `lane` "b" names the
+    second cell of a thread's pair along axis 1."""
+    base = AXVARS[ax] + (lane if ax == 1 else "")
     if c == 0:
-        return AXVARS[ax]
-    return "%s_%s%d" % (AXVARS[ax], "p" if c > 0 else "m", abs(c))
+        return base
+    return "%s_%s%d" % (base, "p" if c > 0 else "m", abs(c))
 
 
 class LevelEmitter:
     def __init__(self, mmp: MM.MMProgram, level: MM.Level, li: int, soft_div: bool,
-                 soft_mul: bool, soft_cmp: bool = True, march_chunk: int = 0):
+                 soft_mul: bool, soft_cmp: bool = True, march_chunk: int = 0,
+                 march_pair: int = 0):
         self.mmp, self.level, self.li = mmp, level, li
         self.soft_div, self.soft_mul, self.soft_cmp = soft_div, soft_mul, soft_cmp
-        self.march_chunk = march_chunk
+        self.march_chunk, self.march_pair = march_chunk, march_pair
         self.shape = mmp.shape
         self.dim = mmp.dim
 
-    def idx_expr(self, cursor: Sequence[int]) -> str:
-        parts = [_wrap_name(a, c) for a, c in enumerate(cursor)]
+    def idx_expr(self, cursor: Sequence[int], lane: str = "") -> str:
+        parts = [_wrap_name(a, c, lane) for a, c in enumerate(cursor)]
         e = "(size_t)%s" % parts[0]
         for a in range(1, self.dim):
             e = "(%s * %d + %s)" % (e, self.shape[a], parts[a])
         return e
 
-    def _emit_ops(self, which, alias: Dict[int, str], w, ind: str) -> None:
+    def _emit_ops(self, which, alias: Dict[int, str], w, ind: str, pfx: str = "a",
+                  lane: str = "", ext_prep: Optional[Dict[int, str]] = None) -> Dict[int, str]:
         """C statements for the micro ops in `which` (topological order), one
-        `const` temporary a<i> each; an op in `alias` is bound to that C
-        expression (a value carried from the previous cell) instead."""
+        `const` temporary <pfx><i> each; an op in `alias` is bound to that C
+        expression (a value carried from the previous cell, or the other cell
+        of the pair) instead.  `lane` selects the axis-1 coordinate variables
+        of the cell; `ext_prep` names run-time reciprocals prepared already
+        (divisor op -> DivVarS variable).  Returns the reciprocals this call
+        can share: divisor op -> variable name."""
         L = self.level
+        n = lambda i: "%s%d" % (pfx, i)  # noqa: E731
         const_vals: Dict[int, object] = {}
         for i, m in enumerate(L.micro):
             if m.kind == "const":
                 const_vals[i] = m.args[0]
-        prepared = set()  # divisor nodes whose reciprocal is prepared
+        prepared: Dict[int, str] = dict(ext_prep or {})
         for i in which:
             m = L.micro[i]
             if i in alias:
-                w(ind + "const %s a%d = %s;" % (m.ctype, i, alias[i]))
+                w(ind + "const %s %s = %s;" % (m.ctype, n(i), alias[i]))
                 continue
             t = m.ctype
-            name = "a%d" % i
+            name = n(i)
             k = m.kind
             if k == "const":
                 const_vals[i] = m.args[0]
                 w(ind + "const %s %s = %s;" % (t, name, MM.c_literal(m.args[0], t)))
             elif k == "loadS":
-                w(ind + "const %s %s = s_%s[%s];" % (t, name, m.args[1], self.idx_expr(m.args[0])))
+                w(ind + "const %s %s = s_%s[%s];" % (t, name, m.args[1],
+                                                    self.idx_expr(m.args[0], lane)))
             elif k == "loadM":
                 arr = self.mmp.arrays[m.args[1]]
-                w(ind + "const %s %s = r_%s[%s];" % (t, name, arr.name, self.idx_expr(m.args[0])))
+                w(ind + "const %s %s = r_%s[%s];" % (t, name, arr.name,
+                                                    self.idx_expr(m.args[0], lane)))
             elif k == "index":
-                w(ind + "const %s %s = (%s)%s;" % (t, name, t, AXVARS[m.args[0]]))
+                w(ind + "const %s %s = (%s)%s;" % (t, name, t, _wrap_name(m.args[0], 0, lane)))
             elif k == "uni":
                 op, a = m.args
                 if op.startswith("external-call/"):
                     f = op.split("/", 1)[1]
-                    w(ind + "const %s %s = %s((double)a%d);" % (t, name, f, a))
+                    w(ind + "const %s %s = %s((double)%s);" % (t, name, f, n(a)))
                 else:
-                    w(ind + "const %s %s = (%sa%d);" % (t, name, op, a))
+                    w(ind + "const %s %s = (%s%s);" % (t, name, op, n(a)))
             elif k == "bin":
                 op, a, b = m.args
                 ta, tb = L.micro[a].ctype, L.micro[b].ctype
                 dd = t == "double" and ta == "double" and tb == "double"
                 if op == "**":
-                    w(ind + "const %s %s = pow((double)a%d, (double)a%d);" % (t, name, a, b))
+                    w(ind + "const %s %s = pow((double)%s, (double)%s);" % (t, name, n(a), n(b)))
                 elif (op == "/" and self.soft_div and dd and b in const_vals and
                       _pow2_exponent(const_vals[b]) is not None):
-                    w(ind + "const %s %s = fm::soft::scale_pow2(a%d, %d);" %
-                      (t, name, a, -_pow2_exponent(const_vals[b])))
+                    w(ind + "const %s %s = fm::soft::scale_pow2(%s, %d);" %
+                      (t, name, n(a), -_pow2_exponent(const_vals[b])))
                 elif (op == "/" and self.soft_div and dd and b in const_vals and
                       _normal_double(const_vals[b]) and const_vals[b] > 0):
-                    w(ind + "const %s %s = fm::soft::div_const_s(a%d, fm::soft::DivConstS%s);" %
-                      (t, name, a, div_const_fields(const_vals[b])))
+                    w(ind + "const %s %s = fm::soft::div_const_s(%s, fm::soft::DivConstS%s);" %
+                      (t, name, n(a), div_const_fields(const_vals[b])))
                 elif op == "/" and self.soft_div and dd and b not in const_vals:
                     if b not in prepared:
-                        prepared.add(b)
-                        w(ind + "const fm::soft::DivVarS dv%d = fm::soft::prep_div_s(a%d);" % (b, b))
-                    w(ind + "const %s %s = fm::soft::div_var_s(a%d, dv%d);" % (t, name, a, b))
+                        prepared[b] = "dv" + n(b)
+                        w(ind + "const fm::soft::DivVarS %s = fm::soft::prep_div_s(%s);" %
+                          (prepared[b], n(b)))
+                    w(ind + "const %s %s = fm::soft::div_var_s(%s, %s);" % (t, name, n(a),
+                                                                            prepared[b]))
                 elif (op == "*" and self.soft_mul and dd and
                       (b in const_vals or a in const_vals) and
                       _pow2_exponent(const_vals[b] if b in const_vals else const_vals[a])
                       is not None):
                     x, c = (a, b) if b in const_vals else (b, a)
-                    w(ind + "const %s %s = fm::soft::scale_pow2(a%d, %d);" %
-                      (t, name, x, _pow2_exponent(const_vals[c])))
+                    w(ind + "const %s %s = fm::soft::scale_pow2(%s, %d);" %
+                      (t, name, n(x), _pow2_exponent(const_vals[c])))
                 elif (op == "*" and self.soft_mul and t == "double" and
                       ((b in const_vals and ta == "double" and _normal_double(const_vals[b])) or
                        (a in const_vals and tb == "double" and _normal_double(const_vals[a])))):
                     x, c = (a, b) if b in const_vals else (b, a)
-                    w(ind + "const %s %s = fm::soft::mul_const_s(a%d, fm::soft::MulConstS%s);" %
-                      (t, name, x, mul_const_fields(const_vals[c])))
+                    w(ind + "const %s %s = fm::soft::mul_const_s(%s, fm::soft::MulConstS%s);" %
+                      (t, name, n(x), mul_const_fields(const_vals[c])))
                 elif (op in CMP_SOFT and self.soft_cmp and ta == "double" and tb == "double"):
                     x, y = (b, a) if op in (">", ">=") else (a, b)
-                    w(ind + "const %s %s = %s;" % (t, name, CMP_SOFT[op] % (x, y)))
+                    w(ind + "const %s %s = %s;" % (t, name, CMP_SOFT[op] % (n(x), n(y))))
                 else:
-                    w(ind + "const %s %s = (a%d %s a%d);" % (t, name, a, op, b))
+                    w(ind + "const %s %s = (%s %s %s);" % (t, name, n(a), op, n(b)))
             elif k == "ite":
                 c, a, b = m.args
-                w(ind + "const %s %s = (a%d ? a%d : a%d);" % (t, name, c, a, b))
+                w(ind + "const %s %s = (%s ? %s : %s);" % (t, name, n(c), n(a), n(b)))
             elif k == "nary":
                 op, xs = m.args
-                names = ["(double)a%d" % x for x in xs]
+                names = ["(double)%s" % n(x) for x in xs]
 
                 def chain(fn, items):
                     acc = items[-1]
@@ -198,12 +212,13 @@ class LevelEmitter:
                 w(ind + "const %s %s = %s;" % (t, name, e))
             else:
                 raise MM.OM.FmrSemanticError("cannot emit %s" % k)
+        return prepared
 
-    # -- marching along axis 0 ------------------------------------------------------------
-    def _shifted(self) -> Dict[int, int]:
-        """For each micro op i, the op j whose value at cell x equals op i's at
-        cell x+1 along axis 0 (i itself for values that do not depend on the
-        position along axis 0), where the level has one."""
+    # -- marching along axis 0, pairs along axis 1 ---------------------------------------
+    def _shifted(self, axis: int = 0) -> Dict[int, int]:
+        """For each micro op i, the op j whose value at a cell equals op i's
+        value at the next cell along `axis` (i itself for values that do not
+        depend on the position along that axis), where the level has one."""
         L = self.level
         index = {(m.kind, m.args, m.ctype): i for i, m in enumerate(L.micro)}
         memo: Dict[int, Optional[int]] = {}
@@ -217,10 +232,11 @@ class LevelEmitter:
             if k in ("const", "imm"):
                 r = i
             elif k == "index":
-                r = None if args[0] == 0 else i
+                r = None if args[0] == axis else i
             elif k in ("loadS", "loadM"):
-                c = (args[0][0] + 1,) + tuple(args[0][1:])
-                r = index.get((k, (c, args[1]), m.ctype))
+                c = list(args[0])
+                c[axis] += 1
+                r = index.get((k, (tuple(c), args[1]), m.ctype))
             else:
                 ops = MM._Builder._operands(k, args)
                 new = [sh(j) for j in ops]
@@ -248,7 +264,7 @@ class LevelEmitter:
         """(ops the loop body needs, carried ops {i: j}): op i is taken from op
         j's value at the previous cell; everything else is computed."""
         L = self.level
-        carried_all = self._shifted()
+        carried_all = self._shifted(0)
         need = set()
         carried = {}
         stack = [a.root for a in L.arrays]
@@ -268,7 +284,38 @@ class LevelEmitter:
                         stack.append(j)
         return need, carried
 
-    def _wrap_lines(self, w, ind: str, axes) -> None:
+    def _pair_plan(self, need_a):
+        """Plan of the second cell (axis-1 coordinate + 1) of a thread's pair,
+        evaluated after the first: (ops its loop body needs, ops taken from
+        the first cell {i: j}, ops carried from its previous cell {i: j}).
+        An op whose shifted form the first cell evaluates anyway is taken from
+        there; otherwise carried along axis 0 where possible, else computed."""
+        L = self.level
+        from_a_all = self._shifted(1)
+        carried_all = self._shifted(0)
+        need = set()
+        from_a, carried = {}, {}
+        stack = [a.root for a in L.arrays]
+        need.update(stack)
+        while stack:
+            i = stack.pop()
+            j = from_a_all.get(i)
+            if j is not None and j in need_a:
+                from_a[i] = j
+            elif i in carried_all:
+                j = carried_all[i]
+                carried[i] = j
+                if j not in need:
+                    need.add(j)
+                    stack.append(j)
+            else:
+                for j in MM._Builder._operands(L.micro[i].kind, L.micro[i].args):
+                    if j not in need:
+                        need.add(j)
+                        stack.append(j)
+        return need, from_a, carried, from_a_all
+
+    def _wrap_lines(self, w, ind: str, axes, lane: str = "") -> None:
         needed = set()
         for m in self.level.micro:
             if m.kind in ("loadS", "loadM"):
@@ -277,32 +324,41 @@ class LevelEmitter:
                         needed.add((a, c))
         for a, c in sorted(needed):
             n = self.shape[a]
-            v = _wrap_name(a, c)
+            v = _wrap_name(a, c, lane)
+            x = _wrap_name(a, 0, lane)
             if abs(c) < n:
                 if c > 0:
                     w(ind + "const int %s = %s + %d >= %d ? %s + %d : %s + %d;" %
-                      (v, AXVARS[a], c, n, AXVARS[a], c - n, AXVARS[a], c))
+                      (v, x, c, n, x, c - n, x, c))
                 else:
                     w(ind + "const int %s = %s - %d < 0 ? %s + %d : %s - %d;" %
-                      (v, AXVARS[a], -c, AXVARS[a], n + c, AXVARS[a], -c))
+                      (v, x, -c, x, n + c, x, -c))
             else:
-                w(ind + "const int %s = ((%s + %d) %% %d + %d) %% %d;" % (v, AXVARS[a], c, n, n, n))
+                w(ind + "const int %s = ((%s + %d) %% %d + %d) %% %d;" % (v, x, c, n, n, n))
 
-    def _march_body(self, need, carried, chunk: int):
-        """Kernel body: each thread takes one column (a cell of axes 1..d-1) and a
-        chunk of `chunk` cells along axis 0; the first cell evaluates every op,
-        the following ones take the carried ops from the previous cell (same
+    def _march_body(self, need, carried, chunk: int, pair: int):
+        """Kernel body: each thread takes one column (a cell of axes 1..d-1), or
+        with pair = 2 two columns adjacent along axis 1, and a chunk of `chunk`
+        cells along axis 0.  The first cell evaluates every op, the following
+        ones take the carried ops from the previous cell; the second column of
+        a pair takes the ops it shares with the first from there (same
         operations on the same values: bit-identical)."""
         L = self.level
         ncol = 1
         for n in self.shape[1:]:
             ncol *= n
+        s1 = ncol // self.shape[1]  # stride of axis 1
         n0 = self.shape[0]
         nchunk = (n0 + chunk - 1) // chunk
+        nitem_col = ncol // pair
         body: List[str] = []
         w = body.append
-        w("    const long long col = item %% %dll;" % ncol)
-        w("    const int x0 = (int)(item / %dll) * %d;" % (ncol, chunk))
+        if pair == 1:
+            w("    const long long col = item %% %dll;" % ncol)
+        else:
+            w("    const long long colp = item %% %dll;" % nitem_col)
+            w("    const long long col = colp / %dll * %dll + colp %% %dll;" % (s1, 2 * s1, s1))
+        w("    const int x0 = (int)(item / %dll) * %d;" % (nitem_col, chunk))
         w("    const int x1 = x0 + %d < %d ? x0 + %d : %d;" % (chunk, n0, chunk, n0))
         w("    size_t rest = (size_t)col;")
         for a in reversed(range(1, self.dim)):
@@ -312,31 +368,73 @@ class LevelEmitter:
                 w("    const int %s = (int)(rest %% %du); rest /= %du;" % (AXVARS[a], self.shape[a],
                                                                        self.shape[a]))
         self._wrap_lines(w, "    ", set(range(1, self.dim)))
-        live_carry = sorted(i for i in carried if i in need)
-        for i in live_carry:
-            w("    %s h%d;" % (L.micro[i].ctype, i))  # value held from the previous cell
-        # first cell of the chunk: every op
+        live_a = sorted(i for i in carried if i in need)
+        for i in live_a:
+            w("    %s ha%d;" % (L.micro[i].ctype, i))  # value held from the previous cell
+        if pair == 2:
+            need_b, from_a, carried_b, from_a_all = self._pair_plan(need)
+            w("    const int %s = %s + 1;" % (_wrap_name(1, 0, "b"), AXVARS[1]))  # c1 even
+            self._wrap_lines(w, "    ", {1}, "b")
+            live_b = sorted(i for i in carried_b if i in need_b)
+            for i in live_b:
+                w("    %s hb%d;" % (L.micro[i].ctype, i))
+
+        def cell(which_a, alias_a, which_b, alias_b_of):
+            prep = self._emit_ops(which_a, alias_a, w, "      ")
+            for arr in L.arrays:
+                w("      w_%s[idx] = a%d;" % (arr.name, arr.root))
+            if pair == 2:
+                alias_b = alias_b_of()
+                ext = {i: prep[j] for i, j in from_a_all.items() if j in prep}
+                self._emit_ops(which_b, alias_b, w, "      ", "b", "b", ext)
+                for arr in L.arrays:
+                    w("      w_%s[idx + %dull] = b%d;" % (arr.name, s1, arr.root))
+            for i in live_a:
+                w("      ha%d = a%d;" % (i, carried[i]))
+            if pair == 2:
+                for i in live_b:
+                    w("      hb%d = b%d;" % (i, carried_b[i]))
+
+        # first cell of the chunk: every op (the second column takes whatever
+        # the first evaluates)
         w("    {")
         w("      const int c0 = x0;")
         w("      const size_t idx = (size_t)c0 * %dull + (size_t)col;" % ncol)
         self._wrap_lines(w, "      ", {0})
-        self._emit_ops(range(len(L.micro)), {}, w, "      ")
-        for arr in L.arrays:
-            w("      w_%s[idx] = a%d;" % (arr.name, arr.root))
-        for i in live_carry:
-            w("      h%d = a%d;" % (i, carried[i]))
+        cell(range(len(L.micro)), {}, range(len(L.micro)),
+             lambda: {i: "a%d" % j for i, j in from_a_all.items()})
         w("    }")
         # the rest of the chunk
         w("    for (int c0 = x0 + 1; c0 < x1; ++c0) {")
         w("      const size_t idx = (size_t)c0 * %dull + (size_t)col;" % ncol)
         self._wrap_lines(w, "      ", {0})
-        self._emit_ops(sorted(need), {i: "h%d" % i for i in live_carry}, w, "      ")
-        for arr in L.arrays:
-            w("      w_%s[idx] = a%d;" % (arr.name, arr.root))
-        for i in live_carry:
-            w("      h%d = a%d;" % (i, carried[i]))
+
+        def steady_b():
+            al = {i: "a%d" % j for i, j in from_a.items()}
+            al.update({i: "hb%d" % i for i in live_b})
+            return al
+
+        cell(sorted(need), {i: "ha%d" % i for i in live_a},
+             sorted(need_b) if pair == 2 else (), steady_b)
         w("    }")
-        return body, ncol * nchunk
+        return body, nitem_col * nchunk
+
+    def _pair_choice(self, chunk: int, ncells: int) -> int:
+        """Cells along axis 1 per thread (1 or 2).  A pair needs at least three
+        axes (axis 1 is then not the coalesced one) and an even extent of axis
+        1; `march_pair` 1 or 2 forces the choice where the shape allows it,
+        0 pairs small levels (<= 200 micro ops: the large ones already run at
+        the 128-register cap) while ~150k threads remain."""
+        if self.dim < 3 or self.shape[1] % 2:
+            return 1
+        if self.march_pair in (1, 2):
+            return self.march_pair
+        if len(self.level.micro) > 200 or ncells // 150000 < 2 * chunk:
+            return 1
+        shared = self._shifted(1)
+        if not any(self.level.micro[i].kind != "index" for i in shared):
+            return 1  # the two cells share nothing but coordinates
+        return 2
 
     def emit(self) -> Tuple[str, List[str], List[int], List[MM.Array]]:
         """Kernel source of the level.  Launch bounds (256 threads, 2 CTAs per SM) cap
@@ -366,16 +464,19 @@ class LevelEmitter:
             chunk = min(self.march_chunk, self.shape[0])
         else:
             chunk = min(16, self.shape[0], max(1, ncells // 150000))
-        if chunk > 1 and self.dim >= 2:
+        march, pair = False, 1
+        if self.dim >= 2:
             need, carried = self._march_plan()
-            if any(i in need for i in carried):
-                body, nitems = self._march_body(need, carried, chunk)
-                src = ["__global__ void __launch_bounds__(256, 2) %s(%s) {" % (kname, ", ".join(params)),
-                       "  for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;"
-                       " item < %dll; item += (long long)gridDim.x * blockDim.x) {" % nitems]
-                src += body
-                src += ["  }", "}", ""]
-                return "\n".join(src), state_names, arr_ids, L.arrays
+            march = chunk > 1 and any(i in need for i in carried)
+            pair = self._pair_choice(chunk if march else 1, ncells)
+        if march or pair == 2:
+            body, nitems = self._march_body(need, carried, chunk if march else 1, pair)
+            src = ["__global__ void __launch_bounds__(256, 2) %s(%s) {" % (kname, ", ".join(params)),
+                   "  for (long long item = (long long)blockIdx.x * blockDim.x + threadIdx.x;"
+                   " item < %dll; item += (long long)gridDim.x * blockDim.x) {" % nitems]
+            src += body
+            src += ["  }", "}", ""]
+            return "\n".join(src), state_names, arr_ids, L.arrays
         body: List[str] = []
         w = body.append
         # coordinates
@@ -416,16 +517,18 @@ class LevelEmitter:
 
 
 def emit_kernels(mmp: MM.MMProgram, soft_div: bool = True, soft_mul: bool = True,
-                 soft_cmp: bool = True, march_chunk: int = 0):
+                 soft_cmp: bool = True, march_chunk: int = 0, march_pair: int = 0):
     """Kernel source and, per level, (kernel name, state names read, arrays
     read, arrays written).  A thread evaluates a chunk of cells along axis 0
     and carries the values a cell shares with the next one: march_chunk cells
-    (1: one cell per thread), or with 0 up to 16 while ~150k threads remain."""
+    (1: one cell per thread), or with 0 up to 16 while ~150k threads remain.
+    march_pair 2 gives a thread two cells along axis 1 that share values,
+    1 one cell, 0 lets each level choose (`LevelEmitter._pair_choice`)."""
     parts = []
     levels = []
     for li, L in enumerate(mmp.levels):
         src, sn, ar, aw = LevelEmitter(mmp, L, li, soft_div, soft_mul, soft_cmp,
-                                       march_chunk).emit()
+                                       march_chunk, march_pair).emit()
         parts.append(src)
         levels.append(("fmr_level_%d" % li, sn, ar, aw))
     return "\n".join(parts), levels

@@ -1,0 +1,123 @@
+"""Host build of the CUDA kernels that the .fmr front end generates: test
+infrastructure for the CPU suite.
+
+The generated kernels are plain C++ apart from the launch qualifiers and the
+grid-stride loop's built-in indices, and their exact binary64 forms
+(csrc/fm_softfp.cuh) compile for the host as well.  So the emitted kernel
+source is compiled with g++ under a prelude that defines those names for a
+grid of one block of one thread: the single "thread" walks every item of the
+grid-stride loop, i.e. every (column, chunk) work item of the marching and
+pairing schedules, in order.  The step loop mirrors the generated host code
+(formura_gb300/backend.py, `_fmr_parts`): each level reads the current state
+and the arrays of earlier levels, and the state buffers swap after a step.
+Floating-point contraction is off, as in the device build (--fmad=false).
+"""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import subprocess
+import tempfile
+from pathlib import Path
+from typing import Dict
+
+import numpy as np
+
+from formura_gb300.fmr.emit_cuda import emit_kernels
+
+ROOT = Path(__file__).resolve().parents[1]
+CSRC = ROOT / "formura_gb300" / "csrc"
+BUILD = Path(tempfile.gettempdir()) / "fmr_host_kernels"
+NP_TYPES = {"double": np.float64, "float": np.float32}
+
+PRELUDE = r"""
+#include <math.h>
+#include <stddef.h>
+#include <stdlib.h>
+#include <string.h>
+#include "fm_softfp.cuh"
+#define __global__
+#define __launch_bounds__(threads, blocks)
+namespace {
+struct FmHostDim { unsigned x, y, z; };
+const FmHostDim blockIdx = {0u, 0u, 0u}, threadIdx = {0u, 0u, 0u};
+const FmHostDim gridDim = {1u, 1u, 1u}, blockDim = {1u, 1u, 1u};
+}  // namespace
+"""
+
+
+def host_source(mmp, march_chunk: int = 0, march_pair: int = 0) -> str:
+    kern, levels = emit_kernels(mmp, march_chunk=march_chunk, march_pair=march_pair)
+    states = [n for n, _ in mmp.state]
+    stype = dict(mmp.state)
+    sidx = {n: i for i, n in enumerate(states)}
+    arrays = sorted(mmp.arrays.values(), key=lambda a: a.node)
+    aidx = {a.node: i for i, a in enumerate(arrays)}
+    ncells = int(np.prod(mmp.shape))
+    out = [PRELUDE, "namespace {", kern, "}  // namespace", "",
+           'extern "C" int fmr_host_run(int steps, void **state) {',
+           "  const size_t n = %dull;" % ncells,
+           "  void *cur[%d], *nxt[%d], *arr[%d];" % (len(states), len(states), max(1, len(arrays))),
+           "  size_t bytes;"]
+    w = out.append
+    for i, s in enumerate(states):
+        w("  bytes = n * sizeof(%s);" % stype[s])
+        w("  cur[%d] = malloc(bytes); nxt[%d] = malloc(bytes);" % (i, i))
+        w("  if (!cur[%d] || !nxt[%d]) return 1;" % (i, i))
+        w("  memcpy(cur[%d], state[%d], bytes);" % (i, i))
+    for a in arrays:
+        if a.store_of is None:
+            w("  arr[%d] = malloc(n * sizeof(%s)); if (!arr[%d]) return 1;" % (aidx[a.node], a.ctype,
+                                                                                aidx[a.node]))
+    w("  for (int t = 0; t < steps; ++t) {")
+    for kname, sn, ar, aw in levels:
+        args = ["(const %s*)cur[%d]" % (stype[s], sidx[s]) for s in sn]
+        for x in ar:
+            a = mmp.arrays[x]
+            args.append("(const %s*)%s" % (a.ctype, "arr[%d]" % aidx[x] if a.store_of is None
+                                           else "nxt[%d]" % sidx[a.store_of]))
+        for a in aw:
+            args.append("(%s*)%s" % (a.ctype, "arr[%d]" % aidx[a.node] if a.store_of is None
+                                     else "nxt[%d]" % sidx[a.store_of]))
+        w("    %s(%s);" % (kname, ", ".join(args)))
+    w("    for (int i = 0; i < %d; ++i) { void *x = cur[i]; cur[i] = nxt[i]; nxt[i] = x; }"
+      % len(states))
+    w("  }")
+    for i, s in enumerate(states):
+        w("  memcpy(state[%d], cur[%d], n * sizeof(%s)); free(cur[%d]); free(nxt[%d]);"
+          % (i, i, stype[s], i, i))
+    for a in arrays:
+        if a.store_of is None:
+            w("  free(arr[%d]);" % aidx[a.node])
+    w("  return 0;")
+    w("}")
+    return "\n".join(out) + "\n"
+
+
+class HostKernels:
+    """The generated kernels of one compiled program (mm.MMProgram), built for
+    the host."""
+
+    def __init__(self, mmp, march_chunk: int = 0, march_pair: int = 0):
+        self.mmp = mmp
+        self.source = host_source(mmp, march_chunk, march_pair)
+        key = hashlib.sha256((self.source + (CSRC / "fm_softfp.cuh").read_text()).encode())
+        BUILD.mkdir(parents=True, exist_ok=True)
+        so = BUILD / ("k_%s.so" % key.hexdigest()[:16])
+        if not so.exists():
+            src = so.with_suffix(".cpp")
+            src.write_text(self.source)
+            tmp = Path(str(so) + ".tmp")
+            subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fPIC", "-shared",
+                            "-w", "-I", str(CSRC), "-o", str(tmp), str(src), "-lm"], check=True)
+            tmp.replace(so)
+        self.lib = ctypes.CDLL(str(so))
+        self.lib.fmr_host_run.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+
+    def run(self, state: Dict[str, np.ndarray], steps: int) -> Dict[str, np.ndarray]:
+        arrs = [np.ascontiguousarray(state[n], dtype=NP_TYPES[t]).reshape(self.mmp.shape).copy()
+                for n, t in self.mmp.state]
+        ptrs = (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+        if self.lib.fmr_host_run(int(steps), ptrs) != 0:
+            raise MemoryError("host kernel run: allocation failed")
+        return {n: a for (n, _), a in zip(self.mmp.state, arrs)}

@@ -205,7 +205,7 @@ def test_generated_integer_pipe_forms_compile(tmp_path):
     # the divisor 1 + a*a is prepared once for its two quotients (w and g)
     import collections
     import re
-    uses = collections.Counter(re.findall(r"div_var_s\(a\d+, (dv\d+)\)", kern))
+    uses = collections.Counter(re.findall(r"div_var_s\(a\d+, (dva\d+)\)", kern))
     assert max(uses.values()) == 2 and kern.count("prep_div_s(") == len(uses)
     assert "fmax(" not in kern and "fmin(" not in kern and " / " not in kern
     backend.build_program(p, outdir=tmp_path)
@@ -220,17 +220,44 @@ def test_marching_kernels_carry_shared_values():
     from formura_gb300.fmr.emit_cuda import emit_kernels
 
     p = load_program(EX / "gray-scott-3d.fmr")
-    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)))
+    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)), march_pair=1)
     first, loop = kern.split("for (int c0 = x0 + 1;")
     first = first[first.index("const int c0 = x0;"):]
     count = lambda text, s: text.count(s)
     assert count(loop, "s_U[") + count(loop, "s_V[") == 10   # 14 in the first cell
     assert count(first, "s_U[") + count(first, "s_V[") == 14
     assert count(loop, "div_const_s") == count(first, "div_const_s") - 2
-    assert "h0 = a" in loop and "= h0;" in loop
+    assert "ha0 = a" in loop and "= ha0;" in loop
     # one cell per thread when asked
-    flat, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)), march_chunk=1)
+    flat, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)), march_chunk=1,
+                           march_pair=1)
     assert "x0" not in flat
+
+
+def test_paired_kernels_share_values_along_axis_1():
+    """With pairs a thread evaluates cells y and y+1 of each plane; the second
+    takes from the first what they share (its centre and y-1 loads are the
+    first cell's y+1 and centre loads, its face flux at y-1/2 is the first
+    cell's at y+1/2).  gray-scott-3d at 256^3 is paired by default; the large
+    levels of 3d-mhd-rk4 are not (they already run at the register cap)."""
+    from formura_gb300.fmr.emit_cuda import emit_kernels
+
+    p = load_program(EX / "gray-scott-3d.fmr")
+    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)))
+    assert "c1b" in kern
+    first, loop = kern.split("for (int c0 = x0 + 1;")
+    first = first[first.index("const int c0 = x0;"):]
+    count = lambda text, s: text.count(s)
+    # per pair: 10 + 8 loads in the loop (20 unpaired), 14 + 10 in the first cell
+    assert count(loop, "s_U[") + count(loop, "s_V[") == 18
+    assert count(first, "s_U[") + count(first, "s_V[") == 24
+    # 16 + 14 divisions by dx in the loop (32 unpaired)
+    assert count(loop, "div_const_s") == 30
+    assert "w_st_U[idx + 256ull] = b" in loop
+    if (REF / "examples" / "3d-mhd-rk4.fmr").exists():
+        src = (REF / "examples" / "3d-mhd-rk4.fmr").read_text()
+        mhd, _ = emit_kernels(compile_source(src, (256, 256, 256)))
+        assert "c1b" not in mhd
 
 
 CURRENT_SYNTAX_EXAMPLES = [

@@ -1,0 +1,89 @@
+"""The CUDA kernels generated by the .fmr front end, compiled for the host
+(tests/fmr_host.py) and run against the C oracle of the same program
+(oracle/fmr_c.py): bit for bit, under every schedule the emitter has — one
+cell per thread, chunks marching along axis 0 with carried values (chunks that
+do and do not divide the axis), and pairs of cells along axis 1 sharing values
+(with and without marching, forced onto shapes that do not allow them).
+
+These check the generated arithmetic and the carrying and sharing of values
+on the CPU; tests/test_gpu_fmr.py runs the same kernels on the GPU.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from formura_gb300 import inits
+from formura_gb300.fmr import load_program
+from oracle import fmr_c
+
+from fmr_host import HostKernels
+
+EX = Path(__file__).resolve().parents[1] / "examples"
+REF = Path("/root/reference")
+
+
+def _state(p, seed):
+    if p.fmr_source and "gray" in p.name:
+        U0, V0 = inits.gray_scott_3d(*p.shape, seed=seed, ncubes=2, side=4)
+        return {"U": U0, "V": V0}
+    rng = np.random.default_rng(seed)
+    return {name: rng.random(p.shape).astype(np.float32 if t == "float" else np.float64)
+            for name, t in p.states()}
+
+
+def _check(p, pair, steps, seed=5):
+    hk = HostKernels(p.compiled(), p.march_chunk, pair)
+    s0 = _state(p, seed)
+    got = hk.run(s0, steps)
+    want = fmr_c.FmrOracle(p.fmr_source, p.shape).run(s0, steps)
+    for name in s0:
+        assert np.array_equal(got[name], want[name]), name
+    return hk.source
+
+
+@pytest.mark.parametrize("fmr,kw,pair", [
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[16, 24, 40], march_chunk=1), 1),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[16, 24, 40], march_chunk=4), 1),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[16, 24, 40], march_chunk=4), 2),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[19, 8, 16], march_chunk=5), 2),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[6, 10, 12], march_chunk=1), 2),
+    ("fmr-3d-advection.fmr", dict(march_chunk=6), 2),
+    ("fmr-3d-advection.fmr", dict(intra_node_shape=[5, 4, 33], march_chunk=2), 2),
+    ("fmr-3d-advection.fmr", dict(intra_node_shape=[5, 3, 33]), 0),
+    ("fmr-features.fmr", {}, 0),
+    ("fmr-features.fmr", dict(march_chunk=7), 0),
+    ("fmr-features.fmr", dict(intra_node_shape=[7, 33], march_chunk=3), 2),
+    ("fmr-limiter.fmr", dict(march_chunk=3), 0),
+    ("fmr-1d-float.fmr", dict(intra_node_shape=[7]), 0),
+    ("fmr-libm.fmr", {}, 0),
+    ("diffusion-2d.fmr", dict(intra_node_shape=[64, 48], march_chunk=16), 0),
+])
+def test_host_kernels_match_c_oracle(fmr, kw, pair):
+    p = load_program(EX / fmr, **kw)
+    src = _check(p, pair, steps=7)
+    paired = "c1b" in src
+    assert paired == (pair == 2 and p.dim >= 3 and p.shape[1] % 2 == 0)
+
+
+def test_pair_forced_on_odd_axis_falls_back():
+    p = load_program(EX / "gray-scott-3d.fmr", intra_node_shape=[8, 7, 16], march_chunk=3)
+    src = _check(p, 2, steps=4)
+    assert "c1b" not in src and "ha" in src
+
+
+@pytest.mark.skipif(not (REF / "examples" / "3d-mhd-rk4.fmr").exists(),
+                    reason="reference tree absent")
+def test_host_kernels_mhd_rk4_paired():
+    """All 8 levels of the reference's 3d-mhd-rk4.fmr (72 manifest arrays),
+    marching in chunks of 3 with pairs forced onto every level."""
+    p = load_program(REF / "examples" / "3d-mhd-rk4.fmr", intra_node_shape=[8, 8, 8],
+                     monitor_interval=2, mpi_grid_shape=[1, 1, 1], march_chunk=3)
+    o = fmr_c.FmrOracle(p.fmr_source, p.shape)
+    s0 = dict(zip(o.state_names, inits.mhd_3d(8, seed=3)))
+    hk = HostKernels(p.compiled(), p.march_chunk, 2)
+    assert hk.source.count("c1b + 1") >= 1
+    got = hk.run(s0, 2)
+    want = o.run(s0, 2)
+    for name in s0:
+        assert np.array_equal(got[name], want[name]), name

@@ -47,6 +47,14 @@ def _random_state(prog, rng):
     ("fmr-features.fmr", dict(march_chunk=7)),
     ("fmr-limiter.fmr", dict(march_chunk=3)),
     ("diffusion-2d.fmr", dict(intra_node_shape=[64, 48], monitor_interval=7, march_chunk=16)),
+    # pairs of cells along y sharing values, with and without marching along x
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[16, 24, 40], monitor_interval=5, march_chunk=4,
+                               march_pair=2)),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[19, 8, 16], monitor_interval=3, march_chunk=5,
+                               march_pair=2)),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[6, 10, 12], monitor_interval=3, march_chunk=1,
+                               march_pair=2)),
+    ("fmr-3d-advection.fmr", dict(march_chunk=6, march_pair=2)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)
