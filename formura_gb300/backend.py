@@ -76,8 +76,8 @@ class Program:
     # form "fmr": cells per thread along axis 0 in the generated kernels (values shared by
     # consecutive cells carried in registers); 0 = automatic (up to 16, keeping ~150k threads)
     march_chunk: int = 0
-    # form "fmr": cells per thread along axis 1 (2 = two adjacent cells sharing values, 1 = one,
-    # 0 = automatic per level); a pair needs 3+ axes and an even extent of axis 1
+    # form "fmr": 2 = two cells per thread adjacent along axis 1, sharing values (needs 3+ axes
+    # and an even extent of axis 1; measured slower on gray-scott-3d), 0 or 1 = one cell
     march_pair: int = 0
 
     @property

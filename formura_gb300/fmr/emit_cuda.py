@@ -419,22 +419,18 @@ class LevelEmitter:
         w("    }")
         return body, nitem_col * nchunk
 
-    def _pair_choice(self, chunk: int, ncells: int) -> int:
+    def _pair_choice(self) -> int:
         """Cells along axis 1 per thread (1 or 2).  A pair needs at least three
         axes (axis 1 is then not the coalesced one) and an even extent of axis
-        1; `march_pair` 1 or 2 forces the choice where the shape allows it,
-        0 pairs small levels (<= 200 micro ops: the large ones already run at
-        the 128-register cap) while ~150k threads remain."""
+        1; `march_pair` 2 asks for pairs where the shape allows them, 0 and 1
+        give one cell.  Pairs are not the default because they measured slower:
+        gray-scott-3d at 256^3 ran 15.7 GLUP/s paired (101 registers, 2 CTAs
+        per SM) and 17.2 paired at 3 CTAs per SM (80 registers) against 17.4
+        unpaired (74 registers); the saved division, two subtractions and two
+        loads per pair do not pay for the longer live ranges."""
         if self.dim < 3 or self.shape[1] % 2:
             return 1
-        if self.march_pair in (1, 2):
-            return self.march_pair
-        if len(self.level.micro) > 200 or ncells // 150000 < 2 * chunk:
-            return 1
-        shared = self._shifted(1)
-        if not any(self.level.micro[i].kind != "index" for i in shared):
-            return 1  # the two cells share nothing but coordinates
-        return 2
+        return 2 if self.march_pair == 2 else 1
 
     def emit(self) -> Tuple[str, List[str], List[int], List[MM.Array]]:
         """Kernel source of the level.  Launch bounds (256 threads, 2 CTAs per SM) cap
@@ -468,7 +464,7 @@ class LevelEmitter:
         if self.dim >= 2:
             need, carried = self._march_plan()
             march = chunk > 1 and any(i in need for i in carried)
-            pair = self._pair_choice(chunk if march else 1, ncells)
+            pair = self._pair_choice()
         if march or pair == 2:
             body, nitems = self._march_body(need, carried, chunk if march else 1, pair)
             src = ["__global__ void __launch_bounds__(256, 2) %s(%s) {" % (kname, ", ".join(params)),
@@ -522,8 +518,8 @@ def emit_kernels(mmp: MM.MMProgram, soft_div: bool = True, soft_mul: bool = True
     read, arrays written).  A thread evaluates a chunk of cells along axis 0
     and carries the values a cell shares with the next one: march_chunk cells
     (1: one cell per thread), or with 0 up to 16 while ~150k threads remain.
-    march_pair 2 gives a thread two cells along axis 1 that share values,
-    1 one cell, 0 lets each level choose (`LevelEmitter._pair_choice`)."""
+    march_pair 2 gives a thread two cells along axis 1 that share values
+    (where the shape allows it), 0 or 1 one cell (`LevelEmitter._pair_choice`)."""
     parts = []
     levels = []
     for li, L in enumerate(mmp.levels):

@@ -238,12 +238,14 @@ def test_paired_kernels_share_values_along_axis_1():
     """With pairs a thread evaluates cells y and y+1 of each plane; the second
     takes from the first what they share (its centre and y-1 loads are the
     first cell's y+1 and centre loads, its face flux at y-1/2 is the first
-    cell's at y+1/2).  gray-scott-3d at 256^3 is paired by default; the large
-    levels of 3d-mhd-rk4 are not (they already run at the register cap)."""
+    cell's at y+1/2).  Pairs are asked for (march_pair = 2); the default
+    evaluates one cell per thread."""
     from formura_gb300.fmr.emit_cuda import emit_kernels
 
     p = load_program(EX / "gray-scott-3d.fmr")
-    kern, _ = emit_kernels(compile_source(p.fmr_source, tuple(p.shape)))
+    mmp = compile_source(p.fmr_source, tuple(p.shape))
+    assert "c1b" not in emit_kernels(mmp)[0]
+    kern, _ = emit_kernels(mmp, march_pair=2)
     assert "c1b" in kern
     first, loop = kern.split("for (int c0 = x0 + 1;")
     first = first[first.index("const int c0 = x0;"):]
@@ -254,10 +256,6 @@ def test_paired_kernels_share_values_along_axis_1():
     # 16 + 14 divisions by dx in the loop (32 unpaired)
     assert count(loop, "div_const_s") == 30
     assert "w_st_U[idx + 256ull] = b" in loop
-    if (REF / "examples" / "3d-mhd-rk4.fmr").exists():
-        src = (REF / "examples" / "3d-mhd-rk4.fmr").read_text()
-        mhd, _ = emit_kernels(compile_source(src, (256, 256, 256)))
-        assert "c1b" not in mhd
 
 
 CURRENT_SYNTAX_EXAMPLES = [
