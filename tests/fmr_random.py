@@ -2,16 +2,17 @@
 infrastructure).
 
 A program has two state grids p and q (q optionally float, updated from q
-alone so that its type stays float), constants, and a
-step whose updates are random expression trees over: neighbour reads at
-offsets up to +-2 on every axis, constants, a linear function of the
-coordinates, + - *, division by a
+alone so that its type stays float), constants, and a step whose updates are
+random expression trees over: neighbour reads at offsets up to +-2 on every
+axis, constants, a linear function of the coordinates, + - *, division by a
 constant (powers of two included), division by a positive run-time value
 (1.5 + e*e), n-ary max/min (>? <?), the limiter (<%), if-then-else on each of
 the six comparisons, negation, and optionally a manifest half-offset grid
-differenced along the first axis.  The updates are clamped to [-4, 4] with
->? and <?, which also maps a NaN to the bound (C fmax/fmin semantics), so
-long runs stay finite while every operation form is exercised.
+differenced along the first axis; `extended` adds let-in and a lambda (a
+second difference along the first axis) applied to the grids.  The updates
+are clamped to [-4, 4] with >? and <?, which also maps a NaN to the bound
+(C fmax/fmin semantics), so long runs stay finite while every operation form
+is exercised.
 """
 from __future__ import annotations
 
@@ -22,7 +23,8 @@ IDX = ["i", "j", "k"]
 AXES = ["x", "y", "z"]
 
 
-def random_program(seed: int, dim: int, float_q: bool = False, depth: int = 3) -> str:
+def random_program(seed: int, dim: int, float_q: bool = False, depth: int = 3,
+                   extended: bool = False) -> str:
     rng = random.Random(seed)
     idx = IDX[:dim]
     states = ["p", "q"]
@@ -36,6 +38,8 @@ def random_program(seed: int, dim: int, float_q: bool = False, depth: int = 3) -
 
     def leaf() -> str:
         r = rng.random()
+        if extended and r < 0.1:
+            return "(d2 %s)" % rng.choice(states)
         if r < 0.7:
             return ref(rng.choice(states))
         if r < 0.9 or "p" not in states:
@@ -62,13 +66,18 @@ def random_program(seed: int, dim: int, float_q: bool = False, depth: int = 3) -
         if r < 0.77:
             return "(if %s %s %s then %s else %s)" % (
                 sub(), rng.choice([">", "<", ">=", "<=", "==", "!="]), sub(), sub(), sub())
-        if r < 0.85:
+        if r < (0.82 if extended else 0.85):
             return "(-%s)" % sub()
+        if extended and r < 0.86:
+            return "(let t = %s in t * t - %s)" % (sub(), sub())
         return "(%s * %s)" % (const(), sub())
 
     out: List[str] = ["dimension :: %d" % dim, "axes :: %s" % ", ".join(AXES[:dim]), ""]
     out.append("double :: ca = %r, cb = %r" % (round(rng.uniform(-1, 1), 3),
                                               rng.choice([0.5, 0.25, 2.0, 0.1, 3.0])))
+    if extended:
+        out.append("d2 = fun(a) (a[%s] + a[%s]) - 2 * a" % (
+            ", ".join(["i+1"] + idx[1:]), ", ".join(["i-1"] + idx[1:])))
     out += ["", "begin function init() returns (p, q)", "  double [] :: p = 0",
             "  %s [] :: q = 0" % ("float" if float_q else "double"), "end function", "",
             "begin function step(p, q) returns (p_next, q_next)"]

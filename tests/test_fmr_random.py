@@ -5,6 +5,7 @@ oracle of the same program (oracle/fmr_c.py), bit for bit after 5 steps.
 
 Shapes include axes of extent 2 and 3, below the largest read offset (2), so
 the modulo form of the periodic wrap runs as well as the conditional one.
+The extended cases add 1D programs, deeper trees, let-in and a lambda.
 """
 import random
 
@@ -40,6 +41,31 @@ def initial_state(seed, shape, float_q):
 @pytest.mark.parametrize("seed", range(24))
 def test_random_program_host_kernels_match_c_oracle(seed):
     src, shape, chunk, pair, float_q = case(seed)
+    hk = HostKernels(compile_source(src, shape), chunk, pair)
+    s0 = initial_state(seed, shape, float_q)
+    got = hk.run(s0, 5)
+    want = fmr_c.FmrOracle(src, shape).run(s0, 5)
+    for name in s0:
+        assert np.array_equal(got[name].view(np.uint8), want[name].view(np.uint8)), (name, src)
+
+
+def extended_case(seed):
+    """(source, shape, march_chunk, march_pair, float q) with 1 to 3 axes,
+    trees of depth 2 to 4, let-in and a lambda."""
+    rng = random.Random(5000 + seed)
+    dim = rng.choice([1, 2, 3])
+    float_q = rng.random() < 0.3
+    depth = rng.choice([2, 3, 4])
+    shape = {3: lambda: (rng.randint(3, 9), rng.choice([2, 6, 8, 10]), rng.randint(2, 12)),
+             2: lambda: (rng.randint(2, 12), rng.randint(2, 33)),
+             1: lambda: (rng.randint(2, 40),)}[dim]()
+    return (random_program(seed, dim, float_q, depth, extended=True), shape,
+            rng.choice([1, 2, 3, 5, 16]), rng.choice([1, 2]), float_q)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_extended_random_program_host_kernels_match_c_oracle(seed):
+    src, shape, chunk, pair, float_q = extended_case(seed)
     hk = HostKernels(compile_source(src, shape), chunk, pair)
     s0 = initial_state(seed, shape, float_q)
     got = hk.run(s0, 5)
