@@ -8,8 +8,10 @@ axis, constants, a linear function of the coordinates, + - *, division by a
 constant (powers of two included), division by a positive run-time value
 (1.5 + e*e), n-ary max/min (>? <?), the limiter (<%), if-then-else on each of
 the six comparisons, negation, and optionally a manifest half-offset grid
-differenced along the first axis; `extended` adds let-in and a lambda (a
-second difference along the first axis) applied to the grids.  The updates
+differenced along the first axis; `extended` adds let-in, a lambda (a
+second difference along the first axis) applied to the grids, a second
+manifest grid reading the first (a second level) and a tuple binding with
+tuple arithmetic.  The updates
 are clamped to [-4, 4] with >? and <?, which also maps a NaN to the bound
 (C fmax/fmin semantics), so long runs stay finite while every operation form
 is exercised.
@@ -90,6 +92,17 @@ def random_program(seed: int, dim: int, float_q: bool = False, depth: int = 3,
         out.append("  manifest :: f")
         out.append("  f[i+1/2%s%s] = %s" % (sep, rest, expr(depth - 1)))
         flux = " + (f[i+1/2%s%s] - f[i-1/2%s%s])" % (sep, rest, sep, rest)
+        if extended and rng.random() < 0.6:
+            # a second manifest grid reading the first: one more level
+            out.append("  manifest :: g")
+            out.append("  g = %s + 0.5 * (f[i+1/2%s%s] + f[i-1/2%s%s])" % (
+                expr(depth - 2), sep, rest, sep, rest))
+            flux += " + 0.1 * (g[%s] - g)" % ", ".join(["i+1"] + idx[1:])
+    if extended and rng.random() < 0.5:
+        # tuple binding and tuple arithmetic
+        out.append("  (u1, u2) = (%s, %s) * 0.5 + (%s, %s)" % (
+            expr(depth - 2), expr(depth - 2), expr(depth - 2), expr(depth - 2)))
+        flux += " + u1 * 0.5 - u2"
     out.append("  p_next = ((p + 0.01 * (%s%s)) >? -4) <? 4" % (expr(depth), flux))
     if float_q:
         states = ["q"]  # a float update reads float grids only (no promotion to double)
