@@ -483,24 +483,7 @@ class LevelEmitter:
             else:
                 w("    const int %s = (int)(rest %% %du); rest /= %du;" % (AXVARS[a], self.shape[a],
                                                                        self.shape[a]))
-        needed = set()
-        for m in L.micro:
-            if m.kind in ("loadS", "loadM"):
-                for a, c in enumerate(m.args[0]):
-                    if c:
-                        needed.add((a, c))
-        for a, c in sorted(needed):
-            n = self.shape[a]
-            v = _wrap_name(a, c)
-            if abs(c) < n:
-                if c > 0:
-                    w("    const int %s = %s + %d >= %d ? %s + %d : %s + %d;" %
-                      (v, AXVARS[a], c, n, AXVARS[a], c - n, AXVARS[a], c))
-                else:
-                    w("    const int %s = %s - %d < 0 ? %s + %d : %s - %d;" %
-                      (v, AXVARS[a], -c, AXVARS[a], n + c, AXVARS[a], -c))
-            else:
-                w("    const int %s = ((%s + %d) %% %d + %d) %% %d;" % (v, AXVARS[a], c, n, n, n))
+        self._wrap_lines(w, "    ", set(range(self.dim)))
         self._emit_ops(range(len(L.micro)), {}, w, "    ")
         for arr in L.arrays:
             w("    w_%s[idx] = a%d;" % (arr.name, arr.root))
