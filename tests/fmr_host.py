@@ -46,8 +46,11 @@ const FmHostDim gridDim = {1u, 1u, 1u}, blockDim = {1u, 1u, 1u};
 """
 
 
-def host_source(mmp, march_chunk: int = 0, march_pair: int = 0) -> str:
-    kern, levels = emit_kernels(mmp, march_chunk=march_chunk, march_pair=march_pair)
+def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True) -> str:
+    """Host C++ of the generated kernels plus a step loop; `soft` False emits
+    the plain IEEE operations instead of the integer-pipe forms."""
+    kern, levels = emit_kernels(mmp, soft_div=soft, soft_mul=soft, soft_cmp=soft,
+                                march_chunk=march_chunk, march_pair=march_pair)
     states = [n for n, _ in mmp.state]
     stype = dict(mmp.state)
     sidx = {n: i for i, n in enumerate(states)}
@@ -98,9 +101,9 @@ class HostKernels:
     """The generated kernels of one compiled program (mm.MMProgram), built for
     the host."""
 
-    def __init__(self, mmp, march_chunk: int = 0, march_pair: int = 0):
+    def __init__(self, mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True):
         self.mmp = mmp
-        self.source = host_source(mmp, march_chunk, march_pair)
+        self.source = host_source(mmp, march_chunk, march_pair, soft)
         key = hashlib.sha256((self.source + (CSRC / "fm_softfp.cuh").read_text()).encode())
         BUILD.mkdir(parents=True, exist_ok=True)
         so = BUILD / ("k_%s.so" % key.hexdigest()[:16])

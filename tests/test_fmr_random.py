@@ -74,6 +74,20 @@ def test_extended_random_program_host_kernels_match_c_oracle(seed):
         assert np.array_equal(got[name].view(np.uint8), want[name].view(np.uint8)), (name, src)
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_random_program_plain_ieee_forms_match_c_oracle(seed):
+    """The same kernels with the integer-pipe forms switched off (plain IEEE
+    division, multiplication, fmax/fmin and comparisons)."""
+    src, shape, chunk, pair, float_q = case(seed)
+    hk = HostKernels(compile_source(src, shape), chunk, pair, soft=False)
+    assert "fm::soft::" not in hk.source
+    s0 = initial_state(seed, shape, float_q)
+    got = hk.run(s0, 5)
+    want = fmr_c.FmrOracle(src, shape).run(s0, 5)
+    for name in s0:
+        assert np.array_equal(got[name].view(np.uint8), want[name].view(np.uint8)), (name, src)
+
+
 def test_random_programs_cover_the_operation_forms():
     """The emitted kernels of the seeds above use every integer-pipe form."""
     from formura_gb300.fmr.emit_cuda import emit_kernels
