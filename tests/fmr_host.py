@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes
 import hashlib
+import re
 import subprocess
 import tempfile
 from pathlib import Path
@@ -46,18 +47,56 @@ const FmHostDim gridDim = {1u, 1u, 1u}, blockDim = {1u, 1u, 1u};
 """
 
 
-def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True) -> str:
+STORE = re.compile(r"^(\s*)(w_\w+)\[(.*)\] = (\w+);$")
+
+COUNTING = r"""
+#include <unordered_map>
+#include <vector>
+namespace {
+std::unordered_map<const void *, std::vector<int>> g_store_count;
+void count_store(const void *array, size_t i, size_t n) {
+  std::vector<int> &c = g_store_count[array];
+  if (c.empty()) c.assign(n, 0);
+  if (i < n) c[i] += 1; else c[0] += 1000000;  // an index out of range fails the check
+}
+}  // namespace
+extern "C" void fmr_host_store_counts(int *arrays, int *lo, int *hi) {
+  int a = 0, mn = 1 << 30, mx = 0;
+  for (auto &kv : g_store_count) {
+    ++a;
+    for (int c : kv.second) { mn = c < mn ? c : mn; mx = c > mx ? c : mx; }
+  }
+  *arrays = a; *lo = a ? mn : 0; *hi = mx;
+  g_store_count.clear();
+}
+"""
+
+
+def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True,
+                count_stores: bool = False) -> str:
     """Host C++ of the generated kernels plus a step loop; `soft` False emits
-    the plain IEEE operations instead of the integer-pipe forms."""
+    the plain IEEE operations instead of the integer-pipe forms.  With
+    `count_stores` every store of a kernel also counts, per array and cell, how
+    often it was written (read back by fmr_host_store_counts)."""
     kern, levels = emit_kernels(mmp, soft_div=soft, soft_mul=soft, soft_cmp=soft,
                                 march_chunk=march_chunk, march_pair=march_pair)
+    if count_stores:
+        n = int(np.prod(mmp.shape))
+        lines = []
+        for line in kern.split("\n"):
+            m = STORE.match(line)
+            if m:
+                line = "%s%s[%s] = %s; count_store(%s, (size_t)(%s), %dull);" % (
+                    m.group(1), m.group(2), m.group(3), m.group(4), m.group(2), m.group(3), n)
+            lines.append(line)
+        kern = "\n".join(lines)
     states = [n for n, _ in mmp.state]
     stype = dict(mmp.state)
     sidx = {n: i for i, n in enumerate(states)}
     arrays = sorted(mmp.arrays.values(), key=lambda a: a.node)
     aidx = {a.node: i for i, a in enumerate(arrays)}
     ncells = int(np.prod(mmp.shape))
-    out = [PRELUDE, "namespace {", kern, "}  // namespace", "",
+    out = [PRELUDE, COUNTING if count_stores else "", "namespace {", kern, "}  // namespace", "",
            'extern "C" int fmr_host_run(int steps, void **state) {',
            "  const size_t n = %dull;" % ncells,
            "  void *cur[%d], *nxt[%d], *arr[%d];" % (len(states), len(states), max(1, len(arrays))),
@@ -101,9 +140,10 @@ class HostKernels:
     """The generated kernels of one compiled program (mm.MMProgram), built for
     the host."""
 
-    def __init__(self, mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True):
+    def __init__(self, mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True,
+                 count_stores: bool = False):
         self.mmp = mmp
-        self.source = host_source(mmp, march_chunk, march_pair, soft)
+        self.source = host_source(mmp, march_chunk, march_pair, soft, count_stores)
         key = hashlib.sha256((self.source + (CSRC / "fm_softfp.cuh").read_text()).encode())
         BUILD.mkdir(parents=True, exist_ok=True)
         so = BUILD / ("k_%s.so" % key.hexdigest()[:16])
@@ -117,6 +157,7 @@ class HostKernels:
             tmp.replace(so)
         self.lib = ctypes.CDLL(str(so))
         self.lib.fmr_host_run.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        self.count_stores = count_stores
 
     def run(self, state: Dict[str, np.ndarray], steps: int) -> Dict[str, np.ndarray]:
         arrs = [np.ascontiguousarray(state[n], dtype=NP_TYPES[t]).reshape(self.mmp.shape).copy()
@@ -125,3 +166,11 @@ class HostKernels:
         if self.lib.fmr_host_run(int(steps), ptrs) != 0:
             raise MemoryError("host kernel run: allocation failed")
         return {n: a for (n, _), a in zip(self.mmp.state, arrs)}
+
+    def store_counts(self):
+        """(arrays written, fewest and most writes of one cell) since the last
+        call; needs count_stores."""
+        assert self.count_stores
+        a, lo, hi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.lib.fmr_host_store_counts(ctypes.byref(a), ctypes.byref(lo), ctypes.byref(hi))
+        return a.value, lo.value, hi.value

@@ -115,3 +115,27 @@ def test_host_kernels_reference_examples(name):
     got = HostKernels(compile_source(src, tuple(shape)), 3, 2).run(s0, 2)
     for n in want:
         assert np.array_equal(got[n].view(np.uint8), want[n].view(np.uint8)), n
+
+
+SCHEDULE_CASES = [
+    ("gray-scott-3d.fmr", [19, 8, 16], 5, 2), ("gray-scott-3d.fmr", [16, 24, 40], 16, 2),
+    ("gray-scott-3d.fmr", [7, 5, 9], 3, 2), ("gray-scott-3d.fmr", [6, 10, 12], 1, 2),
+    ("gray-scott-3d.fmr", [33, 2, 3], 4, 1), ("fmr-3d-advection.fmr", [5, 4, 33], 2, 2),
+    ("fmr-3d-advection.fmr", [9, 6, 7], 4, 2), ("fmr-features.fmr", [7, 33], 3, 1),
+    ("fmr-limiter.fmr", [24, 40], 7, 1), ("fmr-1d-float.fmr", [97], 16, 1),
+    ("diffusion-2d.fmr", [64, 48], 16, 1),
+]
+
+
+@pytest.mark.parametrize("fmr,shape,chunk,pair", SCHEDULE_CASES)
+def test_schedule_writes_every_cell_once(fmr, shape, chunk, pair):
+    """The work items of a generated kernel (columns or column pairs along
+    axis 1, chunks along axis 0, ragged last chunks) cover the grid exactly:
+    in one step every cell of every array the program writes is stored once,
+    and no store falls outside the array."""
+    p = load_program(EX / fmr, intra_node_shape=shape, march_chunk=chunk)
+    mmp = p.compiled()
+    hk = HostKernels(mmp, chunk, pair, count_stores=True)
+    hk.run(_state(p, 3), 1)
+    arrays, lo, hi = hk.store_counts()
+    assert (arrays, lo, hi) == (len(mmp.arrays), 1, 1)

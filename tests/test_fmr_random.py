@@ -99,3 +99,15 @@ def test_random_programs_cover_the_operation_forms():
     for form in ("div_const_s", "div_var_s", "prep_div_s", "scale_pow2", "mul_const_s",
                  "max_s", "min_s", "lt_s", "le_s", "eq_s", "c1b", "ha"):
         assert form in text, form
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_program_schedule_writes_every_cell_once(seed):
+    """Store counts of one step under each seed's schedule: every cell of
+    every written array exactly once."""
+    src, shape, chunk, pair, float_q = case(seed)
+    mmp = compile_source(src, shape)
+    hk = HostKernels(mmp, chunk, pair, count_stores=True)
+    hk.run(initial_state(seed, shape, float_q), 1)
+    assert hk.store_counts() == (len(mmp.arrays), 1, 1)
+
