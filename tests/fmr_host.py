@@ -54,10 +54,14 @@ COUNTING = r"""
 #include <vector>
 namespace {
 std::unordered_map<const void *, std::vector<int>> g_store_count;
-void count_store(const void *array, size_t i, size_t n) {
+// Counts a store; false (and a count that fails the check) for an index out of range,
+// whose store is then skipped.
+bool count_store(const void *array, size_t i, size_t n) {
   std::vector<int> &c = g_store_count[array];
   if (c.empty()) c.assign(n, 0);
-  if (i < n) c[i] += 1; else c[0] += 1000000;  // an index out of range fails the check
+  if (i < n) { c[i] += 1; return true; }
+  c[0] += 1000000;
+  return false;
 }
 }  // namespace
 extern "C" void fmr_host_store_counts(int *arrays, int *lo, int *hi) {
@@ -86,8 +90,8 @@ def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = Tru
         for line in kern.split("\n"):
             m = STORE.match(line)
             if m:
-                line = "%s%s[%s] = %s; count_store(%s, (size_t)(%s), %dull);" % (
-                    m.group(1), m.group(2), m.group(3), m.group(4), m.group(2), m.group(3), n)
+                line = "%sif (count_store(%s, (size_t)(%s), %dull)) %s[%s] = %s;" % (
+                    m.group(1), m.group(2), m.group(3), n, m.group(2), m.group(3), m.group(4))
             lines.append(line)
         kern = "\n".join(lines)
     states = [n for n, _ in mmp.state]
