@@ -137,6 +137,10 @@ class Program:
                 raise ValueError("%s: form fmr needs fmr_source" % self.name)
             if self.monitor_interval < 1:
                 raise ValueError("%s: monitor_interval must be >= 1" % self.name)
+            if self.march_chunk < 0:
+                raise ValueError("%s: march_chunk must be >= 0 (0 = automatic)" % self.name)
+            if self.march_pair not in (0, 1, 2):
+                raise ValueError("%s: march_pair must be 0, 1 or 2" % self.name)
             self.compiled()
             return
         if self.form not in FORMS:

@@ -1,4 +1,6 @@
 """Back-end emission: the generated-code API and its step-count semantics."""
+from pathlib import Path
+
 import pytest
 
 from formura_gb300 import backend
@@ -47,6 +49,17 @@ def test_validation():
         prog(constants=dict(F=1)).validate()
     with pytest.raises(ValueError, match="3D"):
         prog(intra_node_shape=(16, 32)).validate()
+
+
+def test_validation_of_generated_schedule_keys():
+    from formura_gb300.fmr import load_program
+
+    ex = Path(__file__).resolve().parents[1] / "examples" / "gray-scott-3d.fmr"
+    load_program(ex, intra_node_shape=[8, 8, 8], march_chunk=3, march_pair=2).validate()
+    with pytest.raises(ValueError, match="march_pair"):
+        load_program(ex, intra_node_shape=[8, 8, 8], march_pair=3).validate()
+    with pytest.raises(ValueError, match="march_chunk"):
+        load_program(ex, intra_node_shape=[8, 8, 8], march_chunk=-1).validate()
 
 
 def test_delta_rank_names_follow_toCName():
