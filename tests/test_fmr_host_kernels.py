@@ -58,6 +58,8 @@ def _check(p, pair, steps, seed=5):
     ("fmr-1d-float.fmr", dict(intra_node_shape=[7]), 0),
     ("fmr-libm.fmr", {}, 0),
     ("diffusion-2d.fmr", dict(intra_node_shape=[64, 48], march_chunk=16), 0),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[1, 4, 1], march_chunk=3), 2),
+    ("fmr-features.fmr", dict(intra_node_shape=[1, 1]), 0),
 ])
 def test_host_kernels_match_c_oracle(fmr, kw, pair):
     p = load_program(EX / fmr, **kw)
@@ -124,6 +126,10 @@ SCHEDULE_CASES = [
     ("fmr-3d-advection.fmr", [9, 6, 7], 4, 2), ("fmr-features.fmr", [7, 33], 3, 1),
     ("fmr-limiter.fmr", [24, 40], 7, 1), ("fmr-1d-float.fmr", [97], 16, 1),
     ("diffusion-2d.fmr", [64, 48], 16, 1),
+    # axes of extent 1 (every neighbour read wraps onto the cell itself), chunks longer
+    # than the axis
+    ("gray-scott-3d.fmr", [1, 4, 1], 3, 2), ("gray-scott-3d.fmr", [3, 1, 5], 50, 2),
+    ("fmr-features.fmr", [1, 1], 1, 1), ("fmr-1d-float.fmr", [1], 16, 1),
 ]
 
 
