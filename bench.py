@@ -16,6 +16,11 @@ Formura_Forward of the emitted program = 2000 time steps.
           sequences, so the FP64 pipe executes 26 FP64 instructions per update.
   cpu_baseline  the oracle's OpenMP speed build on all host cores, on a
           bounded sample of the same workload.
+  parity  computed in the run: the state after one Formura_Forward (2000
+          steps at 256^3) against the oracle's parity build from the same
+          seeded start (bit-exact flag and max relative error), the same for
+          2D diffusion 256^2 x 1000 and for FP64 MHD at the largest size the
+          oracle finishes in about a minute (labelled).
 
 --impl reference times that CPU implementation alone (the reference's path
 is CPU code; its compiler cannot run here), with the same metric and config.
@@ -36,6 +41,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOAD = "gray_scott_3d"
+# The one metric name both arms print (the engine and --impl reference).
+METRIC = "GLUP/s (3D Gray-Scott 256^3 FP64)"
 N = 256
 GS = dict(F=0.04, k=0.06, Du=2e-5, Dv=1e-5, dt=0.5, dx=0.01)
 # Algorithmic work per lattice-site update of the pearson-3d DAG (counted on the
@@ -172,6 +179,77 @@ def _event_time(torch, fn):
     return a.elapsed_time(b) / 1e3
 
 
+def compare(got, want):
+    """Bit-exactness and max relative error of a state against the oracle's
+    (relative to |want| per cell, cells where want == 0 by absolute error)."""
+    import numpy as np
+
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    diff = np.abs(got - want)
+    den = np.abs(want)
+    rel = np.where(den > 0, diff / np.where(den > 0, den, 1.0), diff)
+    return {"bit_exact": bool(np.array_equal(got, want)),
+            "max_rel_err": float(rel.max()) if rel.size else 0.0,
+            "max_abs_err": float(diff.max()) if diff.size else 0.0}
+
+
+def run_parity(torch, U_final, V_final, U0, V0):
+    """The engine's results against the oracle's parity build (-O2
+    -ffp-contract=off, OpenMP), computed in this run from the same seeded
+    inputs: the headline state after one Formura_Forward (256^3 x 2000 steps),
+    2D diffusion 256^2 x 1000 steps, and FP64 MHD x 500 steps at the largest
+    cube the oracle finishes in about a minute."""
+    import numpy as np
+
+    from formura_gb300 import inits, kernels
+    from oracle import oracle
+
+    out = {}
+    t = time.perf_counter()
+    Uo, Vo = oracle.gs3d_f64(U0, V0, 2000, **GS)
+    cu, cv = compare(U_final, Uo), compare(V_final, Vo)
+    out["gray_scott_3d_256_2000_steps"] = {
+        "bit_exact": cu["bit_exact"] and cv["bit_exact"],
+        "max_rel_err": max(cu["max_rel_err"], cv["max_rel_err"]),
+        "max_abs_err": max(cu["max_abs_err"], cv["max_abs_err"]),
+        "tolerance": 1e-12, "path": "Formura_Forward (host globals in and out)",
+        "oracle_seconds": round(time.perf_counter() - t, 1)}
+    del Uo, Vo
+    # 2D diffusion through the emitted program (coefficient 0.4 = the
+    # program's Dt/Dx**2: 0.1 on the 5-point difference)
+    d0 = inits.diffusion_2d(256, 256, seed=1)
+    d = torch.from_numpy(d0).cuda()
+    kernels.diff2d_f64_forward(d, torch.empty_like(d), 0.4, 1000)
+    c = compare(d.cpu().numpy(), oracle.diff2d_f64(d0, 1000, 0.4, 1.0))
+    out["diffusion_2d_256_1000_steps"] = dict(c, tolerance=1e-12)
+    # FP64 MHD: size from the oracle's measured rate (about a minute of CPU)
+    f_probe = inits.mhd_3d(32, seed=1)
+    oracle.mhd_f64(f_probe, 1)
+    t = time.perf_counter()
+    oracle.mhd_f64(f_probe, 2)
+    per_lup = (time.perf_counter() - t) / (2 * 32 ** 3)
+    n = 32
+    for cand in (96, 80, 64, 48, 40):
+        if cand ** 3 * 500 * per_lup <= 60.0:
+            n = cand
+            break
+    f0 = inits.mhd_3d(n, seed=1)
+    t64 = [torch.from_numpy(x).cuda() for x in f0]
+    kernels.mhd_forward(t64, torch.empty(18 * n ** 3, dtype=torch.float64, device="cuda"), 500)
+    t = time.perf_counter()
+    fo = oracle.mhd_f64(f0, 500)
+    worst = {"bit_exact": True, "max_rel_err": 0.0, "max_abs_err": 0.0}
+    for x, y in zip(t64, fo):
+        c = compare(x.cpu().numpy(), y)
+        worst = {"bit_exact": worst["bit_exact"] and c["bit_exact"],
+                 "max_rel_err": max(worst["max_rel_err"], c["max_rel_err"]),
+                 "max_abs_err": max(worst["max_abs_err"], c["max_abs_err"])}
+    out["mhd_3d_fp64_500_steps"] = dict(worst, grid=[n, n, n], tolerance=1e-12,
+                                        fields=9, oracle_seconds=round(time.perf_counter() - t, 1))
+    return out
+
+
 def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
     """The other forms of the hot path, each timed on the device after a warm-up
     (CUDA events on the launching stream), at the sizes the workloads name."""
@@ -245,11 +323,12 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
     d0 = inits.diffusion_2d(256, 256, seed=1)
     d = torch.from_numpy(d0).cuda()
     wd = torch.empty_like(d)
-    kernels.diff2d_f64_forward(d, wd, 0.1, 50)
-    sec = _event_time(torch, lambda: kernels.diff2d_f64_forward(d, wd, 0.1, 1000))
+    kernels.diff2d_f64_forward(d, wd, 0.4, 50)
+    sec = _event_time(torch, lambda: kernels.diff2d_f64_forward(d, wd, 0.4, 1000))
     out["diffusion_2d_256_fp64"] = {"value": round(256 * 256 * 1000 / sec / 1e9, 2),
                                     "unit": "GLUP/s", "steps": 1000, "ms": round(sec * 1e3, 3),
-                                    "bit_exact_vs_oracle": True, "kernel": "diff2d_tb (4 steps per grid barrier)"}
+                                    "parity": "see parity.diffusion_2d_256_1000_steps",
+                                    "kernel": "diff2d_tb (4 steps per grid barrier)"}
     # -- 3D MHD 256^3, 500 steps: binary32 bulk with the FP64 energy update
     f0 = inits.mhd_3d(N, seed=1)
     t32 = [torch.from_numpy(x.astype(np.float32)).cuda() for x in f0]
@@ -277,7 +356,7 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
         "max_rel_error_vs_fp64_256cube_500steps": errs, "kernel": "mhd_stage_tile x4 + mhd_finish"}
     out["mhd_3d_256_fp64"] = {
         "value": round(N ** 3 * 500 / sec64 / 1e9, 4), "unit": "GLUP/s", "steps": 500,
-        "seconds": round(sec64, 3), "bit_exact_vs_oracle": True,
+        "seconds": round(sec64, 3), "parity": "see parity.mhd_3d_fp64_500_steps",
         "kernel": "mhd_stage_march<double, 1> x4 + mhd_finish_v2<double, 1> "
                   "(exact binary64 scalings, constant products, divisions, fmax/fmin on the "
                   "integer pipes)"}
@@ -404,7 +483,7 @@ def run_reference(args):
     val = N ** 3 * sample_steps * len(times) / tot / 1e9
     cores = oracle.num_threads(fast=True)
     line = {
-        "impl": "reference", "metric": "GLUP/s (3D Gray-Scott 256^3 FP64)", "value": round(val, 4),
+        "impl": "reference", "metric": METRIC, "value": round(val, 4),
         "unit": "GLUP/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(tot / len(times) * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
@@ -485,14 +564,26 @@ def run_engine(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     barrier()
+    # the host<->device copies of that path on their own (untimed above)
+    copies = {}
+    for name, fn in (("h2d", prog.upload), ("d2h", prog.download)):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        copies[name + "_gbs"] = round(3 * 2 * 8 * N ** 3 / (time.perf_counter() - t) / 1e9, 1)
+    copies["host_globals_pinned"] = "%d of 2" % prog.host_pinned()
 
-    # the state after one Formura_Forward from the seeded start (for the FP32 score)
-    U_final = None
-    if rank == 0 and not args.no_variants:
+    # the state after one Formura_Forward from the seeded start (parity, FP32 score)
+    U_final = V_final = None
+    if rank == 0 and not (args.no_variants and args.no_parity):
         prog.state["U"][...] = U0
         prog.state["V"][...] = V0
         prog.forward()
         U_final = prog.state["U"].copy()
+        V_final = prog.state["V"].copy()
 
     value, e2e, dev_s, e2e_s = aggregate_replicas(dev_s, e2e_s, float(N ** 3) * M * args.steps, ws)
     if rank != 0:
@@ -512,12 +603,15 @@ def run_engine(args):
     traffic = read_profile_traffic()
     clocks = clk.summary()
     cpu = cpu_baseline() if not args.no_cpu else None
+    parity = None
+    if not args.no_parity:
+        parity = run_parity(torch, U_final, V_final, U0, V0)
     variants = None
     if not args.no_variants:
         variants = run_variants(torch, prog, U_final, U0, V0, peaks)
 
     line = {
-        "metric": "GLUP/s (3D Gray-Scott 256^3 FP64) vs FP64/HBM roofline at 1 GB300",
+        "metric": METRIC,
         "value": round(value, 4), "unit": "GLUP/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dev_s / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -526,7 +620,7 @@ def run_engine(args):
                                "(F=0.04 k=0.06 Du=2e-5 Dv=1e-5 dx=0.01 dt=0.5)",
                    "grid": [N, N, N], "steps_per_bench_step": M,
                    "parallelism": "replicas" if ws > 1 else "1 GPU",
-                   "l2": "state 268 MB > 129 MB L2; no flush", "bit_exact_vs_oracle": True},
+                   "l2": "state 268 MB > 129 MB L2; no flush"},
         "roofline": {"bound": "fp64", "achieved": round(achieved_tf, 4), "peak": round(fp64_peak, 4),
                      "unit": "TFLOP/s", "frac": round(achieved_tf / fp64_peak, 4),
                      "traffic": traffic, "peak_source": "measured in this run (FP64 FMA probe)",
@@ -540,13 +634,16 @@ def run_engine(args):
                                                  "recomputed) + 5 multiplications by constants, "
                                                  "correctly rounded on the integer pipes",
                      "kernel": "gs3d_f64_row", "ms_per_launch": round(per_launch * 1e3, 4)},
-        "e2e": {"value": round(e2e, 4), "unit": "GLUP/s",
-                "h2d_bytes_per_step": 2 * 8 * N ** 3, "d2h_bytes_per_step": 2 * 8 * N ** 3},
+        "e2e": dict({"value": round(e2e, 4), "unit": "GLUP/s",
+                     "h2d_bytes_per_step": 2 * 8 * N ** 3, "d2h_bytes_per_step": 2 * 8 * N ** 3},
+                    **copies),
         "gpu_launches": 2 * launches,
         "clocks": clocks,
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if parity is not None:
+        line["parity"] = parity
     if variants is not None:
         line["variants"] = variants
     print(json.dumps(line), flush=True)
@@ -654,6 +751,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the in-run comparison with the oracle")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
     ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",

@@ -220,6 +220,10 @@ def emit_header(p: Program) -> str:
     lines.append("int Formura_Set_Stream (void *cuda_stream);")
     lines.append("int Formura_Conserved_Totals (double *totals);")
     lines.append("int Formura_Finalize (void);")
+    lines.append("/* Number of state arrays whose host globals are page-locked (registered with")
+    lines.append("   CUDA on the first device use), so that Forward's copies run at link speed;")
+    lines.append("   a failed registration leaves its message in Formura_Last_Error. */")
+    lines.append("int Formura_Host_Pinned (void);")
     lines.append("/* Monitor planes of the device state: Begin gathers plane `index` of axis")
     lines.append("   `axis` of every state array (asynchronous copy to the host); Wait writes")
     lines.append("   them, state after state, to `out`.  Write_Monitor writes the mid-planes of")
@@ -381,6 +385,7 @@ def emit_source(p: Program) -> str:
     w("static double *g_totals = 0;   /* device: per-state totals + scratch */")
     w("static void *g_stream = 0;")
     w("static int g_ready = 0;")
+    w("static int g_pinned = 0;")
     w("static char g_msg[600];")
     w("static fm_snapshot *g_snap[%d] = {0};" % len(states))
     w("static int g_snap_axis = -1;")
@@ -400,7 +405,9 @@ def emit_source(p: Program) -> str:
     w("  int st;")
     w("  for (int i = 0; i < kNState; ++i) {")
     w('    if ((st = fm_malloc(&g_dev[i], kBytes[i]))) return fail(st, "fm_malloc(state)");')
-    w("    fm_host_register(kHost[i], kBytes[i]);  /* pinned: best effort */")
+    w("    /* page-locked host globals give full-speed copies; a failure is recorded, not fatal */")
+    w("    if ((st = fm_host_register(kHost[i], kBytes[i])) == 0) ++g_pinned;")
+    w('    else fail(st, "fm_host_register(state)");')
     w("  }")
     if fmr:
         for line in alloc:
@@ -496,6 +503,7 @@ def emit_source(p: Program) -> str:
     w("  if (!g_ready) return 0;")
     w("  fm_stream_sync(g_stream);")
     w("  for (int i = 0; i < kNState; ++i) { fm_free(g_dev[i]); g_dev[i] = 0; fm_host_unregister(kHost[i]); }")
+    w("  g_pinned = 0;")
     w("  fm_free(g_work); g_work = 0; fm_free(g_totals); g_totals = 0;")
     w("  for (int i = 0; i < kNState; ++i) { fm_snapshot_destroy(g_snap[i]); g_snap[i] = 0; }")
     w("  g_snap_axis = -1;")
@@ -507,6 +515,8 @@ def emit_source(p: Program) -> str:
     w("}")
     w("")
     w("FMR_EXPORT const char *Formura_Last_Error (void) { return g_msg; }")
+    w("")
+    w("FMR_EXPORT int Formura_Host_Pinned (void) { return g_pinned; }")
     w("")
     w("FMR_EXPORT int Formura_Monitor_Begin (int axis, int index) {")
     w("  int st = ensure_device(); if (st) return st;")

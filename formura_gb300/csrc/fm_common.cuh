@@ -38,9 +38,14 @@ int cuda_status(cudaError_t e, const char *what);
 // Number of SMs and max cooperative grid helpers (cached per device).
 int device_sm_count(int *sms);
 
-// Bounded spin limit for device-side waits: a wait that exceeds it records an
-// error word and returns instead of hanging the GPU.
-constexpr long long kSpinLimit = 20000000;  // ~ seconds with __nanosleep
+// Bounded spin limit for the grid barriers of the persistent kernels: a wait
+// that exceeds it records an error word and returns instead of hanging the
+// GPU.  The default (~ seconds with __nanosleep) can be lowered per process
+// with the tuning knob "sync.spin_limit" (polls, >= 1), which the failure
+// tests use to make a wait run out; spin_limit() reads it on the host and the
+// kernels receive the value as an argument.
+constexpr long long kSpinLimitDefault = 20000000;
+long long spin_limit();
 
 __device__ __forceinline__ int wrap_dn(int i, int n) { return i == 0 ? n - 1 : i - 1; }
 __device__ __forceinline__ int wrap_up(int i, int n) { return i + 1 == n ? 0 : i + 1; }

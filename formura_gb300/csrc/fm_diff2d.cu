@@ -5,8 +5,8 @@
 // FP64 work spread over every SM.  Launch overhead would dominate, so all
 // steps run in ONE cooperative persistent launch; blocks meet at a grid
 // barrier between steps.  Every wait in that barrier is bounded: past
-// fm::kSpinLimit polls the block sets an error word and all blocks return, and
-// the entry point reports FM_ERR_TIMEOUT.
+// fm::spin_limit() polls the block sets an error word and all blocks return,
+// and the entry point reports FM_ERR_TIMEOUT.
 //
 // Per cell (diffusion.fmr:5-7,20):  lap_a = ((d[+1]-d)/2 - (d-d[-1])/2)/2,
 //   dens' = dens + coef*(lap_x + lap_y).  x/2 is evaluated as x*0.5 — the same
@@ -35,7 +35,8 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
 }
 
 // Grid-wide barrier for a cooperative launch; false if the wait gave up.
-__device__ bool grid_barrier(GridSync *gs, unsigned nblocks, unsigned &gen_local) {
+__device__ bool grid_barrier(GridSync *gs, unsigned nblocks, unsigned &gen_local,
+                             long long limit) {
   __shared__ int s_fail;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -49,7 +50,7 @@ __device__ bool grid_barrier(GridSync *gs, unsigned nblocks, unsigned &gen_local
     } else {
       long long spins = 0;
       while (ld_acquire_u32(&gs->gen) != target) {
-        if (++spins > fm::kSpinLimit || *((volatile int *)&gs->err) != 0) {
+        if (++spins > limit || *((volatile int *)&gs->err) != 0) {
           atomicExch(&gs->err, 1);
           fail = 1;
           break;
@@ -87,7 +88,7 @@ __device__ __forceinline__ double diff_cell(const double *__restrict__ src, int 
 
 __global__ void __launch_bounds__(256)
     diff2d_persistent(double *a, double *b, int nx, int ny, double coef, int steps,
-                      GridSync *gs) {
+                      GridSync *gs, long long limit) {
   const int lane = threadIdx.x & 31;
   const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -101,7 +102,7 @@ __global__ void __launch_bounds__(256)
       const int y = (sg % segs_per_row) * 32 + lane;
       __stcg(dst + (size_t)x * ny + y, diff_cell(src, x, y, nx, ny, lane, coef));
     }
-    if (!grid_barrier(gs, gridDim.x, gen)) return;
+    if (!grid_barrier(gs, gridDim.x, gen, limit)) return;
     double *t = src;
     src = dst;
     dst = t;
@@ -145,7 +146,7 @@ constexpr int kDX = 16, kDY = 32;
 template <int K>
 __global__ void __launch_bounds__(256)
     diff2d_tb(double *a, double *b, int nx, int ny, double coef, fm::soft::MulConstS cs,
-              int soft_coef, int steps, int ntx, int nty, GridSync *gs) {
+              int soft_coef, int steps, int ntx, int nty, GridSync *gs, long long limit) {
   constexpr int RX = kDX + 2 * K, RY = kDY + 2 * K;
   __shared__ double buf[2][RX][RY];
   unsigned gen = 0;
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(256)
       }
       __syncthreads();
     }
-    if (!grid_barrier(gs, gridDim.x, gen)) return;
+    if (!grid_barrier(gs, gridDim.x, gen, limit)) return;
     double *tmp = src;
     src = dst;
     dst = tmp;
@@ -289,7 +290,8 @@ extern "C" int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
       double *a = dens, *b = work;
       int nxv = nx, nyv = ny, stv = steps, ntxv = ntx, ntyv = nty;
       double cf = coef;
-      void *args[] = {&a, &b, &nxv, &nyv, &cf, &cs, &soft, &stv, &ntxv, &ntyv, &gs};
+      long long lim = fm::spin_limit();
+      void *args[] = {&a, &b, &nxv, &nyv, &cf, &cs, &soft, &stv, &ntxv, &ntyv, &gs, &lim};
       FM_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s));
       GridSync host;
       FM_TRY_CUDA(cudaMemcpyAsync(&host, gs, sizeof(GridSync), cudaMemcpyDeviceToHost, s));
@@ -312,7 +314,8 @@ extern "C" int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
     double *a = dens, *b = work;
     int nxv = nx, nyv = ny, stv = steps;
     double cf = coef;
-    void *args[] = {&a, &b, &nxv, &nyv, &cf, &stv, &gs};
+    long long lim = fm::spin_limit();
+    void *args[] = {&a, &b, &nxv, &nyv, &cf, &stv, &gs, &lim};
     FM_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)diff2d_persistent, dim3(want),
                                             dim3(256), args, 0, s));
     GridSync host;
@@ -404,7 +407,7 @@ extern "C" int fm_diff2d_f64_forward_noalloc(int nx, int ny, double *dens, doubl
   NoAllocScratch sc;
   int st = noalloc_scratch(&sc);
   if (st) return st;
-  int dev = 0, coop = 0, sms = 0, per_sm = 0;
+  int dev = 0, coop = 0, sms = 0;
   FM_TRY_CUDA(cudaGetDevice(&dev));
   FM_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
   if (!coop) {
@@ -413,32 +416,58 @@ extern "C" int fm_diff2d_f64_forward_noalloc(int nx, int ny, double *dens, doubl
   }
   st = fm::device_sm_count(&sms);
   if (st) return st;
-  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, diff2d_persistent, 256, 0));
+  // The kernel of fm_diff2d_f64_forward: diff2d_tb<K> with K steps per grid
+  // barrier ("diff2d.tb", default 4), or one step per barrier for tb 0.
+  const int tb = fm::tune_get("diff2d.tb", 4);
+  const bool tiled = tb == 2 || tb == 4 || tb == 8;
+  const void *fn = !tiled    ? (const void *)diff2d_persistent
+                   : tb == 2 ? (const void *)diff2d_tb<2>
+                   : tb == 4 ? (const void *)diff2d_tb<4>
+                             : (const void *)diff2d_tb<8>;
+  int per_sm = 0;
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0));
   if (per_sm < 1) {
     fm::set_error("fm_diff2d_f64_forward_noalloc: kernel does not fit on an SM");
     return FM_ERR_UNSUPPORTED;
   }
-  const long long nseg = (long long)nx * (ny / 32);
-  const int grid = (int)std::max<long long>(
-      1, std::min<long long>((nseg + 7) / 8, (long long)sms * std::min(per_sm, 2)));
   // The barrier word keeps the previous call's contents: it must start at zero.
   FM_TRY_CUDA(cudaMemsetAsync(sc.sync, 0, sizeof(GridSync), s));
   double *a = dens, *b = sc.work;
   int nxv = nx, nyv = ny, stv = steps;
   double cf = coef;
   GridSync *gs = sc.sync;
-  void *args[] = {&a, &b, &nxv, &nyv, &cf, &stv, &gs};
-  FM_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)diff2d_persistent, dim3(grid), dim3(256),
-                                          args, 0, s));
+  long long lim = fm::spin_limit();
+  bool odd;
+  if (tiled) {
+    const int ntx = (nx + kDX - 1) / kDX, nty = (ny + kDY - 1) / kDY;
+    const int grid = (int)std::min<long long>((long long)ntx * nty, (long long)sms * per_sm);
+    const double ac = coef < 0 ? -coef : coef;
+    int soft = ac >= 0x1p-1022 && ac <= 0x1.fffffffffffffp1023;
+    fm::soft::MulConstS cs = soft ? fm::soft::make_mul_const_s(coef) : fm::soft::MulConstS();
+    int ntxv = ntx, ntyv = nty;
+    void *args[] = {&a, &b, &nxv, &nyv, &cf, &cs, &soft, &stv, &ntxv, &ntyv, &gs, &lim};
+    FM_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s));
+    odd = ((steps + tb - 1) / tb) & 1;
+  } else {
+    const long long nseg = (long long)nx * (ny / 32);
+    const int grid = (int)std::max<long long>(
+        1, std::min<long long>((nseg + 7) / 8, (long long)sms * std::min(per_sm, 2)));
+    void *args[] = {&a, &b, &nxv, &nyv, &cf, &stv, &gs, &lim};
+    FM_TRY_CUDA(cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(256), args, 0, s));
+    odd = steps & 1;
+  }
   GridSync host;
   FM_TRY_CUDA(cudaMemcpyAsync(&host, sc.sync, sizeof(GridSync), cudaMemcpyDeviceToHost, s));
+  // After an odd number of passes the result is in the static scratch: the
+  // copy back into dens is queued before the synchronization below, so that
+  // dens is final (and the scratch free for the next call) when this returns.
+  if (odd)
+    FM_TRY_CUDA(cudaMemcpyAsync(dens, sc.work, (size_t)nx * ny * sizeof(double),
+                                cudaMemcpyDeviceToDevice, s));
   FM_TRY_CUDA(cudaStreamSynchronize(s));
   if (host.err) {
     fm::set_error("fm_diff2d_f64_forward_noalloc: grid barrier wait gave up");
     return FM_ERR_TIMEOUT;
   }
-  if (steps & 1)
-    FM_TRY_CUDA(cudaMemcpyAsync(dens, sc.work, (size_t)nx * ny * sizeof(double),
-                                cudaMemcpyDeviceToDevice, s));
   return FM_OK;
 }

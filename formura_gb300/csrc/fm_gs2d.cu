@@ -46,7 +46,8 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   return v;
 }
 
-__device__ bool grid_barrier(GridSync *gs, unsigned nblocks, unsigned &gen_local) {
+__device__ bool grid_barrier(GridSync *gs, unsigned nblocks, unsigned &gen_local,
+                             long long limit) {
   __shared__ int s_fail;
   __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -60,7 +61,7 @@ __device__ bool grid_barrier(GridSync *gs, unsigned nblocks, unsigned &gen_local
     } else {
       long long spins = 0;
       while (ld_acquire_u32(&gs->gen) != target) {
-        if (++spins > fm::kSpinLimit || *((volatile int *)&gs->err) != 0) {
+        if (++spins > limit || *((volatile int *)&gs->err) != 0) {
           atomicExch(&gs->err, 1);
           fail = 1;
           break;
@@ -151,7 +152,7 @@ template <int TS, int T>
 __global__ void __launch_bounds__(256)
     gs2d_ensemble(const EnsInst *__restrict__ insts, const EnsTile *__restrict__ tiles,
                   int ntiles, float *U0, float *V0, float *U1, float *V1, int steps, int tb,
-                  GridSync *gs) {
+                  GridSync *gs, long long limit) {
   constexpr int R = TS + 2 * T;  // region edge
   extern __shared__ float sm[];
   // buffer b of field f at sm + (2*f + b) * R*R
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(256)
       }
       __syncthreads();
     }
-    if (!grid_barrier(gs, gridDim.x, gen)) return;
+    if (!grid_barrier(gs, gridDim.x, gen, limit)) return;
   }
 }
 
@@ -243,7 +244,8 @@ constexpr int kWfWidth = 64;
 template <int T>
 __global__ void __launch_bounds__(128)
     gs2d_ens_wf(const EnsInst *__restrict__ insts, const WfTile *__restrict__ tiles, int ntiles,
-                float *U0, float *V0, float *U1, float *V1, int steps, int tb, GridSync *gs) {
+                float *U0, float *V0, float *U1, float *V1, int steps, int tb, GridSync *gs,
+                long long limit) {
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * 4 + (threadIdx.x >> 5);
   const int nw = gridDim.x * 4;
@@ -366,7 +368,7 @@ __global__ void __launch_bounds__(128)
         }
       }
     }
-    if (!grid_barrier(gs, gridDim.x, gen)) return;
+    if (!grid_barrier(gs, gridDim.x, gen, limit)) return;
   }
 }
 
@@ -389,6 +391,7 @@ struct fm_ensemble {
   cudaGraphExec_t gexec = nullptr;
   const void *g_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   int g_steps = -1;
+  long long g_limit = -1;
   cudaStream_t g_stream = nullptr;
 };
 
@@ -602,7 +605,7 @@ int ens_prepare(fm_ensemble *e, EnsLaunch *L) {
 }
 
 int ens_launch(fm_ensemble *e, const EnsLaunch &L, float *U, float *V, float *wU, float *wV,
-               int steps, cudaStream_t s) {
+               int steps, long long limit, cudaStream_t s) {
   const void *kern = L.kern;
   const size_t smem = L.smem;
   const int grid = L.grid;
@@ -611,7 +614,7 @@ int ens_launch(fm_ensemble *e, const EnsLaunch &L, float *U, float *V, float *wU
   const EnsTile *dt = e->d_tiles;
   int nt = e->ntiles, stp = steps, tb = e->tb;
   GridSync *gs = e->d_sync;
-  void *args[] = {&di, &dt, &nt, &U, &V, &wU, &wV, &stp, &tb, &gs};
+  void *args[] = {&di, &dt, &nt, &U, &V, &wU, &wV, &stp, &tb, &gs, &limit};
   FM_TRY_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), e->kind == 1 ? dim3(128) : dim3(32, 8),
                                           args, smem, s));
   return FM_OK;
@@ -629,9 +632,10 @@ extern "C" int fm_gs2d_ensemble_forward(fm_ensemble *e, float *U, float *V, floa
   EnsLaunch L;
   int pst = ens_prepare(e, &L);
   if (pst) return pst;
+  const long long limit = fm::spin_limit();
   if (use_graph) {
     const void *key[5] = {U, V, work_U, work_V, s};
-    bool same = e->gexec && e->g_steps == steps;
+    bool same = e->gexec && e->g_steps == steps && e->g_limit == limit;
     for (int i = 0; i < 5 && same; ++i) same = e->g_key[i] == key[i];
     if (!same) {
       if (e->gexec) {
@@ -643,7 +647,7 @@ extern "C" int fm_gs2d_ensemble_forward(fm_ensemble *e, float *U, float *V, floa
       cudaGraph_t g = nullptr;
       cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
       int st = FM_OK;
-      if (ce == cudaSuccess) st = ens_launch(e, L, U, V, work_U, work_V, steps, cap);
+      if (ce == cudaSuccess) st = ens_launch(e, L, U, V, work_U, work_V, steps, limit, cap);
       cudaError_t ee = cudaStreamEndCapture(cap, &g);
       cudaStreamDestroy(cap);
       if (ce != cudaSuccess) return fm::cuda_status(ce, "cudaStreamBeginCapture");
@@ -660,10 +664,11 @@ extern "C" int fm_gs2d_ensemble_forward(fm_ensemble *e, float *U, float *V, floa
       }
       for (int i = 0; i < 5; ++i) e->g_key[i] = key[i];
       e->g_steps = steps;
+      e->g_limit = limit;
     }
     FM_TRY_CUDA(cudaGraphLaunch(e->gexec, s));
   } else {
-    int st = ens_launch(e, L, U, V, work_U, work_V, steps, s);
+    int st = ens_launch(e, L, U, V, work_U, work_V, steps, limit, s);
     if (st) return st;
   }
   // Result lands in work_* after an odd number of time blocks: copy back.

@@ -20,6 +20,11 @@ int tune_get(const char *key, int fallback) {
   auto it = knobs().find(key);
   return it == knobs().end() ? fallback : it->second;
 }
+
+long long spin_limit() {
+  const int v = tune_get("sync.spin_limit", 0);
+  return v >= 1 ? (long long)v : kSpinLimitDefault;
+}
 }  // namespace fm
 
 extern "C" int fm_tune_set(const char *key, int value) {

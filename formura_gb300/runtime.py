@@ -140,6 +140,11 @@ class FormuraProgram:
         self._check(self.lib.Formura_Write_Monitor(str(directory).encode(), int(rank)),
                     "Formura_Write_Monitor")
 
+    def host_pinned(self) -> int:
+        """How many state arrays' host globals are page-locked (0 before the
+        first device use)."""
+        return int(self.lib.Formura_Host_Pinned())
+
     def finalize(self):
         self._check(self.lib.Formura_Finalize(), "Formura_Finalize")
 

@@ -156,7 +156,8 @@ int fm_gs2d_f32_forward(int nx, int ny, float *U, float *V, float *work_U,
  * fm_gs2d_ensemble_forward advances every instance `steps` steps in ONE
  * cooperative persistent launch (grid barrier between passes, bounded
  * waits); with use_graph != 0 the launch is captured once into a CUDA graph
- * (re-captured when the buffers, stream or step count change) and replayed.
+ * (re-captured when the buffers, stream, step count or "sync.spin_limit"
+ * change) and replayed.
  * work_U, work_V: ping-pong buffers of total_cells floats.
  * fm_gs2d_ensemble_status synchronizes `stream` and returns FM_ERR_TIMEOUT if
  * the last run's grid barrier gave up.
@@ -306,13 +307,17 @@ int fm_diff2d_f64_forward(int nx, int ny, double *dens, double *work,
  * library, which every GPU that loads the library holds until the process
  * exits.  nx*ny above FM_DIFF2D_NOALLOC_MAX_CELLS returns FM_ERR_ARG.
  *
- * Same results, bit for bit, as fm_diff2d_f64_forward.  The first call on a
+ * Runs the kernel of fm_diff2d_f64_forward (the same "diff2d.tb" choice) on
+ * the static scratch: same results, bit for bit.  The first call on a
  * device looks up the scratch's device address (cudaGetSymbolAddress), which
  * may load the library's device code on that device; make that first call
  * before any stream capture.  Every call shares the one scratch area, so
  * calls whose work overlaps on the GPU (different streams, or different host
  * threads, without ordering between them) race; the barrier word is cleared
- * at the start of each call.  Synchronizes `stream` before returning.
+ * at the start of each call.  Synchronizes `stream` before returning, after
+ * every copy of the call (including the copy of the result out of the
+ * scratch), so on return dens is final for any stream and the scratch is
+ * free for the next call.
  */
 #define FM_DIFF2D_NOALLOC_MAX_CELLS (1 << 20)
 int fm_diff2d_f64_forward_noalloc(int nx, int ny, double *dens, double coef,
@@ -391,6 +396,12 @@ void fm_snapshot_destroy(fm_snapshot *s);
  *                      computing each slope and face flux once, all fields per plane
  *                      (default for f64), 0 per-point kernel (default for f32)
  *   "mhd.xchunk"       x planes per tile of the x-marching kernel (0 = automatic)
+ *   "sync.spin_limit"  polls before a grid-barrier wait of the persistent kernels
+ *                      (fm_diff2d_f64_forward[_noalloc], fm_gs2d_ensemble_forward) gives
+ *                      up, sets the error word and returns FM_ERR_TIMEOUT (>= 1; default
+ *                      20,000,000, seconds of waiting).  A small value makes the waits run
+ *                      out on purpose, to test the timeout path; it does not change results
+ *                      of runs that finish
  *   "conv.kernel"      fm_conv3x3_fwd_bf16 with 64 output channels: 1 weight-resident
  *                      persistent kernel (default; falls back to 0 when its staged region
  *                      does not fit in shared memory), 2 the same with its regions and

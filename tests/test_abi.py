@@ -151,3 +151,103 @@ def test_argument_validation_of_the_other_entry_points(core_lib):
     assert core_lib.fm_conv3x3_fwd_bf16(1, 8, 8, 48, fake, fake, None, None, None, 0, None, fake,
                                         None, err, None) == 1  # cout 32 or 64
     assert core_lib.fm_diff2d_f64_forward_noalloc(2048, 1024, fake, 0.1, 1, None) == 1  # > 2^20
+
+
+# A C++ driver in the shape of the reference's examples/diffusion-main.cpp:
+# <mpi.h> (here the single-process header), `Formura_Navigator navi;`,
+# MPI_Init, Formura_Init(&navi, MPI_COMM_WORLD), Formura_Forward in a loop until
+# T_MAX, MPI_Finalize.  It also loads the initial state from argv[1] into the
+# globals between lower and upper, and writes the final state to argv[2].
+CPP_DRIVER = r'''
+#include <stdio.h>
+#include <mpi.h>
+#include "%(name)s.h"
+
+const int T_MAX = %(tmax)d;
+
+int main (int argc, char **argv) {
+  Formura_Navigator navi;
+  MPI_Init(&argc, &argv);
+  Formura_Init(&navi, MPI_COMM_WORLD);
+  FILE *in = fopen(argv[1], "rb");
+  for (int x = navi.lower_x; x < navi.upper_x; ++x)
+    if (fread(%(state)s[x] + navi.lower_y, sizeof(double), navi.upper_y - navi.lower_y, in) == 0)
+      return 3;
+  fclose(in);
+  while(navi.time_step < T_MAX) {
+    if (Formura_Forward(&navi) != 0) { printf("error %%s\n", Formura_Last_Error()); return 2; }
+    printf("t = %%d\n", navi.time_step);
+  }
+  FILE *out = fopen(argv[2], "wb");
+  for (int x = navi.lower_x; x < navi.upper_x; ++x)
+    fwrite(%(state)s[x] + navi.lower_y, sizeof(double), navi.upper_y - navi.lower_y, out);
+  fclose(out);
+  MPI_Finalize();
+}
+'''
+
+
+def _build_cpp_driver(tmp_path, prog, state, tmax):
+    so = backend.build_program(prog, outdir=tmp_path)
+    src = tmp_path / "main.cpp"
+    src.write_text(CPP_DRIVER % dict(name=prog.name, state=state, tmax=tmax))
+    exe = tmp_path / "drv"
+    subprocess.run(["g++", "-std=c++11", "-I", str(tmp_path), "-I", str(INCLUDE / "single_process_mpi"),
+                    "-I", str(INCLUDE), str(src), "-o", str(exe), "-L", str(so.parent),
+                    "-l" + prog.name, "-Wl,-rpath," + str(so.parent)], check=True)
+    return exe
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fmr", [False, True])
+def test_reference_style_driver_runs_on_gpu(tmp_path, cuda_device, fmr):
+    """The driver loop of examples/diffusion-main.cpp on the GPU, against the
+    hand-tuned diffusion program and against the same program compiled by the
+    front end from examples/diffusion-2d.fmr: 5 Forwards of 20 steps on 64 x 96,
+    the final state bit-exact with the oracle's 100 steps."""
+    import numpy as np
+
+    from formura_gb300 import inits
+    from oracle import oracle
+
+    if fmr:
+        from formura_gb300.fmr import load_program
+
+        prog = load_program(INCLUDE.parent / "examples" / "diffusion-2d.fmr", name="drv_fmr_diff",
+                            intra_node_shape=[64, 96], monitor_interval=20,
+                            mpi_grid_shape=[1, 1])
+    else:
+        prog = backend.Program(name="drv_diff_gpu", form="diff2d_f64", intra_node_shape=(64, 96),
+                               constants=dict(Dt=0.4, Dx=1.0), monitor_interval=20)
+    exe = _build_cpp_driver(tmp_path, prog, "dens", 100)
+    d0 = inits.diffusion_2d(64, 96, seed=31)
+    d0.tofile(tmp_path / "in.bin")
+    r = subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin")],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.split("\n")[:5] == ["t = %d" % t for t in (20, 40, 60, 80, 100)]
+    got = np.fromfile(tmp_path / "out.bin", dtype=np.float64).reshape(64, 96)
+    assert np.array_equal(got, oracle.diff2d_f64(d0, 100, 0.4, 1.0))
+
+
+def test_reference_diffusion_driver_compiles_unmodified(tmp_path):
+    """The reference's own examples/diffusion-main.cpp, read where it lies,
+    compiles and links unchanged against the library the front end emits for
+    the reference's examples/diffusion.fmr (shape reduced to 16^3, one rank),
+    with the single-process <mpi.h>.  (It is not run here: without a GPU,
+    Formura_Forward fails and that driver's loop never ends.)"""
+    from formura_gb300.fmr import load_program
+    from oracle import oracle
+
+    ref = oracle.DEFAULT_REFERENCE / "examples"
+    if not (ref / "diffusion-main.cpp").exists():
+        pytest.skip("reference tree absent")
+    prog = load_program(ref / "diffusion.fmr", name="diffusion", intra_node_shape=[16, 16, 16],
+                        mpi_grid_shape=[1, 1, 1])
+    so = backend.build_program(prog, outdir=tmp_path)
+    exe = tmp_path / "diffusion-main"
+    subprocess.run(["g++", "-I", str(tmp_path), "-I", str(INCLUDE / "single_process_mpi"),
+                    "-I", str(INCLUDE), str(ref / "diffusion-main.cpp"), "-o", str(exe),
+                    "-L", str(so.parent), "-ldiffusion", "-Wl,-rpath," + str(so.parent)],
+                   check=True)
+    assert exe.exists()

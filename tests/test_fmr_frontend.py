@@ -27,7 +27,7 @@ from oracle import fmr_c, oracle
 
 ROOT = Path(__file__).resolve().parents[1]
 EX = ROOT / "examples"
-REF = Path("/root/reference")
+REF = oracle.DEFAULT_REFERENCE  # FORMURA_REFERENCE, else the oracle recipe's location
 GS = dict(F=0.04, k=0.06, Du=2e-5, Dv=1e-5, dt=0.5, dx=0.01)
 
 

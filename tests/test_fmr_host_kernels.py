@@ -15,12 +15,12 @@ import pytest
 
 from formura_gb300 import inits
 from formura_gb300.fmr import load_program
-from oracle import fmr_c
+from oracle import fmr_c, oracle
 
 from fmr_host import HostKernels
 
 EX = Path(__file__).resolve().parents[1] / "examples"
-REF = Path("/root/reference")
+REF = oracle.DEFAULT_REFERENCE  # FORMURA_REFERENCE, else the oracle recipe's location
 
 
 def _state(p, seed):

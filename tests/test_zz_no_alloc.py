@@ -60,3 +60,29 @@ def test_noalloc_rejects_sizes_beyond_the_static_scratch(cuda_device):
     st = lib.fm_diff2d_f64_forward_noalloc(nx, ny, ctypes.c_void_p(0x1000), 0.1, 1, None)
     assert st == 1
     assert b"exceeds" in lib.fm_last_error()
+
+
+def test_noalloc_result_is_final_on_return_for_another_stream(cuda_device):
+    """An odd number of passes leaves the result in the static scratch, and the
+    copy back into dens is part of the call: when the call returns, another
+    stream may read dens, and a second call on another stream may reuse the
+    scratch, with no device-wide synchronization in between."""
+    lib = _lib.lib()
+    coef, steps = 0.1, 41  # 11 passes of 4 steps: odd
+    d0a = inits.diffusion_2d(256, 256, seed=7)
+    d0b = inits.diffusion_2d(128, 256, seed=8)
+    da, db = torch.from_numpy(d0a).cuda(), torch.from_numpy(d0b).cuda()
+    torch.cuda.synchronize()
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    st = lib.fm_diff2d_f64_forward_noalloc(256, 256, ctypes.c_void_p(da.data_ptr()), coef, steps,
+                                           ctypes.c_void_p(sa.cuda_stream))
+    _lib.check(st, "fm_diff2d_f64_forward_noalloc")
+    with torch.cuda.stream(sb):
+        seen = da.clone()  # read on stream B right after the call returned
+        st = lib.fm_diff2d_f64_forward_noalloc(128, 256, ctypes.c_void_p(db.data_ptr()), coef,
+                                               steps, ctypes.c_void_p(sb.cuda_stream))
+        _lib.check(st, "fm_diff2d_f64_forward_noalloc")
+        got_b = db.clone()
+    sb.synchronize()
+    assert np.array_equal(seen.cpu().numpy(), _existing(d0a, coef, steps))
+    assert np.array_equal(got_b.cpu().numpy(), _existing(d0b, coef, steps))
