@@ -280,7 +280,10 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
         "rel_l2_error_vs_fp64": err, "max_rel_error_vs_fp64": errmax,
         "hbm_untiled_roofline_glups": round(hbm / 32.0, 1),
         "hbm_roofline_at_tb_glups": round(hbm / (32.0 / tune["tb"]), 1),
-        "kernel": "gs3d_f32k_tb"}
+        "frac_of_hbm_roofline_at_tb": round(g / (hbm / (32.0 / tune["tb"])), 3),
+        "kernel": ["gs3d_f32k_tb (one row per warp)", "gs3d_f32k_tbr<4 rows, 8 warps>",
+                   "gs3d_f32k_tbr<2 rows, 16 warps>"][tune["kernel"]],
+        "tuned": {"timings_s_per_step": tune["timings"]}}
     del U, V, cU, cV, w, Uw, Vw
     # -- uneven ensemble of 512 2D Gray-Scott instances, 5000 steps, one launch
     sizes, F, k = inits.gs2d_ensemble(512, seed=1)
@@ -349,6 +352,7 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
         errs[name] = float((x.double() - y).abs().max() / y.abs().max().clamp_min(1e-300))
     del t32, t64
     out["gray_scott_3d_generated_from_fmr"] = run_generated_variant(torch, U0, V0)
+    out["gray_scott_3d_float_blocked_from_fmr"] = run_generated_blocked_variant(torch, U0, V0, hbm)
     out["surrogate_gs2d_512"] = run_surrogate_variant(torch)
     out["mhd_3d_256_fp32_bulk_fp64_energy"] = {
         "value": round(N ** 3 * 500 / sec / 1e9, 3), "unit": "GLUP/s", "steps": 500,
@@ -395,6 +399,47 @@ def run_generated_variant(torch, U0, V0):
     prog.finalize()
     return {"value": round(N ** 3 * steps / sec / 1e9, 3), "unit": "GLUP/s", "steps": steps,
             "bit_equal_to_hand_kernel": same, "kernel": "fmr_level_0 (generated from .fmr)"}
+
+
+def run_generated_blocked_variant(torch, U0, V0, hbm):
+    """examples/gray-scott-3d-float.fmr (binary32, temporal_blocking_interval 4)
+    compiled by the front end at 256^3: the generated temporally blocked kernel
+    (4 steps per pass) against the same program run one step per launch, both
+    timed over one Formura_Advance of 2000 steps on the resident state, and
+    bit-equality of the two after those steps."""
+    import numpy as np
+
+    from formura_gb300 import backend
+    from formura_gb300.fmr import load_program
+    from formura_gb300.runtime import load_program as load_lib
+
+    res = {}
+    finals = []
+    for tbk, label in ((1, "blocked"), (-1, "per_step")):
+        p = load_program(ROOT / "examples" / "gray-scott-3d-float.fmr", tb_kernel=tbk,
+                         name="fmr_gs3d_float_%s" % label)
+        plan = backend.blocked_kernel(p)
+        prog = load_lib(p)
+        prog.init()
+        prog.state["U"][...] = U0.astype(np.float32)
+        prog.state["V"][...] = V0.astype(np.float32)
+        prog.upload()
+        prog.advance(1)  # warm-up
+        prog.upload()
+        sec = _event_time(torch, lambda: prog.advance(1))
+        prog.download()
+        finals.append((prog.state["U"].copy(), prog.state["V"].copy()))
+        res[label + "_glups"] = round(N ** 3 * p.steps_per_forward / sec / 1e9, 2)
+        if plan is not None:
+            pl = plan[1]
+            res["tile"] = {"interior": pl.TI[1:], "region": pl.RG[1:], "x_chunk": pl.XC,
+                           "tiles": pl.ntiles, "smem_bytes": pl.smem}
+        prog.finalize()
+    same = all(np.array_equal(a, b) for a, b in zip(finals[0], finals[1]))
+    return {"value": res["blocked_glups"], "unit": "GLUP/s", "steps": 2000, "tb": 4,
+            "per_step_glups": res["per_step_glups"], "bit_equal_blocked_vs_per_step": same,
+            "hbm_roofline_at_tb_glups": round(hbm / (16.0 / 4), 1), "tile": res.get("tile"),
+            "kernel": "fmr_level_tb (generated, 4 steps per pass) vs fmr_level_0"}
 
 
 def run_surrogate_variant(torch):

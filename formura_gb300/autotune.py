@@ -116,15 +116,21 @@ def _apply_ensemble(res: dict) -> None:
     lib().fm_tune_set(b"gs2d_ens.tb", int(res["tb"]))
 
 
+GS3D_F32K_CANDIDATES: Tuple[Tuple[int, int], ...] = tuple(
+    (kern, tb) for kern in (0, 1, 2) for tb in (1, 2, 3, 4))  # (gs3d_f32k.kernel, tb)
+
+
 def tune_gs3d_f32k(n: Tuple[int, int, int] = (256, 256, 256), sample_steps: int = 24,
+                   candidates: Iterable[Tuple[int, int]] = GS3D_F32K_CANDIDATES,
                    use_cache: bool = True) -> dict:
-    """Pick the temporal-blocking depth of fm_gs3d_f32k_tb_forward on an
-    n-sized problem; sets the "gs3d_f32k.tb" default."""
+    """Pick the kernel form and the temporal-blocking depth of
+    fm_gs3d_f32k_tb_forward on an n-sized problem; sets the "gs3d_f32k.kernel"
+    and "gs3d_f32k.tb" defaults.  Returns {"kernel", "tb", "timings"}."""
     key = "gs3d_f32k|%s|%s" % (_gpu_name(), "x".join(map(str, n)))
     if use_cache:
         hit = _load_cache().get(key)
-        if hit:
-            lib().fm_tune_set(b"gs3d_f32k.tb", int(hit["tb"]))
+        if hit and "kernel" in hit:
+            _apply_gs3d_f32k(hit)
             return hit
     from . import inits
 
@@ -135,11 +141,24 @@ def tune_gs3d_f32k(n: Tuple[int, int, int] = (256, 256, 256), sample_steps: int 
     w = torch.empty(4 * U.numel(), dtype=torch.float32, device="cuda")
     p = kernels.gs_params(0.04, 0.06, 2e-5, 1e-5, 0.5, 0.01)
     timings = []
-    for tb in (1, 2, 3, 4):
-        t = _time(lambda: kernels.gs3d_f32k_tb_forward(U, V, cU, cV, w, p, sample_steps, tb))
-        timings.append((tb, t / sample_steps))
-    tb, t = min(timings, key=lambda r: r[1])
-    res = {"tb": tb, "seconds_per_step": t, "timings": timings}
+    L = lib()
+    prev = L.fm_tune_get(b"gs3d_f32k.kernel", -1)
+    try:
+        for kern, tb in candidates:
+            L.fm_tune_set(b"gs3d_f32k.kernel", int(kern))
+            t = _time(lambda: kernels.gs3d_f32k_tb_forward(U, V, cU, cV, w, p, sample_steps, tb))
+            timings.append((kern, tb, t / sample_steps))
+    finally:
+        if prev >= 0:
+            L.fm_tune_set(b"gs3d_f32k.kernel", prev)
+    kern, tb, t = min(timings, key=lambda r: r[2])
+    res = {"kernel": kern, "tb": tb, "seconds_per_step": t,
+           "timings": [list(r) for r in timings]}
     _store(key, res)
-    lib().fm_tune_set(b"gs3d_f32k.tb", int(tb))
+    _apply_gs3d_f32k(res)
     return res
+
+
+def _apply_gs3d_f32k(res: dict) -> None:
+    lib().fm_tune_set(b"gs3d_f32k.kernel", int(res["kernel"]))
+    lib().fm_tune_set(b"gs3d_f32k.tb", int(res["tb"]))

@@ -79,6 +79,11 @@ class Program:
     # form "fmr": 2 = two cells per thread adjacent along axis 1, sharing values (needs 3+ axes
     # and an even extent of axis 1; measured slower on gray-scott-3d), 0 or 1 = one cell
     march_pair: int = 0
+    # form "fmr": the temporally blocked kernel (temporal_blocking_interval steps per pass,
+    # emit_cuda.TBEmitter) for single-level programs: 0 = when its plane region (tile plus
+    # halo) holds at most twice the cells it writes, 1 = whenever the program allows it,
+    # -1 = never (one step per launch; temporal_blocking_interval then only rounds M)
+    tb_kernel: int = 0
 
     @property
     def dim(self) -> int:
@@ -141,6 +146,8 @@ class Program:
                 raise ValueError("%s: march_chunk must be >= 0 (0 = automatic)" % self.name)
             if self.march_pair not in (0, 1, 2):
                 raise ValueError("%s: march_pair must be 0, 1 or 2" % self.name)
+            if self.tb_kernel not in (-1, 0, 1):
+                raise ValueError("%s: tb_kernel must be -1, 0 or 1" % self.name)
             self.compiled()
             return
         if self.form not in FORMS:
@@ -282,12 +289,40 @@ def _work_elems(p: Program) -> str:
     return "NCELLS"
 
 
+TB_THREADS = 256
+
+
+def blocked_kernel(p: Program):
+    """The temporally blocked kernel of a form-"fmr" program, as
+    emit_cuda.emit_tb_kernel returns it, when the program takes one (see
+    Program.tb_kernel), else None."""
+    from .fmr.emit_cuda import emit_tb_kernel
+
+    T = int(p.temporal_blocking_interval)
+    if p.form != "fmr" or p.tb_kernel < 0 or T < 2:
+        return None
+    r = emit_tb_kernel(p.compiled(), T)
+    if r is None:
+        return None
+    plan = r[1]
+    cells = tile = 1
+    for a in range(1, plan.dim):
+        cells *= plan.RG[a]
+        tile *= plan.TI[a]
+    if p.tb_kernel == 0 and cells > 2 * tile:  # the halo would double the work per plane
+        return None
+    return r
+
+
 def _fmr_parts(p: Program):
     """Kernels, device buffers and the step loop of a form-"fmr" program."""
     from .fmr.emit_cuda import emit_kernels
 
     mmp = p.compiled()
     kern, levels = emit_kernels(mmp, march_chunk=p.march_chunk, march_pair=p.march_pair)
+    tb = blocked_kernel(p)
+    if tb is not None:
+        kern += "\n" + tb[0]
     states = [n for n, _ in mmp.state]
     sidx = {n: i for i, n in enumerate(states)}
     arrays = sorted(mmp.arrays.values(), key=lambda a: a.node)
@@ -302,8 +337,24 @@ def _fmr_parts(p: Program):
                  " cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);"
                  " long long need = ((long long)NCELLS + 255) / 256;"
                  " g_grid = (int)(need < (long long)sms * 16 ? need : (long long)sms * 16); }")
-    run = ["  cudaStream_t s = (cudaStream_t)g_stream;",
-           "  for (int t = 0; t < steps; ++t) {"]
+    run = ["  cudaStream_t s = (cudaStream_t)g_stream;", "  int t = 0;"]
+    if tb is not None:
+        _, plan, sn_tb, aw_tb = tb
+        alloc.append("  if (cudaFuncSetAttribute(fmr_level_tb, cudaFuncAttributeMaxDynamicSharedMemorySize,"
+                     " %d) != cudaSuccess) return fail(FM_ERR_CUDA, \"blocked kernel shared memory\");"
+                     % plan.smem)
+        alloc.append("  { int dev = 0; cudaGetDevice(&dev); int sms = 0;"
+                     " cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);"
+                     " g_grid_tb = %d < sms ? %d : sms; }" % (plan.ntiles, plan.ntiles))
+        args = ["(const %s*)g_dev[%d]" % (dict(mmp.state)[n], sidx[n]) for n in sn_tb]
+        args += ["(%s*)g_next[%d]" % (a.ctype, sidx[a.store_of]) for a in aw_tb]
+        run += ["  /* %d steps per pass of the blocked kernel, the rest one step per launch */" % plan.T,
+                "  for (; t + %d <= steps; t += %d) {" % (plan.T, plan.T),
+                "    fmr_level_tb<<<g_grid_tb, %d, %d, s>>>(%s);" % (TB_THREADS, plan.smem,
+                                                                   ", ".join(args)),
+                "    for (int i = 0; i < kNState; ++i) { void *x = g_dev[i]; g_dev[i] = g_next[i]; g_next[i] = x; }",
+                "  }"]
+    run += ["  for (; t < steps; ++t) {"]
     for kname, sn, ar, aw in levels:
         args = ["(const %s*)g_dev[%d]" % (dict(mmp.state)[n], sidx[n]) for n in sn]
         args += ["(const %s*)g_arr[%d]" % (mmp.arrays[x].ctype, aidx[x]) if mmp.arrays[x].store_of is None
@@ -327,7 +378,7 @@ def _fmr_parts(p: Program):
     free += ["  fm_free(g_arr[%d]); g_arr[%d] = 0;" % (aidx[a.node], aidx[a.node]) for a in inner]
     decls = ["static void *g_next[%d] = {0};" % max(1, len(states)),
              "static void *g_arr[%d] = {0};" % max(1, len(arrays)),
-             "static int g_grid = 1;"]
+             "static int g_grid = 1;", "static int g_grid_tb = 1;"]
     return kern, decls, alloc, run, free
 
 

@@ -26,8 +26,8 @@
 // when it misses L2) and out (16 B), i.e. ~32/T B per lattice update.
 //
 // Arithmetic: the binary32 fast form of the Gray-Scott step (oracle
-// fo_gs3d_run_f32k_fast) — differences summed per axis, explicit FMAs — so
-// every T gives bit-identical results.
+// fo_gs3d_run_f32k_fast) — per axis the difference of the two face
+// differences, explicit FMAs — so every T gives bit-identical results.
 #include <algorithm>
 
 #include "fm_common.cuh"
@@ -61,6 +61,25 @@ __device__ __forceinline__ void cell_step(float u, float v, float lu, float lv, 
   const float tv = v + yv;
   cvn = (tv - v) - yv;
   vn = tv;
+}
+
+// x planes per tile: the "gs3d_f32k.xchunk" knob, else the chunk that minimises
+// waves x (chunk + 2T pipeline fill) over `resident` CTAs.
+int pick_xchunk(int nx, long long nyz, int resident, int T) {
+  int xc = fm::tune_get("gs3d_f32k.xchunk", 0);
+  if (xc <= 0) {
+    double best = 1e300;
+    for (int cand = 4; cand <= nx; cand += 4) {
+      const long long tiles = nyz * ((nx + cand - 1) / cand);
+      const double cost = (double)((tiles + resident - 1) / resident) * (cand + 2 * T);
+      if (cost < best - 1e-9) {
+        best = cost;
+        xc = cand;
+      }
+    }
+    if (xc <= 0) xc = nx;
+  }
+  return std::min(xc, nx);
 }
 
 template <int T>
@@ -167,10 +186,10 @@ __global__ void __launch_bounds__(kE *kE, 1)
           const float uyp = s_u[(base + row + 1) * kE + lane];
           const float vym = s_v[(base + row - 1) * kE + lane];
           const float vyp = s_v[(base + row + 1) * kE + lane];
-          const float lu = (((wu[s - 1][2] - u) + (wu[s - 1][0] - u)) + ((uyp - u) + (uym - u))) +
-                           ((uzp - u) + (uzm - u));
-          const float lv = (((wv[s - 1][2] - v) + (wv[s - 1][0] - v)) + ((vyp - v) + (vym - v))) +
-                           ((vzp - v) + (vzm - v));
+          const float lu = (((wu[s - 1][2] - u) - (u - wu[s - 1][0])) + ((uyp - u) - (u - uym))) +
+                           ((uzp - u) - (u - uzm));
+          const float lv = (((wv[s - 1][2] - v) - (v - wv[s - 1][0])) + ((vyp - v) - (v - vym))) +
+                           ((vzp - v) - (v - vzm));
           float un, vn, cun, cvn;
           cell_step(u, v, lu, lv, cin_u, cin_v, c, un, vn, cun, cvn);
           if (s < T) {
@@ -203,6 +222,230 @@ __global__ void __launch_bounds__(kE *kE, 1)
   }
 }
 
+// gs3d_f32k_tbr<T, RY, W>: the same pipeline with register blocking along y
+// and each face difference computed once.
+//
+//  * A CTA of W warps owns a tile of 32 (z, one cell per lane) x RY*W (y)
+//    columns; each thread owns RY consecutive rows of one z column, for every
+//    time level.  The inner (RY*W - 2T) x (32 - 2T) columns are written back.
+//  * Per level l the thread keeps, for each of its cells and field, P = the
+//    value at the plane level l+1 advances next, N = the plane after it, and
+//    D = the face difference below P (P - previous plane).  Level l+1 forms
+//    the x term as (N - P) - D and keeps N - P as the next D.
+//  * y neighbours of the inner rows are the thread's own registers; its first
+//    and last rows exchange values with the warps above and below through
+//    shared memory (double-buffered by plane parity, one __syncthreads per
+//    plane), so shared memory carries 2 of the RY rows.  The y term of row j
+//    is f[j+1] - f[j] over the thread's RY+1 face differences.
+//  * z: one shuffle brings the value of z+1, the face difference z+1/2 is
+//    computed once, and a second shuffle brings the face below from lane - 1.
+//  * Every level runs on every row; cells outside a level's valid region
+//    (rows and lanes within s of the tile's edge at level s) hold values that
+//    no valid cell reads.
+// The operations per cell are the fast form's, in its order, so the results
+// equal the 32x32-thread kernel's and the oracle's bit for bit.
+template <int T, int RY, int W>
+__global__ void __launch_bounds__(32 * W, 1)
+    gs3d_f32k_tbr(const float *__restrict__ U, const float *__restrict__ V,
+                  const float *__restrict__ cU, const float *__restrict__ cV,
+                  float *__restrict__ Un, float *__restrict__ Vn, float *__restrict__ cUn,
+                  float *__restrict__ cVn, int nx, int ny, int nz, int xchunk, int nty,
+                  int ntz, int ntiles, Gs32f c) {
+  constexpr int OY = RY * W - 2 * T, OZ = 32 - 2 * T;  // output tile
+  // halo rows hs[level][parity][slot][edge][field][lane]: warp w writes slot w+1
+  // (edge 0: its first row, edge 1: its last row); slots 0 and W+1 stay unwritten
+  constexpr int kSlot = 2 * 2 * 32, kPar = (W + 2) * kSlot, kLev = 2 * kPar;
+  extern __shared__ float hs[];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const size_t sx = (size_t)ny * nz;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tz = t % ntz;
+    const int ty = (t / ntz) % nty;
+    const int tx = t / (ntz * nty);
+    const int x0 = tx * xchunk;
+    const int x1 = min(x0 + xchunk, nx);
+    const int gz = tz * OZ + lane - T;
+    const int zc = wrap_any(gz, nz);
+    const bool zw = lane >= T && lane < T + OZ && gz < nz;
+    int col[RY];
+    bool writer[RY];
+#pragma unroll
+    for (int j = 0; j < RY; ++j) {
+      const int r = w * RY + j;
+      const int gy = ty * OY + r - T;
+      col[j] = wrap_any(gy, ny) * nz + zc;
+      writer[j] = zw && r >= T && r < T + OY && gy < ny;
+    }
+    float P[T][2][RY], N[T][2][RY], D[T][2][RY], C[T][2][RY];
+#pragma unroll
+    for (int l = 0; l < T; ++l)
+#pragma unroll
+      for (int f = 0; f < 2; ++f)
+#pragma unroll
+        for (int j = 0; j < RY; ++j) P[l][f][j] = N[l][f][j] = D[l][f][j] = C[l][f][j] = 0.0f;
+    constexpr int kPF = 2;
+    float pf[kPF][4][RY];
+#pragma unroll
+    for (int k = 0; k < kPF; ++k) {
+      const size_t g = (size_t)wrap_any(x0 - T + k, nx) * sx;
+#pragma unroll
+      for (int j = 0; j < RY; ++j) {
+        pf[k][0][j] = __ldg(U + g + col[j]);
+        pf[k][1][j] = __ldg(V + g + col[j]);
+        pf[k][2][j] = __ldg(cU + g + col[j]);
+        pf[k][3][j] = __ldg(cV + g + col[j]);
+      }
+    }
+    // unrolled by 2: the P/N roles, the prefetch queue and the parity rotate by renaming
+#pragma unroll 2
+    for (int i = x0 - T; i < x1 + T; ++i) {
+      const int par = i & 1;
+      float in[4][RY];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int j = 0; j < RY; ++j) {
+          in[a][j] = pf[0][a][j];
+#pragma unroll
+          for (int k = 0; k + 1 < kPF; ++k) pf[k][a][j] = pf[k + 1][a][j];
+        }
+      if (i + kPF < x1 + T) {
+        int ip = i + kPF;
+        if (nx >= 8)
+          ip = ip < 0 ? ip + nx : (ip >= nx ? ip - nx : ip);
+        else
+          ip = wrap_any(ip, nx);
+        const size_t g = (size_t)ip * sx;
+#pragma unroll
+        for (int j = 0; j < RY; ++j) {
+          pf[kPF - 1][0][j] = __ldg(U + g + col[j]);
+          pf[kPF - 1][1][j] = __ldg(V + g + col[j]);
+          pf[kPF - 1][2][j] = __ldg(cU + g + col[j]);
+          pf[kPF - 1][3][j] = __ldg(cV + g + col[j]);
+        }
+      }
+      // ---- level 0: plane i
+      float carry[2][RY];
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+#pragma unroll
+        for (int j = 0; j < RY; ++j) {
+          P[0][f][j] = N[0][f][j];
+          N[0][f][j] = in[f][j];
+          carry[f][j] = C[0][f][j];  // level 0's compensation at plane i-1
+          C[0][f][j] = in[2 + f][j];
+        }
+        float *h = hs + par * kPar + (w + 1) * kSlot + f * 32 + lane;
+        h[0] = N[0][f][0];
+        h[2 * 32] = N[0][f][RY - 1];
+      }
+      // ---- levels 1..T: level s advances plane i-s from level s-1
+#pragma unroll
+      for (int s = 1; s <= T; ++s) {
+        const int l = s - 1;
+        float lap[2][RY];
+#pragma unroll
+        for (int f = 0; f < 2; ++f) {
+          const float *hr = hs + l * kLev + (par ^ 1) * kPar + f * 32 + lane;
+          const float top = hr[w * kSlot + 2 * 32];   // last row of warp w-1
+          const float bot = hr[(w + 2) * kSlot];      // first row of warp w+1
+          float fy_prev = P[l][f][0] - top;           // face below row 0
+#pragma unroll
+          for (int j = 0; j < RY; ++j) {
+            const float p = P[l][f][j];
+            const float dn = N[l][f][j] - p;          // x face above
+            const float lx = dn - D[l][f][j];
+            D[l][f][j] = dn;
+            const float fy = (j + 1 < RY ? P[l][f][j + 1] : bot) - p;
+            const float ly = fy - fy_prev;
+            fy_prev = fy;
+            const float zp = __shfl_down_sync(0xffffffffu, p, 1);
+            const float fz = zp - p;                  // z face above
+            const float fzm = __shfl_up_sync(0xffffffffu, fz, 1);
+            const float lz = fz - fzm;
+            lap[f][j] = (lx + ly) + lz;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < RY; ++j) {
+          float un, vn, cun, cvn;
+          cell_step(P[l][0][j], P[l][1][j], lap[0][j], lap[1][j], carry[0][j], carry[1][j], c,
+                    un, vn, cun, cvn);
+          if (s < T) {
+            carry[0][j] = C[s][0][j];
+            carry[1][j] = C[s][1][j];
+            C[s][0][j] = cun;
+            C[s][1][j] = cvn;
+            P[s][0][j] = N[s][0][j];
+            N[s][0][j] = un;
+            P[s][1][j] = N[s][1][j];
+            N[s][1][j] = vn;
+          } else {
+            const int p = i - T;
+            if (writer[j] && p >= x0) {
+              const size_t g = (size_t)p * sx + col[j];
+              Un[g] = un;
+              Vn[g] = vn;
+              cUn[g] = cun;
+              cVn[g] = cvn;
+            }
+          }
+        }
+        if (s < T) {
+#pragma unroll
+          for (int f = 0; f < 2; ++f) {
+            float *h = hs + s * kLev + par * kPar + (w + 1) * kSlot + f * 32 + lane;
+            h[0] = N[s][f][0];
+            h[2 * 32] = N[s][f][RY - 1];
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <int T, int RY, int W>
+int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const float *cu,
+               const float *cv, float *un, float *vn, float *cun, float *cvn, const Gs32f &c,
+               cudaStream_t s) {
+  constexpr int OY = RY * W - 2 * T, OZ = 32 - 2 * T;
+  const size_t smem = (size_t)T * 2 * (W + 2) * 2 * 2 * 32 * sizeof(float);
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  FM_TRY_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && !attr_set[dev]) {
+    FM_TRY_CUDA(cudaFuncSetAttribute(gs3d_f32k_tbr<T, RY, W>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set[dev] = true;
+  }
+  int sms = 0;
+  int st = fm::device_sm_count(&sms);
+  if (st) return st;
+  int per_sm = 0;
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs3d_f32k_tbr<T, RY, W>,
+                                                             32 * W, smem));
+  if (per_sm < 1) {
+    fm::set_error("fm_gs3d_f32k_tb_forward: register-blocked kernel does not fit on an SM");
+    return FM_ERR_UNSUPPORTED;
+  }
+  const int resident = sms * per_sm;
+  const int nty = (ny + OY - 1) / OY, ntz = (nz + OZ - 1) / OZ;
+  const long long nyz = (long long)nty * ntz;
+  const int xc = pick_xchunk(nx, nyz, resident, T);
+  const long long ntiles = nyz * ((nx + xc - 1) / xc);
+  if (ntiles > (1ll << 30)) {
+    fm::set_error("fm_gs3d_f32k_tb_forward: grid too large");
+    return FM_ERR_UNSUPPORTED;
+  }
+  const int grid = (int)std::min<long long>(ntiles, resident);
+  gs3d_f32k_tbr<T, RY, W><<<grid, 32 * W, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz,
+                                                      xc, nty, ntz, (int)ntiles, c);
+  FM_TRY_CUDA(cudaGetLastError());
+  return FM_OK;
+}
+
 template <int T>
 int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const float *cu,
               const float *cv, float *un, float *vn, float *cun, float *cvn, const Gs32f &c,
@@ -226,21 +469,7 @@ int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const floa
   const int resident = sms * std::max(per_sm, 1);
   const int nty = (ny + O - 1) / O, ntz = (nz + O - 1) / O;
   const long long nyz = (long long)nty * ntz;
-  int xc = fm::tune_get("gs3d_f32k.xchunk", 0);
-  if (xc <= 0) {
-    // minimise waves x (chunk + 2T pipeline fill)
-    double best = 1e300;
-    for (int cand = 4; cand <= nx; cand += 4) {
-      const long long tiles = nyz * ((nx + cand - 1) / cand);
-      const double cost = (double)((tiles + resident - 1) / resident) * (cand + 2 * T);
-      if (cost < best - 1e-9) {
-        best = cost;
-        xc = cand;
-      }
-    }
-    if (xc <= 0) xc = nx;
-  }
-  xc = std::min(xc, nx);
+  const int xc = pick_xchunk(nx, nyz, resident, T);
   const long long ntiles = nyz * ((nx + xc - 1) / xc);
   if (ntiles > (1ll << 30)) {
     fm::set_error("fm_gs3d_f32k_tb_forward: grid too large");
@@ -277,10 +506,27 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   const size_t n = (size_t)nx * ny * nz;
   float *cur[4] = {U, V, cU, cV};
   float *nxt[4] = {work, work + n, work + 2 * n, work + 3 * n};
+  // 1: register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread,
+  // 16 warps; 0: one row per warp (32x32 threads)
+  const int kern = fm::tune_get("gs3d_f32k.kernel", 0);
   int done = 0;
   while (done < steps) {
     const int t = std::min(tb, steps - done);
     int st;
+    if (kern == 1 || kern == 2) {
+      float *a[8] = {cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3]};
+#define FM_TBR(TT, RR, WW) \
+  launch_tbr<TT, RR, WW>(nx, ny, nz, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], c, s)
+      if (kern == 1)
+        st = t == 1 ? FM_TBR(1, 4, 8) : t == 2 ? FM_TBR(2, 4, 8) : t == 3 ? FM_TBR(3, 4, 8) : FM_TBR(4, 4, 8);
+      else
+        st = t == 1 ? FM_TBR(1, 2, 16) : t == 2 ? FM_TBR(2, 2, 16) : t == 3 ? FM_TBR(3, 2, 16) : FM_TBR(4, 2, 16);
+#undef FM_TBR
+      if (st) return st;
+      for (int k = 0; k < 4; ++k) std::swap(cur[k], nxt[k]);
+      done += t;
+      continue;
+    }
     switch (t) {
       case 1: st = launch_tb<1>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
       case 2: st = launch_tb<2>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;

@@ -30,7 +30,8 @@ def load_program(fmr_path, yaml_path=None, name: Optional[str] = None, **overrid
     """A backend Program (form "fmr") from a .fmr file and its numerical
     config (``<name>.yaml`` beside it unless given); keyword arguments
     override config keys (intra_node_shape, mpi_grid_shape, monitor_interval,
-    temporal_blocking_interval, and this engine's march_chunk and march_pair)."""
+    temporal_blocking_interval, and this engine's march_chunk, march_pair and
+    tb_kernel)."""
     from ..backend import Program
 
     fmr_path = Path(fmr_path)
@@ -46,4 +47,5 @@ def load_program(fmr_path, yaml_path=None, name: Optional[str] = None, **overrid
                    temporal_blocking_interval=int(cfg.get("temporal_blocking_interval", 1)),
                    mpi_grid_shape=cfg.get("mpi_grid_shape"), fmr_source=src,
                    march_chunk=int(cfg.get("march_chunk", 0)),
-                   march_pair=int(cfg.get("march_pair", 0)))
+                   march_pair=int(cfg.get("march_pair", 0)),
+                   tb_kernel=int(cfg.get("tb_kernel", 0)))

@@ -105,14 +105,17 @@ class LevelEmitter:
         return e
 
     def _emit_ops(self, which, alias: Dict[int, str], w, ind: str, pfx: str = "a",
-                  lane: str = "", ext_prep: Optional[Dict[int, str]] = None) -> Dict[int, str]:
+                  lane: str = "", ext_prep: Optional[Dict[int, str]] = None,
+                  load_state=None) -> Dict[int, str]:
         """C statements for the micro ops in `which` (topological order), one
         `const` temporary <pfx><i> each; an op in `alias` is bound to that C
         expression (a value carried from the previous cell, or the other cell
         of the pair) instead.  `lane` selects the axis-1 coordinate variables
         of the cell; `ext_prep` names run-time reciprocals prepared already
-        (divisor op -> DivVarS variable).  Returns the reciprocals this call
-        can share: divisor op -> variable name."""
+        (divisor op -> DivVarS variable); `load_state(name, cursor)`, when
+        given, is the C expression of a state read (else the global array at
+        the wrapped cursor).  Returns the reciprocals this call can share:
+        divisor op -> variable name."""
         L = self.level
         n = lambda i: "%s%d" % (pfx, i)  # noqa: E731
         const_vals: Dict[int, object] = {}
@@ -132,8 +135,9 @@ class LevelEmitter:
                 const_vals[i] = m.args[0]
                 w(ind + "const %s %s = %s;" % (t, name, MM.c_literal(m.args[0], t)))
             elif k == "loadS":
-                w(ind + "const %s %s = s_%s[%s];" % (t, name, m.args[1],
-                                                    self.idx_expr(m.args[0], lane)))
+                src = (load_state(m.args[1], m.args[0]) if load_state is not None else
+                       "s_%s[%s]" % (m.args[1], self.idx_expr(m.args[0], lane)))
+                w(ind + "const %s %s = %s;" % (t, name, src))
             elif k == "loadM":
                 arr = self.mmp.arrays[m.args[1]]
                 w(ind + "const %s %s = r_%s[%s];" % (t, name, arr.name,
@@ -493,6 +497,245 @@ class LevelEmitter:
         src += body
         src += ["  }", "}", ""]
         return "\n".join(src), state_names, arr_ids, L.arrays
+
+
+# ---------------------------------------------------------------------------
+# Temporal blocking of single-level programs
+
+TB_SMEM_BUDGET = 200 * 1024  # bytes of shared memory a blocked kernel may take
+TB_THREADS = 256
+
+
+def tb_eligible(mmp: MM.MMProgram) -> bool:
+    """A program can be temporally blocked here when its step is one level
+    that reads only the state (no other manifest array) and writes exactly
+    the next value of every state variable, on 2 or 3 axes: then T steps are
+    the level applied T times."""
+    if mmp.dim not in (2, 3) or len(mmp.levels) != 1:
+        return False
+    L = mmp.levels[0]
+    if L.reads_arrays:
+        return False
+    stores = [a.store_of for a in L.arrays]
+    return None not in stores and sorted(stores) == sorted(n for n, _ in mmp.state)
+
+
+class TBPlan:
+    """Geometry of the blocked kernel: stencil reach R[a] per axis (largest
+    |cursor| of a state read), halo H[a] = T * R[a] on the plane axes, the
+    plane tile (interior TI[a], region RG[a] = TI[a] + 2 H[a]) sized to the
+    shared-memory budget, the ring of NS = 2 R[0] + 2 planes per time level,
+    and the chunk XC of planes along axis 0 per tile."""
+
+    def __init__(self, mmp: MM.MMProgram, T: int, budget: int = TB_SMEM_BUDGET,
+                 sms: int = 152):
+        L = mmp.levels[0]
+        d = mmp.dim
+        self.T, self.dim, self.shape = T, d, list(mmp.shape)
+        R = [0] * d
+        for _, cur in L.reads_state:
+            for a, c in enumerate(cur):
+                R[a] = max(R[a], abs(c))
+        self.R = R
+        self.NS = 2 * R[0] + 2
+        self.read = sorted({n for n, _ in L.reads_state})
+        stype = dict(mmp.state)
+        size = {"double": 8, "float": 4, "int": 4, "bool": 1}
+        per_pos = sum(size[stype[n]] for n in self.read) * self.NS * T
+        H = [0] + [T * R[a] for a in range(1, d)]
+        TI = [0] * d
+        if d == 3:
+            TI[2] = min(self.shape[2], max(8, 64 - 2 * H[2]))
+            rg2 = TI[2] + 2 * H[2]
+            rg1 = budget // max(1, per_pos * rg2)
+            TI[1] = min(self.shape[1], rg1 - 2 * H[1])
+        else:
+            TI[1] = min(self.shape[1], budget // max(1, per_pos) - 2 * H[1], 4096)
+        self.H, self.TI = H, TI
+        self.ok = all(TI[a] >= 1 for a in range(1, d))
+        self.RG = [0] + [TI[a] + 2 * H[a] for a in range(1, d)]
+        self.NT = [0] + [(self.shape[a] + TI[a] - 1) // TI[a] if self.ok else 1
+                         for a in range(1, d)]
+        self.plane = 1
+        for a in range(1, d):
+            self.plane *= self.RG[a]
+        self.smem = per_pos * self.plane
+        nyz = 1
+        for a in range(1, d):
+            nyz *= self.NT[a]
+        # planes per tile: the chunk that minimises waves x (chunk + pipeline fill) over
+        # one resident CTA per SM (the rings take most of an SM's shared memory)
+        fill = T * (2 * R[0] + 1)
+        n0 = self.shape[0]
+        best, self.XC = None, n0
+        for cand in range(1, n0 + 1):
+            tiles = nyz * ((n0 + cand - 1) // cand)
+            cost = ((tiles + sms - 1) // sms) * (cand + fill)
+            if best is None or cost < best:
+                best, self.XC = cost, cand
+        self.nchunk = (n0 + self.XC - 1) // self.XC
+        self.ntiles = self.nchunk * nyz
+        self.sizes = {n: size[stype[n]] for n in self.read}
+
+
+class TBEmitter(LevelEmitter):
+    """Kernel ``fmr_level_tb``: T steps of the program's one level per pass
+    over the state.  A CTA owns a plane tile (axes 1..d-1, region = interior
+    plus the halo of T steps) and marches along axis 0 over a chunk of
+    planes.  Each time level s = 0..T-1 keeps a ring of NS planes of the
+    region in shared memory; at iteration i level 0 loads plane i (periodic
+    wrap) and level s = 1..T evaluates plane i - s (R0 + 1) of the cells that
+    are still valid at level s (s R[a] away from the region's edge) from
+    level s-1's planes within R0 of it, all of which were written in earlier
+    iterations, so one __syncthreads per iteration orders every level.  Level
+    T writes the interior of the chunk's planes.  Each cell evaluates the
+    level's operations in the per-step kernel's order on the same values, so
+    the results equal T steps of that kernel bit for bit (the reference's
+    temporal blocking unrolls the step graph the same way,
+    src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134)."""
+
+    def __init__(self, mmp, plan: TBPlan, soft_div=True, soft_mul=True, soft_cmp=True):
+        super().__init__(mmp, mmp.levels[0], 0, soft_div, soft_mul, soft_cmp)
+        self.plan = plan
+
+    def emit(self) -> Tuple[str, List[str], List[MM.Array]]:
+        L, P = self.level, self.plan
+        d, T, R, NS, RG, TI, H = P.dim, P.T, P.R, P.NS, P.RG, P.TI, P.H
+        stypes = dict(self.mmp.state)
+        state_names = sorted({n for n, _ in L.reads_state})
+        params = ["const %s *__restrict__ s_%s" % (stypes[n], n) for n in state_names]
+        params += ["%s *__restrict__ w_%s" % (a.ctype, a.name) for a in L.arrays]
+        plane = P.plane
+        out: List[str] = []
+        w = out.append
+        n0 = self.shape[0]
+        w("#ifdef FMR_HOST_BUILD")
+        w("static unsigned char fmr_tb_smem[%d];" % max(16, P.smem))
+        w("#endif")
+        w("__global__ void __launch_bounds__(%d, 1) fmr_level_tb(%s) {" % (TB_THREADS, ", ".join(params)))
+        w("#ifndef FMR_HOST_BUILD")
+        w("  extern __shared__ __align__(16) unsigned char fmr_tb_smem[];")
+        w("#endif")
+        off = 0
+        for n in state_names:
+            w("  %s *const m_%s = (%s *)(fmr_tb_smem + %d);  // [level][slot][plane]" %
+              (stypes[n], n, stypes[n], off))
+            off += P.sizes[n] * NS * T * plane
+        nyz = 1
+        for a in range(1, d):
+            nyz *= P.NT[a]
+        w("  for (int tile = blockIdx.x; tile < %d; tile += gridDim.x) {" % P.ntiles)
+        w("    int rest = tile;")
+        for a in reversed(range(1, d)):
+            w("    const int o%d = (rest %% %d) * %d - %d;  // region origin along axis %d"
+              % (a, P.NT[a], TI[a], H[a], a))
+            w("    rest /= %d;" % P.NT[a])
+        w("    const int x0 = rest * %d;" % P.XC)
+        w("    const int x1 = x0 + %d < %d ? x0 + %d : %d;" % (P.XC, n0, P.XC, n0))
+
+        def wrap(e: str, n: int) -> str:
+            return "(((%s) %% %d + %d) %% %d)" % (e, n, n, n)
+
+        def pos_coords(ind: str, valid_lo: List[int], vext: List[int]):
+            """j<a> (region coordinates) of item q within the valid box."""
+            if d == 3:
+                w(ind + "const int j1 = %d + q / %d, j2 = %d + q %% %d;" %
+                  (valid_lo[1], vext[2], valid_lo[2], vext[2]))
+            else:
+                w(ind + "const int j1 = %d + q;" % valid_lo[1])
+
+        def plane_index(js: List[str]) -> str:
+            if d == 3:
+                return "(%s) * %d + (%s)" % (js[1], RG[2], js[2])
+            return js[1]
+
+        w("    for (int i = x0 - %d; i < x1 + %d; ++i) {" % (T * R[0], T * (R[0] + 1)))
+        w("      const int ib = ((i %% %d) + %d) %% %d;" % (NS, NS, NS))
+        # level 0
+        w("      if (i < x1 + %d) {" % (T * R[0]))
+        w("        const int gx = %s;" % wrap("i", n0))
+        w("        for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % plane)
+        pos_coords("          ", [0] * d, RG)
+        gidx = "(size_t)gx"
+        for a in range(1, d):
+            w("          const int g%d = %s;" % (a, wrap("o%d + j%d" % (a, a), self.shape[a])))
+            gidx = "(%s * %d + g%d)" % (gidx, self.shape[a], a)
+        for n in state_names:
+            w("          m_%s[ib * %d + q] = s_%s[%s];" % (n, plane, n, gidx))
+        w("        }")
+        w("      }")
+        has_index = {m.args[0] for m in L.micro if m.kind == "index"}
+        for s_ in range(1, T + 1):
+            lag = s_ * (R[0] + 1)
+            lo = [0] + [s_ * R[a] for a in range(1, d)]
+            vext = [0] + [RG[a] - 2 * s_ * R[a] for a in range(1, d)]
+            cnt = 1
+            for a in range(1, d):
+                cnt *= vext[a]
+            w("      {  // level %d: plane i - %d" % (s_, lag))
+            w("        const int p = i - %d;" % lag)
+            w("        if (p >= x0 - %d && p < x1 + %d) {" % ((T - s_) * R[0], (T - s_) * R[0]))
+            base_in = (s_ - 1) * NS * plane
+            slots = {}
+            for c0 in range(-R[0], R[0] + 1):
+                v = "sl%s%d" % ("m" if c0 < 0 else "p", abs(c0))
+                slots[c0] = v
+                w("          const int %s = (ib + %d) %% %d;" % (v, (c0 - lag) % NS, NS))
+            if s_ < T:
+                w("          const int so = (ib + %d) %% %d;" % ((-lag) % NS, NS))
+            if 0 in has_index:
+                w("          const int c0 = %s;" % wrap("p", n0))
+            w("          for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % cnt)
+            pos_coords("            ", lo, vext)
+            for a in range(1, d):
+                if a in has_index:
+                    w("            const int c%d = %s;" % (a, wrap("o%d + j%d" % (a, a), self.shape[a])))
+
+            def load(name, cur, _b=base_in, _sl=slots):
+                js = [None] + ["j%d%s" % (a, "" if cur[a] == 0 else "%+d" % cur[a]) for a in range(1, d)]
+                return "m_%s[%d + %s * %d + %s]" % (name, _b, _sl[cur[0]], plane, plane_index(js))
+
+            self._emit_ops(range(len(L.micro)), {}, w, "            ", load_state=load)
+            if s_ < T:
+                for arr in L.arrays:
+                    if arr.store_of in state_names:
+                        w("            m_%s[%d + so * %d + %s] = a%d;" %
+                          (arr.store_of, s_ * NS * plane, plane, plane_index([None, "j1", "j2"]),
+                           arr.root))
+            else:
+                conds = ["p >= x0"]
+                gidx = "(size_t)p"
+                for a in range(1, d):
+                    conds.append("o%d + j%d < %d" % (a, a, self.shape[a]))
+                    gidx = "(%s * %d + (o%d + j%d))" % (gidx, self.shape[a], a, a)
+                w("            if (%s) {" % " && ".join(conds))
+                w("              const size_t gi = %s;" % gidx)
+                for arr in L.arrays:
+                    w("              w_%s[gi] = a%d;" % (arr.name, arr.root))
+                w("            }")
+            w("          }")
+            w("        }")
+            w("      }")
+        w("      __syncthreads();")
+        w("    }")
+        w("  }")
+        w("}")
+        w("")
+        return "\n".join(out), state_names, L.arrays
+
+
+def emit_tb_kernel(mmp: MM.MMProgram, T: int, soft_div: bool = True, soft_mul: bool = True,
+                   soft_cmp: bool = True, budget: int = TB_SMEM_BUDGET):
+    """(source, plan, state names read, arrays written) of the blocked kernel
+    ``fmr_level_tb`` (T steps per pass), or None when the program is not
+    eligible (`tb_eligible`) or its halo leaves no room in shared memory."""
+    if T < 2 or not tb_eligible(mmp):
+        return None
+    plan = TBPlan(mmp, T, budget)
+    if not plan.ok:
+        return None
+    src, sn, aw = TBEmitter(mmp, plan, soft_div, soft_mul, soft_cmp).emit()
+    return src, plan, sn, aw
 
 
 def emit_kernels(mmp: MM.MMProgram, soft_div: bool = True, soft_mul: bool = True,

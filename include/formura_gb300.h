@@ -118,7 +118,8 @@ int fm_gs3d_f32k_forward(int nx, int ny, int nz, float *U, float *V, float *cU,
  * overlapped 32x32 (y,z) tiles along x (Formura's temporal blocking,
  * src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134 and the skewed
  * regions of src/Formura/MPICxx/Cut.hs:240-281, as on-chip pipelines).
- * Arithmetic is the binary32 "fast form" (per-axis sums of differences,
+ * Arithmetic is the binary32 "fast form" (per axis the difference of the
+ * two face differences, (W[+1]-W) - (W-W[-1]),
  * explicit FMAs, constants Du/dx^2, Dv/dx^2, F+k rounded once to float):
  * results are bit-identical for every tb and are scored by their error against
  * the FP64 run.  Same arrays as fm_gs3d_f32k_forward; any nx, ny, nz >= 1.

@@ -384,13 +384,13 @@ static void gs3d_step_f32k_fast(int nx, int ny, int nz, const float *restrict U,
         const int zp = wrap_up(z, nz), zm = wrap_dn(z, nz);
         const size_t i = IDX3(x, y, z);
         const float u = U[i], v = V[i];
-        const float sxu = (U[IDX3(xp, y, z)] - u) + (U[IDX3(xm, y, z)] - u);
-        const float syu = (U[IDX3(x, yp, z)] - u) + (U[IDX3(x, ym, z)] - u);
-        const float szu = (U[IDX3(x, y, zp)] - u) + (U[IDX3(x, y, zm)] - u);
+        const float sxu = (U[IDX3(xp, y, z)] - u) - (u - U[IDX3(xm, y, z)]);
+        const float syu = (U[IDX3(x, yp, z)] - u) - (u - U[IDX3(x, ym, z)]);
+        const float szu = (U[IDX3(x, y, zp)] - u) - (u - U[IDX3(x, y, zm)]);
         const float lu = (sxu + syu) + szu;
-        const float sxv = (V[IDX3(xp, y, z)] - v) + (V[IDX3(xm, y, z)] - v);
-        const float syv = (V[IDX3(x, yp, z)] - v) + (V[IDX3(x, ym, z)] - v);
-        const float szv = (V[IDX3(x, y, zp)] - v) + (V[IDX3(x, y, zm)] - v);
+        const float sxv = (V[IDX3(xp, y, z)] - v) - (v - V[IDX3(xm, y, z)]);
+        const float syv = (V[IDX3(x, yp, z)] - v) - (v - V[IDX3(x, ym, z)]);
+        const float szv = (V[IDX3(x, y, zp)] - v) - (v - V[IDX3(x, y, zm)]);
         const float lv = (sxv + syv) + szv;
         const float uvv = (u * v) * v;
         const float dU = fmaf(cu, lu, fmaf(F, 1.0f - u, -uvv));

@@ -61,7 +61,10 @@ void fo_gs3d_run_f32_kahan(int nx, int ny, int nz, float *U, float *V,
 
 /* The binary32 "fast form" of the same 3D Gray-Scott step that the
  * temporally blocked GPU kernel evaluates (FMAs explicit, no divisions):
- *   s_a = (W[a+1]-W) + (W[a-1]-W);  lap = (s_x + s_y) + s_z
+ *   s_a = (W[a+1]-W) - (W-W[a-1]);  lap = (s_x + s_y) + s_z
+ * (the difference of the two face differences, the generated DAG's order
+ * without its divisions; a face difference is the same IEEE value for both
+ * cells it separates, so a kernel may compute it once) 
  *   uvv = (U*V)*V
  *   dU = fmaf(cu, lapU, fmaf(F, 1-U, -uvv))     cu = (float)(Du/(dx*dx))
  *   dV = fmaf(cv, lapV, fmaf(-Fk, V, uvv))      cv = (float)(Dv/(dx*dx)), Fk = (float)(F+k)

@@ -24,7 +24,7 @@ from typing import Dict
 
 import numpy as np
 
-from formura_gb300.fmr.emit_cuda import emit_kernels
+from formura_gb300.fmr.emit_cuda import emit_kernels, emit_tb_kernel
 
 ROOT = Path(__file__).resolve().parents[1]
 CSRC = ROOT / "formura_gb300" / "csrc"
@@ -39,6 +39,8 @@ PRELUDE = r"""
 #include "fm_softfp.cuh"
 #define __global__
 #define __launch_bounds__(threads, blocks)
+#define __syncthreads()
+#define FMR_HOST_BUILD 1
 namespace {
 struct FmHostDim { unsigned x, y, z; };
 const FmHostDim blockIdx = {0u, 0u, 0u}, threadIdx = {0u, 0u, 0u};
@@ -77,13 +79,23 @@ extern "C" void fmr_host_store_counts(int *arrays, int *lo, int *hi) {
 
 
 def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True,
-                count_stores: bool = False) -> str:
+                count_stores: bool = False, tb: int = 1, tb_budget: int = 0) -> str:
     """Host C++ of the generated kernels plus a step loop; `soft` False emits
     the plain IEEE operations instead of the integer-pipe forms.  With
     `count_stores` every store of a kernel also counts, per array and cell, how
-    often it was written (read back by fmr_host_store_counts)."""
+    often it was written (read back by fmr_host_store_counts).  With tb >= 2
+    the temporally blocked kernel runs tb steps per pass (the rest of the
+    steps one per pass), as the generated host code does; `tb_budget` > 0
+    shrinks its shared-memory budget (smaller tiles, more of them)."""
     kern, levels = emit_kernels(mmp, soft_div=soft, soft_mul=soft, soft_cmp=soft,
                                 march_chunk=march_chunk, march_pair=march_pair)
+    tbk = None
+    if tb >= 2:
+        kw = {"budget": tb_budget} if tb_budget else {}
+        tbk = emit_tb_kernel(mmp, tb, soft_div=soft, soft_mul=soft, soft_cmp=soft, **kw)
+        if tbk is None:
+            raise ValueError("program cannot be temporally blocked")
+        kern += "\n" + tbk[0]
     if count_stores:
         n = int(np.prod(mmp.shape))
         lines = []
@@ -115,7 +127,17 @@ def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = Tru
         if a.store_of is None:
             w("  arr[%d] = malloc(n * sizeof(%s)); if (!arr[%d]) return 1;" % (aidx[a.node], a.ctype,
                                                                                 aidx[a.node]))
-    w("  for (int t = 0; t < steps; ++t) {")
+    w("  int t = 0;")
+    if tbk is not None:
+        _, plan, sn_tb, aw_tb = tbk
+        args = ["(const %s*)cur[%d]" % (stype[s], sidx[s]) for s in sn_tb]
+        args += ["(%s*)nxt[%d]" % (a.ctype, sidx[a.store_of]) for a in aw_tb]
+        w("  for (; t + %d <= steps; t += %d) {" % (plan.T, plan.T))
+        w("    fmr_level_tb(%s);" % ", ".join(args))
+        w("    for (int i = 0; i < %d; ++i) { void *x = cur[i]; cur[i] = nxt[i]; nxt[i] = x; }"
+          % len(states))
+        w("  }")
+    w("  for (; t < steps; ++t) {")
     for kname, sn, ar, aw in levels:
         args = ["(const %s*)cur[%d]" % (stype[s], sidx[s]) for s in sn]
         for x in ar:
@@ -145,9 +167,9 @@ class HostKernels:
     the host."""
 
     def __init__(self, mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True,
-                 count_stores: bool = False):
+                 count_stores: bool = False, tb: int = 1, tb_budget: int = 0):
         self.mmp = mmp
-        self.source = host_source(mmp, march_chunk, march_pair, soft, count_stores)
+        self.source = host_source(mmp, march_chunk, march_pair, soft, count_stores, tb, tb_budget)
         key = hashlib.sha256((self.source + (CSRC / "fm_softfp.cuh").read_text()).encode())
         BUILD.mkdir(parents=True, exist_ok=True)
         so = BUILD / ("k_%s.so" % key.hexdigest()[:16])

@@ -145,3 +145,69 @@ def test_schedule_writes_every_cell_once(fmr, shape, chunk, pair):
     hk.run(_state(p, 3), 1)
     arrays, lo, hi = hk.store_counts()
     assert (arrays, lo, hi) == (len(mmp.arrays), 1, 1)
+
+
+# ---- temporally blocked kernels (emit_cuda.TBEmitter) ----------------------------
+
+TB_CASES = [
+    ("gray-scott-3d-float.fmr", [12, 20, 24]), ("gray-scott-3d-float.fmr", [9, 40, 70]),
+    ("gray-scott-3d.fmr", [16, 16, 16]), ("gray-scott-3d.fmr", [5, 7, 33]),
+    ("diffusion-2d.fmr", [40, 64]), ("diffusion-2d.fmr", [7, 300]),
+    ("fmr-libm.fmr", [13, 17]), ("gray-scott-3d-float.fmr", [1, 4, 3]),
+]
+
+
+@pytest.mark.parametrize("fmr,shape", TB_CASES)
+@pytest.mark.parametrize("tb", [2, 3, 4])
+@pytest.mark.parametrize("budget", [0, 24000])
+def test_blocked_kernel_matches_c_oracle(fmr, shape, tb, budget):
+    """The blocked kernel (tb steps per pass, each time level a ring of planes
+    in shared memory) on the host: bit for bit the C oracle's steps, for
+    every depth, with the default tile and with a small shared-memory budget
+    (small tiles, many of them, halos wider than the tile), on ragged shapes
+    and step counts that are not multiples of tb."""
+    p = load_program(EX / fmr, intra_node_shape=shape)
+    s0 = _state(p, 11)
+    try:
+        hk = HostKernels(p.compiled(), tb=tb, tb_budget=budget)
+    except ValueError:
+        pytest.skip("no tile fits this budget")
+    got = hk.run(s0, 2 * tb + 1)
+    want = fmr_c.FmrOracle(p.fmr_source, p.shape).run(s0, 2 * tb + 1)
+    for name in s0:
+        assert np.array_equal(got[name].view(np.uint8), want[name].view(np.uint8)), name
+
+
+@pytest.mark.parametrize("fmr,shape", TB_CASES)
+def test_blocked_kernel_writes_every_cell_once_per_pass(fmr, shape):
+    p = load_program(EX / fmr, intra_node_shape=shape)
+    mmp = p.compiled()
+    hk = HostKernels(mmp, tb=3, tb_budget=24000, count_stores=True) if _fits(mmp, 3, 24000) \
+        else HostKernels(mmp, tb=3, count_stores=True)
+    hk.run(_state(p, 3), 3)  # one pass
+    assert hk.store_counts() == (len(mmp.arrays), 1, 1)
+
+
+def _fits(mmp, tb, budget):
+    from formura_gb300.fmr.emit_cuda import emit_tb_kernel
+
+    return emit_tb_kernel(mmp, tb, budget=budget) is not None
+
+
+def test_which_programs_are_blocked():
+    """Single-level programs (the step reads only the state and writes every
+    state's next value) are blocked; programs with manifest intermediate
+    arrays keep one launch per step, as does a halo that leaves no tile."""
+    from formura_gb300 import backend
+    from formura_gb300.fmr.emit_cuda import tb_eligible
+
+    assert tb_eligible(load_program(EX / "gray-scott-3d-float.fmr").compiled())
+    assert not tb_eligible(load_program(EX / "fmr-limiter.fmr").compiled())
+    assert not tb_eligible(load_program(EX / "fmr-1d-float.fmr").compiled())
+    p = load_program(EX / "gray-scott-3d-float.fmr")
+    assert p.temporal_blocking_interval == 4 and backend.blocked_kernel(p) is not None
+    assert backend.blocked_kernel(load_program(EX / "gray-scott-3d-float.fmr", tb_kernel=-1)) is None
+    assert backend.blocked_kernel(load_program(EX / "gray-scott-3d.fmr")) is None  # interval 1
+    # FP64 with 8 steps per pass: the halo of 8 leaves no tile in shared memory
+    assert backend.blocked_kernel(load_program(EX / "gray-scott-3d.fmr",
+                                               temporal_blocking_interval=8, tb_kernel=1)) is None

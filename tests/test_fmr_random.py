@@ -111,3 +111,38 @@ def test_random_program_schedule_writes_every_cell_once(seed):
     hk.run(initial_state(seed, shape, float_q), 1)
     assert hk.store_counts() == (len(mmp.arrays), 1, 1)
 
+
+
+def blocked_cases(n=40):
+    """Seeds whose random program the blocked kernel takes (a single level)."""
+    from formura_gb300.fmr.emit_cuda import tb_eligible
+
+    out = []
+    for seed in range(200):
+        src, shape, _, _, float_q = case(seed)
+        if tb_eligible(compile_source(src, shape)):
+            out.append(seed)
+        if len(out) == n:
+            break
+    return out
+
+
+@pytest.mark.parametrize("seed", blocked_cases(12))
+def test_random_program_blocked_kernel_matches_c_oracle(seed):
+    """Random single-level programs (reads at offsets up to 2 on every axis,
+    modulo wraps on axes shorter than the halo) through the temporally
+    blocked kernel, 2 to 4 steps per pass, small and default tiles."""
+    src, shape, _, _, float_q = case(seed)
+    tb = 2 + seed % 3
+    mmp = compile_source(src, shape)
+    s0 = initial_state(seed, shape, float_q)
+    want = fmr_c.FmrOracle(src, shape).run(s0, 2 * tb + 1)
+    for budget in (0, 16000):
+        try:
+            hk = HostKernels(mmp, tb=tb, tb_budget=budget)
+        except ValueError:
+            continue
+        got = hk.run(s0, 2 * tb + 1)
+        for name in s0:
+            assert np.array_equal(got[name].view(np.uint8), want[name].view(np.uint8)), \
+                (name, budget, src)

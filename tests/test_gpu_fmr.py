@@ -55,6 +55,18 @@ def _random_state(prog, rng):
     ("gray-scott-3d.fmr", dict(intra_node_shape=[6, 10, 12], monitor_interval=3, march_chunk=1,
                                march_pair=2)),
     ("fmr-3d-advection.fmr", dict(march_chunk=6, march_pair=2)),
+    # the temporally blocked kernel: temporal_blocking_interval steps per pass, each
+    # time level a ring of planes in shared memory (tb_kernel 1: whenever eligible)
+    ("gray-scott-3d-float.fmr", dict(intra_node_shape=[24, 40, 72], monitor_interval=8,
+                                     tb_kernel=1)),
+    ("gray-scott-3d-float.fmr", dict(intra_node_shape=[9, 33, 20], monitor_interval=5,
+                                     temporal_blocking_interval=3, tb_kernel=1)),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[16, 24, 40], monitor_interval=4,
+                               temporal_blocking_interval=2, tb_kernel=1)),
+    ("diffusion-2d.fmr", dict(intra_node_shape=[64, 48], monitor_interval=8,
+                              temporal_blocking_interval=4, tb_kernel=1)),
+    ("diffusion-2d.fmr", dict(intra_node_shape=[5, 700], monitor_interval=6,
+                              temporal_blocking_interval=3, tb_kernel=1)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)
@@ -108,3 +120,25 @@ def test_generated_program_with_device_libm_within_tolerance(cuda_device, tmp_pa
     prog.forward()
     want = fmr_c.FmrOracle(p.fmr_source, p.shape).run({"a": a0}, 2 * p.steps_per_forward)["a"]
     np.testing.assert_allclose(prog.state["a"], want, rtol=1e-12, atol=1e-14)
+
+
+def test_blocked_float_gs3d_equals_per_step_kernels(cuda_device, tmp_path):
+    """examples/gray-scott-3d-float.fmr as configured (4 steps per pass of the
+    blocked kernel) at 64^3 equals the same program run one step per launch,
+    bit for bit, and the blocked kernel is the one the library runs."""
+    from formura_gb300 import backend
+
+    outs = []
+    for tbk in (1, -1):
+        p = load_program(EX / "gray-scott-3d-float.fmr", intra_node_shape=[64, 64, 64],
+                         monitor_interval=40, tb_kernel=tbk, name="gsf_tb%d" % (tbk + 1))
+        assert (backend.blocked_kernel(p) is not None) == (tbk == 1)
+        prog = load_lib(p, outdir=tmp_path)
+        prog.init()
+        U0, V0 = inits.gray_scott_3d(64, 64, 64, seed=2, ncubes=4, side=8)
+        prog.state["U"][...] = U0.astype(np.float32)
+        prog.state["V"][...] = V0.astype(np.float32)
+        prog.forward()
+        outs.append((prog.state["U"].copy(), prog.state["V"].copy()))
+        prog.finalize()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])

@@ -164,30 +164,40 @@ def test_gs3d_f32k_dag_bit_exact(cuda_device, shape, steps):
         assert np.array_equal(g, w)
 
 
+@pytest.mark.parametrize("kernel", [0, 1, 2])
 @pytest.mark.parametrize("tb", [1, 2, 3, 4])
 @pytest.mark.parametrize("shape,steps", [((32, 32, 32), 13), ((20, 24, 64), 8), ((7, 45, 33), 5),
-                                         ((64, 64, 64), 12)])
-def test_gs3d_f32k_tb_bit_exact(cuda_device, shape, steps, tb):
-    """Every blocking depth gives the fast form's step-by-step result bit for bit,
-    including ragged tiles (sizes not multiples of the output tile) and a
-    nonzero incoming compensation."""
-    U0, V0 = inits.gray_scott_3d(*shape, seed=4, ncubes=3, side=4)
+                                         ((64, 64, 64), 12), ((9, 70, 100), 7), ((5, 3, 2), 6)])
+def test_gs3d_f32k_tb_bit_exact(cuda_device, shape, steps, tb, kernel):
+    """Every blocking depth and every kernel form (0: one row per warp; 1, 2:
+    4 or 2 rows per thread with shared face differences) gives the fast form's
+    step-by-step result bit for bit, including ragged tiles (sizes not
+    multiples of the output tile), axes shorter than a tile and a nonzero
+    incoming compensation."""
+    lib = _lib.lib()
+    U0, V0 = inits.gray_scott_3d(*shape, seed=4, ncubes=3, side=min(4, *shape))
     rng = np.random.default_rng(1)
     cU0 = (rng.standard_normal(shape) * 1e-9).astype(np.float32)
     cV0 = (rng.standard_normal(shape) * 1e-9).astype(np.float32)
-    got = run_f32k(U0, V0, steps, tb, cuda_device, cU0, cV0)
+    try:
+        lib.fm_tune_set(b"gs3d_f32k.kernel", kernel)
+        got = run_f32k(U0, V0, steps, tb, cuda_device, cU0, cV0)
+    finally:
+        lib.fm_tune_clear()
     want = oracle.gs3d_f32k_fast(U0.astype(np.float32), V0.astype(np.float32), cU0, cV0, steps,
                                  **GS)
     for g, w in zip(got, want):
         assert np.array_equal(g, w)
 
 
-def test_gs3d_f32k_tb_xchunk_variants(cuda_device):
+@pytest.mark.parametrize("kernel", [0, 1, 2])
+def test_gs3d_f32k_tb_xchunk_variants(cuda_device, kernel):
     lib = _lib.lib()
     U0, V0 = inits.gray_scott_3d(40, 32, 32, seed=9, ncubes=2, side=8)
     Z = np.zeros(U0.shape, np.float32)
     want = oracle.gs3d_f32k_fast(U0.astype(np.float32), V0.astype(np.float32), Z, Z, 8, **GS)
     try:
+        lib.fm_tune_set(b"gs3d_f32k.kernel", kernel)
         for xc in (1, 3, 8, 40, 100):
             lib.fm_tune_set(b"gs3d_f32k.xchunk", xc)
             got = run_f32k(U0, V0, 8, 4, cuda_device)
