@@ -63,11 +63,51 @@ __device__ __forceinline__ void cell_step(float u, float v, float lu, float lv, 
   vn = tv;
 }
 
-// x planes per tile: the "gs3d_f32k.xchunk" knob, else the chunk that minimises
-// waves x (chunk + 2T pipeline fill) over `resident` CTAs.
+// The x-march work of a CTA, as pieces (column c of the (y,z) tile grid, planes
+// [x0, x1)).  xchunk > 0: tiles of xchunk planes dealt round-robin to the CTAs.
+// xchunk <= 0: the nyz * nx column-planes split into gridDim.x contiguous runs
+// of (nearly) equal length, each run cut where it crosses into the next column,
+// so a CTA refills its pipeline once or twice per launch instead of once per
+// chunk.
+// (The host uses runs only when nyz * nx < 2^31.)
+struct Pieces {
+  int q, qend;  // runs: next column-plane, end; chunks: next tile, -1
+  __device__ Pieces(int nyz, int nx, int xchunk) {
+    if (xchunk > 0) {
+      q = blockIdx.x;
+      qend = -1;
+    } else {
+      const long long total = (long long)nyz * nx;
+      q = (int)(total * blockIdx.x / gridDim.x);
+      qend = (int)(total * (blockIdx.x + 1) / gridDim.x);
+    }
+  }
+  __device__ bool next(int nyz, int nx, int xchunk, int ntiles, int &c, int &x0, int &x1) {
+    if (qend < 0) {
+      if (q >= ntiles) return false;
+      c = q % nyz;
+      x0 = (q / nyz) * xchunk;
+      x1 = min(x0 + xchunk, nx);
+      q += gridDim.x;
+      return true;
+    }
+    if (q >= qend) return false;
+    c = q / nx;
+    x0 = q - c * nx;
+    x1 = min(nx, x0 + (qend - q));
+    q += x1 - x0;
+    return true;
+  }
+};
+
+// x planes per tile: the "gs3d_f32k.xchunk" knob (> 0); 0 (default): balanced
+// contiguous runs (Pieces); -1: the chunk that minimises waves x (chunk + 2T
+// pipeline fill) over `resident` CTAs.
 int pick_xchunk(int nx, long long nyz, int resident, int T) {
   int xc = fm::tune_get("gs3d_f32k.xchunk", 0);
-  if (xc <= 0) {
+  if (xc == 0 && nyz * nx < (1ll << 31)) return 0;
+  if (xc < 0) {
+    xc = 0;
     double best = 1e300;
     for (int cand = 4; cand <= nx; cand += 4) {
       const long long tiles = nyz * ((nx + cand - 1) / cand);
@@ -97,12 +137,11 @@ __global__ void __launch_bounds__(kE *kE, 1)
   const int lane = threadIdx.x & 31;
   const int row = threadIdx.x >> 5;
   const size_t sx = (size_t)ny * nz;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int tz = t % ntz;
-    const int ty = (t / ntz) % nty;
-    const int tx = t / (ntz * nty);
-    const int x0 = tx * xchunk;
-    const int x1 = min(x0 + xchunk, nx);
+  Pieces pcs(nty * ntz, nx, xchunk);
+  int pc, x0, x1;
+  while (pcs.next(nty * ntz, nx, xchunk, ntiles, pc, x0, x1)) {
+    const int tz = pc % ntz;
+    const int ty = pc / ntz;
     const int gy_out = ty * O + row - T;  // global y of this thread's column
     const int gz_out = tz * O + lane - T;
     const size_t col = (size_t)wrap_any(gy_out, ny) * nz + wrap_any(gz_out, nz);
@@ -244,7 +283,7 @@ __global__ void __launch_bounds__(kE *kE, 1)
 //    no valid cell reads.
 // The operations per cell are the fast form's, in its order, so the results
 // equal the 32x32-thread kernel's and the oracle's bit for bit.
-template <int T, int RY, int W>
+template <int T, int RY, int W, int PF>
 __global__ void __launch_bounds__(32 * W, 1)
     gs3d_f32k_tbr(const float *__restrict__ U, const float *__restrict__ V,
                   const float *__restrict__ cU, const float *__restrict__ cV,
@@ -259,12 +298,11 @@ __global__ void __launch_bounds__(32 * W, 1)
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   const size_t sx = (size_t)ny * nz;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int tz = t % ntz;
-    const int ty = (t / ntz) % nty;
-    const int tx = t / (ntz * nty);
-    const int x0 = tx * xchunk;
-    const int x1 = min(x0 + xchunk, nx);
+  Pieces pcs(nty * ntz, nx, xchunk);
+  int pc, x0, x1;
+  while (pcs.next(nty * ntz, nx, xchunk, ntiles, pc, x0, x1)) {
+    const int tz = pc % ntz;
+    const int ty = pc / ntz;
     const int gz = tz * OZ + lane - T;
     const int zc = wrap_any(gz, nz);
     const bool zw = lane >= T && lane < T + OZ && gz < nz;
@@ -284,7 +322,7 @@ __global__ void __launch_bounds__(32 * W, 1)
       for (int f = 0; f < 2; ++f)
 #pragma unroll
         for (int j = 0; j < RY; ++j) P[l][f][j] = N[l][f][j] = D[l][f][j] = C[l][f][j] = 0.0f;
-    constexpr int kPF = 2;
+    constexpr int kPF = PF;  // planes prefetched ahead
     float pf[kPF][4][RY];
 #pragma unroll
     for (int k = 0; k < kPF; ++k) {
@@ -406,7 +444,7 @@ __global__ void __launch_bounds__(32 * W, 1)
   }
 }
 
-template <int T, int RY, int W>
+template <int T, int RY, int W, int PF>
 int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const float *cu,
                const float *cv, float *un, float *vn, float *cun, float *cvn, const Gs32f &c,
                cudaStream_t s) {
@@ -416,7 +454,7 @@ int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const flo
   int dev = 0;
   FM_TRY_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !attr_set[dev]) {
-    FM_TRY_CUDA(cudaFuncSetAttribute(gs3d_f32k_tbr<T, RY, W>,
+    FM_TRY_CUDA(cudaFuncSetAttribute(gs3d_f32k_tbr<T, RY, W, PF>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set[dev] = true;
   }
@@ -424,7 +462,7 @@ int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const flo
   int st = fm::device_sm_count(&sms);
   if (st) return st;
   int per_sm = 0;
-  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs3d_f32k_tbr<T, RY, W>,
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs3d_f32k_tbr<T, RY, W, PF>,
                                                              32 * W, smem));
   if (per_sm < 1) {
     fm::set_error("fm_gs3d_f32k_tb_forward: register-blocked kernel does not fit on an SM");
@@ -434,13 +472,13 @@ int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const flo
   const int nty = (ny + OY - 1) / OY, ntz = (nz + OZ - 1) / OZ;
   const long long nyz = (long long)nty * ntz;
   const int xc = pick_xchunk(nx, nyz, resident, T);
-  const long long ntiles = nyz * ((nx + xc - 1) / xc);
+  const long long ntiles = xc > 0 ? nyz * ((nx + xc - 1) / xc) : nyz * nx;
   if (ntiles > (1ll << 30)) {
     fm::set_error("fm_gs3d_f32k_tb_forward: grid too large");
     return FM_ERR_UNSUPPORTED;
   }
   const int grid = (int)std::min<long long>(ntiles, resident);
-  gs3d_f32k_tbr<T, RY, W><<<grid, 32 * W, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz,
+  gs3d_f32k_tbr<T, RY, W, PF><<<grid, 32 * W, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz,
                                                       xc, nty, ntz, (int)ntiles, c);
   FM_TRY_CUDA(cudaGetLastError());
   return FM_OK;
@@ -470,7 +508,7 @@ int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const floa
   const int nty = (ny + O - 1) / O, ntz = (nz + O - 1) / O;
   const long long nyz = (long long)nty * ntz;
   const int xc = pick_xchunk(nx, nyz, resident, T);
-  const long long ntiles = nyz * ((nx + xc - 1) / xc);
+  const long long ntiles = xc > 0 ? nyz * ((nx + xc - 1) / xc) : nyz * nx;
   if (ntiles > (1ll << 30)) {
     fm::set_error("fm_gs3d_f32k_tb_forward: grid too large");
     return FM_ERR_UNSUPPORTED;
@@ -507,20 +545,29 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   float *cur[4] = {U, V, cU, cV};
   float *nxt[4] = {work, work + n, work + 2 * n, work + 3 * n};
   // 1: register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread,
-  // 16 warps; 0: one row per warp (32x32 threads)
+  // 16 warps; 3, 4: the same with 3 planes prefetched instead of 2; 0: one row per
+  // warp (32x32 threads)
   const int kern = fm::tune_get("gs3d_f32k.kernel", 0);
   int done = 0;
   while (done < steps) {
     const int t = std::min(tb, steps - done);
     int st;
-    if (kern == 1 || kern == 2) {
+    if (kern >= 1 && kern <= 4) {
       float *a[8] = {cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3]};
-#define FM_TBR(TT, RR, WW) \
-  launch_tbr<TT, RR, WW>(nx, ny, nz, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], c, s)
+#define FM_TBR(TT, RR, WW, PP) \
+  launch_tbr<TT, RR, WW, PP>(nx, ny, nz, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], c, s)
+#define FM_TBR_T(RR, WW, PP)                                                         \
+  (t == 1 ? FM_TBR(1, RR, WW, PP) : t == 2 ? FM_TBR(2, RR, WW, PP)                  \
+          : t == 3 ? FM_TBR(3, RR, WW, PP) : FM_TBR(4, RR, WW, PP))
       if (kern == 1)
-        st = t == 1 ? FM_TBR(1, 4, 8) : t == 2 ? FM_TBR(2, 4, 8) : t == 3 ? FM_TBR(3, 4, 8) : FM_TBR(4, 4, 8);
+        st = FM_TBR_T(4, 8, 2);
+      else if (kern == 2)
+        st = FM_TBR_T(2, 16, 2);
+      else if (kern == 3)
+        st = FM_TBR_T(4, 8, 3);
       else
-        st = t == 1 ? FM_TBR(1, 2, 16) : t == 2 ? FM_TBR(2, 2, 16) : t == 3 ? FM_TBR(3, 2, 16) : FM_TBR(4, 2, 16);
+        st = FM_TBR_T(2, 16, 3);
+#undef FM_TBR_T
 #undef FM_TBR
       if (st) return st;
       for (int k = 0; k < 4; ++k) std::swap(cur[k], nxt[k]);
