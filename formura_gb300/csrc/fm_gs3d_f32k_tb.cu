@@ -100,13 +100,16 @@ struct Pieces {
   }
 };
 
-// x planes per tile: the "gs3d_f32k.xchunk" knob (> 0); 0 (default): balanced
-// contiguous runs (Pieces); -1: the chunk that minimises waves x (chunk + 2T
-// pipeline fill) over `resident` CTAs.
+// x planes per tile: the "gs3d_f32k.xchunk" knob (> 0); 0 (default): the chunk
+// that minimises waves x (chunk + 2T pipeline fill) over `resident` CTAs; -1:
+// balanced contiguous runs (Pieces).  Runs refill the pipeline less often but
+// measured slower (256^3, tb 3: 183 against 240 GLUP/s): the CTAs then march
+// through different x ranges at once, and the halo rows that neighbouring
+// tiles share no longer meet in L2.
 int pick_xchunk(int nx, long long nyz, int resident, int T) {
   int xc = fm::tune_get("gs3d_f32k.xchunk", 0);
-  if (xc == 0 && nyz * nx < (1ll << 31)) return 0;
-  if (xc < 0) {
+  if (xc == -1 && nyz * nx < (1ll << 31)) return 0;
+  if (xc <= 0) {
     xc = 0;
     double best = 1e300;
     for (int cand = 4; cand <= nx; cand += 4) {
@@ -253,6 +256,139 @@ __global__ void __launch_bounds__(kE *kE, 1)
               cUn[g] = cun;
               cVn[g] = cvn;
             }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// gs3d_f32k_tbf<T>: gs3d_f32k_tb (32x32 threads, one y row per warp) with the
+// x and z face differences computed once, and the per-level state rotated
+// outside the row test so that the unrolled loop rotates it by renaming.
+//  * x: level l keeps P = its plane that level l+1 advances next, N = the plane
+//    after it and D = P - (the plane before P); the x term is (N - P) - D and
+//    N - P becomes the next D (one subtraction per field instead of two).
+//  * z: one shuffle brings W[z+1]; f = W[z+1] - W is the face above, a second
+//    shuffle brings lane - 1's f as the face below (again one subtraction).
+//  * y: from the shared-memory plane of the previous level, as before.
+//  * A warp whose row is outside level s's valid range skips the level's
+//    arithmetic; its new values are 0, which no valid cell reads.
+// Same operations on the same values as the fast form: bit-identical.
+template <int T>
+__global__ void __launch_bounds__(kE *kE, 1)
+    gs3d_f32k_tbf(const float *__restrict__ U, const float *__restrict__ V,
+                  const float *__restrict__ cU, const float *__restrict__ cV,
+                  float *__restrict__ Un, float *__restrict__ Vn, float *__restrict__ cUn,
+                  float *__restrict__ cVn, int nx, int ny, int nz, int xchunk, int nty,
+                  int ntz, int ntiles, Gs32f c) {
+  constexpr int O = kE - 2 * T;
+  extern __shared__ float smem[];
+  float *s_u = smem;
+  float *s_v = smem + T * 2 * kE * kE;
+  const int lane = threadIdx.x & 31;
+  const int row = threadIdx.x >> 5;
+  const size_t sx = (size_t)ny * nz;
+  Pieces pcs(nty * ntz, nx, xchunk);
+  int pc, x0, x1;
+  while (pcs.next(nty * ntz, nx, xchunk, ntiles, pc, x0, x1)) {
+    const int tz = pc % ntz;
+    const int ty = pc / ntz;
+    const int gy_out = ty * O + row - T;
+    const int gz_out = tz * O + lane - T;
+    const size_t col = (size_t)wrap_any(gy_out, ny) * nz + wrap_any(gz_out, nz);
+    const bool writer = row >= T && row < T + O && lane >= T && lane < T + O &&
+                        gy_out < ny && gz_out < nz;
+    float Pu[T], Nu[T], Du[T], Pv[T], Nv[T], Dv[T], clu[T], clv[T];
+#pragma unroll
+    for (int s = 0; s < T; ++s) Pu[s] = Nu[s] = Du[s] = Pv[s] = Nv[s] = Dv[s] = clu[s] = clv[s] = 0.0f;
+    constexpr int kPF = 2;
+    float pu[kPF], pv[kPF], pcu[kPF], pcv[kPF];
+#pragma unroll
+    for (int k = 0; k < kPF; ++k) {
+      const size_t g = (size_t)wrap_any(x0 - T + k, nx) * sx + col;
+      pu[k] = __ldg(U + g);
+      pv[k] = __ldg(V + g);
+      pcu[k] = __ldg(cU + g);
+      pcv[k] = __ldg(cV + g);
+    }
+    // unrolled by 2: the P/N roles, the prefetch queue and the parity all have period 2
+#pragma unroll 2
+    for (int i = x0 - T; i < x1 + T; ++i) {
+      const int par = i & 1;
+      const float in_u = pu[0], in_v = pv[0], in_cu = pcu[0], in_cv = pcv[0];
+#pragma unroll
+      for (int k = 0; k + 1 < kPF; ++k) {
+        pu[k] = pu[k + 1];
+        pv[k] = pv[k + 1];
+        pcu[k] = pcu[k + 1];
+        pcv[k] = pcv[k + 1];
+      }
+      if (i + kPF < x1 + T) {
+        int ip = i + kPF;
+        if (nx >= 8)
+          ip = ip < 0 ? ip + nx : (ip >= nx ? ip - nx : ip);
+        else
+          ip = wrap_any(ip, nx);
+        const size_t g = (size_t)ip * sx + col;
+        pu[kPF - 1] = __ldg(U + g);
+        pv[kPF - 1] = __ldg(V + g);
+        pcu[kPF - 1] = __ldg(cU + g);
+        pcv[kPF - 1] = __ldg(cV + g);
+      }
+      Pu[0] = Nu[0];
+      Nu[0] = in_u;
+      Pv[0] = Nv[0];
+      Nv[0] = in_v;
+      s_u[((0 * 2 + par) * kE + row) * kE + lane] = in_u;
+      s_v[((0 * 2 + par) * kE + row) * kE + lane] = in_v;
+      float carry_u = clu[0], carry_v = clv[0];
+      clu[0] = in_cu;
+      clv[0] = in_cv;
+#pragma unroll
+      for (int s = 1; s <= T; ++s) {
+        const int l = s - 1;
+        const float u = Pu[l], v = Pv[l];
+        const float dnu = Nu[l] - u, dnv = Nv[l] - v;  // x faces above
+        const float lxu = dnu - Du[l], lxv = dnv - Dv[l];
+        Du[l] = dnu;
+        Dv[l] = dnv;
+        float un = 0.0f, vn = 0.0f, cun = 0.0f, cvn = 0.0f;
+        if (row >= s && row < kE - s) {  // warp-uniform
+          const float zpu = __shfl_down_sync(0xffffffffu, u, 1);
+          const float zpv = __shfl_down_sync(0xffffffffu, v, 1);
+          const float fzu = zpu - u, fzv = zpv - v;  // z faces above
+          const float fzmu = __shfl_up_sync(0xffffffffu, fzu, 1);
+          const float fzmv = __shfl_up_sync(0xffffffffu, fzv, 1);
+          const int base = (l * 2 + (par ^ 1)) * kE;
+          const float uym = s_u[(base + row - 1) * kE + lane];
+          const float uyp = s_u[(base + row + 1) * kE + lane];
+          const float vym = s_v[(base + row - 1) * kE + lane];
+          const float vyp = s_v[(base + row + 1) * kE + lane];
+          const float lu = (lxu + ((uyp - u) - (u - uym))) + (fzu - fzmu);
+          const float lv = (lxv + ((vyp - v) - (v - vym))) + (fzv - fzmv);
+          cell_step(u, v, lu, lv, carry_u, carry_v, c, un, vn, cun, cvn);
+        }
+        if (s < T) {
+          carry_u = clu[s];
+          carry_v = clv[s];
+          clu[s] = cun;
+          clv[s] = cvn;
+          Pu[s] = Nu[s];
+          Nu[s] = un;
+          Pv[s] = Nv[s];
+          Nv[s] = vn;
+          s_u[((s * 2 + par) * kE + row) * kE + lane] = un;
+          s_v[((s * 2 + par) * kE + row) * kE + lane] = vn;
+        } else {
+          const int p = i - T;
+          if (writer && p >= x0) {
+            const size_t g = (size_t)p * sx + col;
+            Un[g] = un;
+            Vn[g] = vn;
+            cUn[g] = cun;
+            cVn[g] = cvn;
           }
         }
       }
@@ -484,17 +620,18 @@ int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const flo
   return FM_OK;
 }
 
-template <int T>
+template <int T, bool F = false>
 int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const float *cu,
               const float *cv, float *un, float *vn, float *cun, float *cvn, const Gs32f &c,
               cudaStream_t s) {
+  auto kern = F ? gs3d_f32k_tbf<T> : gs3d_f32k_tb<T>;
   constexpr int O = kE - 2 * T;
   const size_t smem = (size_t)2 * T * 2 * kE * kE * sizeof(float);
   static bool attr_set[64] = {false};
   int dev = 0;
   FM_TRY_CUDA(cudaGetDevice(&dev));
   if (dev < 64 && !attr_set[dev]) {
-    FM_TRY_CUDA(cudaFuncSetAttribute(gs3d_f32k_tb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    FM_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
     attr_set[dev] = true;
   }
@@ -502,8 +639,7 @@ int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const floa
   int st = fm::device_sm_count(&sms);
   if (st) return st;
   int per_sm = 0;
-  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gs3d_f32k_tb<T>, kE * kE,
-                                                             smem));
+  FM_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kE * kE, smem));
   const int resident = sms * std::max(per_sm, 1);
   const int nty = (ny + O - 1) / O, ntz = (nz + O - 1) / O;
   const long long nyz = (long long)nty * ntz;
@@ -514,7 +650,7 @@ int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const floa
     return FM_ERR_UNSUPPORTED;
   }
   const int grid = (int)std::min<long long>(ntiles, resident);
-  gs3d_f32k_tb<T><<<grid, kE * kE, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz, xc,
+  kern<<<grid, kE * kE, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz, xc,
                                                nty, ntz, (int)ntiles, c);
   FM_TRY_CUDA(cudaGetLastError());
   return FM_OK;
@@ -544,9 +680,10 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   const size_t n = (size_t)nx * ny * nz;
   float *cur[4] = {U, V, cU, cV};
   float *nxt[4] = {work, work + n, work + 2 * n, work + 3 * n};
-  // 1: register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread,
-  // 16 warps; 3, 4: the same with 3 planes prefetched instead of 2; 0: one row per
-  // warp (32x32 threads)
+  // 0: one row per warp (32x32 threads); 5: the same with the x and z face
+  // differences computed once; 1: register-blocked kernel, 4 rows per thread, 8
+  // warps; 2: 2 rows per thread, 16 warps; 3, 4: the same with 3 planes prefetched
+  // instead of 2
   const int kern = fm::tune_get("gs3d_f32k.kernel", 0);
   int done = 0;
   while (done < steps) {
@@ -574,12 +711,13 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
       done += t;
       continue;
     }
-    switch (t) {
-      case 1: st = launch_tb<1>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
-      case 2: st = launch_tb<2>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
-      case 3: st = launch_tb<3>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
-      default: st = launch_tb<4>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s); break;
-    }
+#define FM_TB(TT, FF) \
+  launch_tb<TT, FF>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s)
+    if (kern == 5)
+      st = t == 1 ? FM_TB(1, true) : t == 2 ? FM_TB(2, true) : t == 3 ? FM_TB(3, true) : FM_TB(4, true);
+    else
+      st = t == 1 ? FM_TB(1, false) : t == 2 ? FM_TB(2, false) : t == 3 ? FM_TB(3, false) : FM_TB(4, false);
+#undef FM_TB
     if (st) return st;
     for (int k = 0; k < 4; ++k) std::swap(cur[k], nxt[k]);
     done += t;
