@@ -264,139 +264,6 @@ __global__ void __launch_bounds__(kE *kE, 1)
   }
 }
 
-// gs3d_f32k_tbf<T>: gs3d_f32k_tb (32x32 threads, one y row per warp) with the
-// x and z face differences computed once, and the per-level state rotated
-// outside the row test so that the unrolled loop rotates it by renaming.
-//  * x: level l keeps P = its plane that level l+1 advances next, N = the plane
-//    after it and D = P - (the plane before P); the x term is (N - P) - D and
-//    N - P becomes the next D (one subtraction per field instead of two).
-//  * z: one shuffle brings W[z+1]; f = W[z+1] - W is the face above, a second
-//    shuffle brings lane - 1's f as the face below (again one subtraction).
-//  * y: from the shared-memory plane of the previous level, as before.
-//  * A warp whose row is outside level s's valid range skips the level's
-//    arithmetic; its new values are 0, which no valid cell reads.
-// Same operations on the same values as the fast form: bit-identical.
-template <int T>
-__global__ void __launch_bounds__(kE *kE, 1)
-    gs3d_f32k_tbf(const float *__restrict__ U, const float *__restrict__ V,
-                  const float *__restrict__ cU, const float *__restrict__ cV,
-                  float *__restrict__ Un, float *__restrict__ Vn, float *__restrict__ cUn,
-                  float *__restrict__ cVn, int nx, int ny, int nz, int xchunk, int nty,
-                  int ntz, int ntiles, Gs32f c) {
-  constexpr int O = kE - 2 * T;
-  extern __shared__ float smem[];
-  float *s_u = smem;
-  float *s_v = smem + T * 2 * kE * kE;
-  const int lane = threadIdx.x & 31;
-  const int row = threadIdx.x >> 5;
-  const size_t sx = (size_t)ny * nz;
-  Pieces pcs(nty * ntz, nx, xchunk);
-  int pc, x0, x1;
-  while (pcs.next(nty * ntz, nx, xchunk, ntiles, pc, x0, x1)) {
-    const int tz = pc % ntz;
-    const int ty = pc / ntz;
-    const int gy_out = ty * O + row - T;
-    const int gz_out = tz * O + lane - T;
-    const size_t col = (size_t)wrap_any(gy_out, ny) * nz + wrap_any(gz_out, nz);
-    const bool writer = row >= T && row < T + O && lane >= T && lane < T + O &&
-                        gy_out < ny && gz_out < nz;
-    float Pu[T], Nu[T], Du[T], Pv[T], Nv[T], Dv[T], clu[T], clv[T];
-#pragma unroll
-    for (int s = 0; s < T; ++s) Pu[s] = Nu[s] = Du[s] = Pv[s] = Nv[s] = Dv[s] = clu[s] = clv[s] = 0.0f;
-    constexpr int kPF = 2;
-    float pu[kPF], pv[kPF], pcu[kPF], pcv[kPF];
-#pragma unroll
-    for (int k = 0; k < kPF; ++k) {
-      const size_t g = (size_t)wrap_any(x0 - T + k, nx) * sx + col;
-      pu[k] = __ldg(U + g);
-      pv[k] = __ldg(V + g);
-      pcu[k] = __ldg(cU + g);
-      pcv[k] = __ldg(cV + g);
-    }
-    // unrolled by 2: the P/N roles, the prefetch queue and the parity all have period 2
-#pragma unroll 2
-    for (int i = x0 - T; i < x1 + T; ++i) {
-      const int par = i & 1;
-      const float in_u = pu[0], in_v = pv[0], in_cu = pcu[0], in_cv = pcv[0];
-#pragma unroll
-      for (int k = 0; k + 1 < kPF; ++k) {
-        pu[k] = pu[k + 1];
-        pv[k] = pv[k + 1];
-        pcu[k] = pcu[k + 1];
-        pcv[k] = pcv[k + 1];
-      }
-      if (i + kPF < x1 + T) {
-        int ip = i + kPF;
-        if (nx >= 8)
-          ip = ip < 0 ? ip + nx : (ip >= nx ? ip - nx : ip);
-        else
-          ip = wrap_any(ip, nx);
-        const size_t g = (size_t)ip * sx + col;
-        pu[kPF - 1] = __ldg(U + g);
-        pv[kPF - 1] = __ldg(V + g);
-        pcu[kPF - 1] = __ldg(cU + g);
-        pcv[kPF - 1] = __ldg(cV + g);
-      }
-      Pu[0] = Nu[0];
-      Nu[0] = in_u;
-      Pv[0] = Nv[0];
-      Nv[0] = in_v;
-      s_u[((0 * 2 + par) * kE + row) * kE + lane] = in_u;
-      s_v[((0 * 2 + par) * kE + row) * kE + lane] = in_v;
-      float carry_u = clu[0], carry_v = clv[0];
-      clu[0] = in_cu;
-      clv[0] = in_cv;
-#pragma unroll
-      for (int s = 1; s <= T; ++s) {
-        const int l = s - 1;
-        const float u = Pu[l], v = Pv[l];
-        const float dnu = Nu[l] - u, dnv = Nv[l] - v;  // x faces above
-        const float lxu = dnu - Du[l], lxv = dnv - Dv[l];
-        Du[l] = dnu;
-        Dv[l] = dnv;
-        float un = 0.0f, vn = 0.0f, cun = 0.0f, cvn = 0.0f;
-        if (row >= s && row < kE - s) {  // warp-uniform
-          const float zpu = __shfl_down_sync(0xffffffffu, u, 1);
-          const float zpv = __shfl_down_sync(0xffffffffu, v, 1);
-          const float fzu = zpu - u, fzv = zpv - v;  // z faces above
-          const float fzmu = __shfl_up_sync(0xffffffffu, fzu, 1);
-          const float fzmv = __shfl_up_sync(0xffffffffu, fzv, 1);
-          const int base = (l * 2 + (par ^ 1)) * kE;
-          const float uym = s_u[(base + row - 1) * kE + lane];
-          const float uyp = s_u[(base + row + 1) * kE + lane];
-          const float vym = s_v[(base + row - 1) * kE + lane];
-          const float vyp = s_v[(base + row + 1) * kE + lane];
-          const float lu = (lxu + ((uyp - u) - (u - uym))) + (fzu - fzmu);
-          const float lv = (lxv + ((vyp - v) - (v - vym))) + (fzv - fzmv);
-          cell_step(u, v, lu, lv, carry_u, carry_v, c, un, vn, cun, cvn);
-        }
-        if (s < T) {
-          carry_u = clu[s];
-          carry_v = clv[s];
-          clu[s] = cun;
-          clv[s] = cvn;
-          Pu[s] = Nu[s];
-          Nu[s] = un;
-          Pv[s] = Nv[s];
-          Nv[s] = vn;
-          s_u[((s * 2 + par) * kE + row) * kE + lane] = un;
-          s_v[((s * 2 + par) * kE + row) * kE + lane] = vn;
-        } else {
-          const int p = i - T;
-          if (writer && p >= x0) {
-            const size_t g = (size_t)p * sx + col;
-            Un[g] = un;
-            Vn[g] = vn;
-            cUn[g] = cun;
-            cVn[g] = cvn;
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
-}
-
 // gs3d_f32k_tbr<T, RY, W>: the same pipeline with register blocking along y
 // and each face difference computed once.
 //
@@ -620,11 +487,11 @@ int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const flo
   return FM_OK;
 }
 
-template <int T, bool F = false>
+template <int T>
 int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const float *cu,
               const float *cv, float *un, float *vn, float *cun, float *cvn, const Gs32f &c,
               cudaStream_t s) {
-  auto kern = F ? gs3d_f32k_tbf<T> : gs3d_f32k_tb<T>;
+  auto kern = gs3d_f32k_tb<T>;
   constexpr int O = kE - 2 * T;
   const size_t smem = (size_t)2 * T * 2 * kE * kE * sizeof(float);
   static bool attr_set[64] = {false};
@@ -680,30 +547,21 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   const size_t n = (size_t)nx * ny * nz;
   float *cur[4] = {U, V, cU, cV};
   float *nxt[4] = {work, work + n, work + 2 * n, work + 3 * n};
-  // 0: one row per warp (32x32 threads); 5: the same with the x and z face
-  // differences computed once; 1: register-blocked kernel, 4 rows per thread, 8
-  // warps; 2: 2 rows per thread, 16 warps; 3, 4: the same with 3 planes prefetched
-  // instead of 2
+  // 0: one row per warp (32x32 threads, the default: fastest measured); 1: the
+  // register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread, 16 warps
   const int kern = fm::tune_get("gs3d_f32k.kernel", 0);
   int done = 0;
   while (done < steps) {
     const int t = std::min(tb, steps - done);
     int st;
-    if (kern >= 1 && kern <= 4) {
+    if (kern == 1 || kern == 2) {
       float *a[8] = {cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3]};
 #define FM_TBR(TT, RR, WW, PP) \
   launch_tbr<TT, RR, WW, PP>(nx, ny, nz, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], c, s)
 #define FM_TBR_T(RR, WW, PP)                                                         \
   (t == 1 ? FM_TBR(1, RR, WW, PP) : t == 2 ? FM_TBR(2, RR, WW, PP)                  \
           : t == 3 ? FM_TBR(3, RR, WW, PP) : FM_TBR(4, RR, WW, PP))
-      if (kern == 1)
-        st = FM_TBR_T(4, 8, 2);
-      else if (kern == 2)
-        st = FM_TBR_T(2, 16, 2);
-      else if (kern == 3)
-        st = FM_TBR_T(4, 8, 3);
-      else
-        st = FM_TBR_T(2, 16, 3);
+      st = kern == 1 ? FM_TBR_T(4, 8, 2) : FM_TBR_T(2, 16, 2);
 #undef FM_TBR_T
 #undef FM_TBR
       if (st) return st;
@@ -711,12 +569,9 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
       done += t;
       continue;
     }
-#define FM_TB(TT, FF) \
-  launch_tb<TT, FF>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s)
-    if (kern == 5)
-      st = t == 1 ? FM_TB(1, true) : t == 2 ? FM_TB(2, true) : t == 3 ? FM_TB(3, true) : FM_TB(4, true);
-    else
-      st = t == 1 ? FM_TB(1, false) : t == 2 ? FM_TB(2, false) : t == 3 ? FM_TB(3, false) : FM_TB(4, false);
+#define FM_TB(TT) \
+  launch_tb<TT>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s)
+    st = t == 1 ? FM_TB(1) : t == 2 ? FM_TB(2) : t == 3 ? FM_TB(3) : FM_TB(4);
 #undef FM_TB
     if (st) return st;
     for (int k = 0; k < 4; ++k) std::swap(cur[k], nxt[k]);
