@@ -63,13 +63,14 @@ class _Layer:
 
 
 class Surrogate:
-    def __init__(self, seed: int = 0, device: str = "cuda"):
+    def __init__(self, seed: int = 0, device: str = "cuda", n_blocks: int = N_BLOCKS):
         g = torch.Generator().manual_seed(seed)
         self.dev = torch.device(device)
         self.err = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.layers: List[_Layer] = []
+        self.n_blocks = int(n_blocks)
         std = math.sqrt(2.0 / (9 * C))
-        n_layers = 2 + 2 * N_BLOCKS
+        n_layers = 2 + 2 * self.n_blocks
         for i in range(n_layers):
             w = torch.randn(C, 9, C, generator=g) * std
             mask = -1
@@ -112,10 +113,15 @@ class Surrogate:
             arrs["w%d" % i] = L.w.cpu().numpy()
             arrs["b%d" % i] = L.b.cpu().numpy()
         arrs["step"] = np.array(self.step_count)
+        arrs["n_blocks"] = np.array(self.n_blocks)
         np.savez_compressed(path, **arrs)
 
     def load_npz(self, path) -> None:
         with np.load(path) as z:
+            nb = int(z["n_blocks"]) if "n_blocks" in z else N_BLOCKS
+            if nb != self.n_blocks:
+                raise ValueError("%s holds %d residual blocks, this network has %d"
+                                 % (path, nb, self.n_blocks))
             for i, L in enumerate(self.layers):
                 L.w.copy_(torch.from_numpy(z["w%d" % i]).to(self.dev))
                 L.b.copy_(torch.from_numpy(z["b%d" % i]).to(self.dev))
@@ -157,7 +163,7 @@ class Surrogate:
         z0 = self._buf("z0", B, n) if keep else None
         self._conv(B, n, xpad, Ls[0], act=1, z_out=z0, y_out=h)
         acts = [h]
-        for k in range(N_BLOCKS):
+        for k in range(self.n_blocks):
             c1, c2 = Ls[1 + 2 * k], Ls[2 + 2 * k]
             a1 = self._buf("a1_%d" % k if keep else "a1", B, n)
             z1 = self._buf("z1_%d" % k, B, n) if keep else None
@@ -204,13 +210,13 @@ class Surrogate:
             L.gw.zero_()
             L.gb.zero_()
             check(lib().fm_sur_flip(_p(L.wb), _p(L.wf), _stream()), "fm_sur_flip")
-        hs = [self._buf("h%d" % k, B, n) for k in range(N_BLOCKS + 1)]
+        hs = [self._buf("h%d" % k, B, n) for k in range(self.n_blocks + 1)]
         # projection
         self._wgrad(B, n, hs[-1], dy, Ls[-1])
         dh = self._buf("dhA", B, n)
         self._conv(B, n, dy, Ls[-1], weights=Ls[-1].wf, bias=False, y_out=dh)
         # residual blocks, last to first
-        for k in reversed(range(N_BLOCKS)):
+        for k in reversed(range(self.n_blocks)):
             c1, c2 = Ls[1 + 2 * k], Ls[2 + 2 * k]
             a1, z1 = self._buf("a1_%d" % k, B, n), self._buf("z1_%d" % k, B, n)
             self._wgrad(B, n, a1, dh, c2)

@@ -70,9 +70,11 @@ class PairStream:
 
 def train(net: Surrogate, iters: int, n_inst: int = 64, N: int = 128, lr: float = 3e-4,
           seed: int = 1, time_budget: Optional[float] = None, log_every: int = 100,
-          warmup: int = 300) -> Dict:
-    """Adam with linear warm-up and cosine decay; returns the loss history."""
-    stream = PairStream(n_inst, N, seed=seed)
+          warmup: int = 300, burn_in=(0, 2000)) -> Dict:
+    """Adam with linear warm-up and cosine decay; returns the loss history.
+    Pairs come from `n_inst` N x N instances whose pool is re-seeded with a
+    burn-in drawn from `burn_in` steps."""
+    stream = PairStream(n_inst, N, seed=seed, burn_in=burn_in)
     hist = []
     t0 = time.time()
     done = 0
