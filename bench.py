@@ -603,11 +603,16 @@ def run_engine(args):
     prog.download()
     prog.forward()  # warm the host-copy path (registration, first copies)
     barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        prog.forward()
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk_e2e:
+        t0 = time.perf_counter()
+        e0.record()  # the legacy default stream, the one Formura_Forward uses
+        for _ in range(args.steps):
+            prog.forward()
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+    e2e_dev_s = e0.elapsed_time(e1) / 1e3
     barrier()
     # the host<->device copies of that path on their own (untimed above)
     copies = {}
@@ -620,6 +625,11 @@ def run_engine(args):
         torch.cuda.synchronize()
         copies[name + "_gbs"] = round(3 * 2 * 8 * N ** 3 / (time.perf_counter() - t) / 1e9, 1)
     copies["host_globals_pinned"] = "%d of 2" % prog.host_pinned()
+    # where the end-to-end time goes: the same loop's span on the device, and the
+    # SM clock during it (the FP64-bound kernel's time scales with the clock)
+    copies["device_span_s"] = round(e2e_dev_s, 4)
+    copies["wall_s"] = round(e2e_s, 4)
+    copies["clocks"] = clk_e2e.summary()
 
     # the state after one Formura_Forward from the seeded start (parity, FP32 score)
     U_final = V_final = None
