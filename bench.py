@@ -777,6 +777,26 @@ def run_profile_case(args):
         prog.advance(1)
         prog.download()
         prog.finalize()
+    elif args.profile == "fmr_gs3d_float_tb":
+        # examples/gray-scott-3d-float.fmr through the front end, blocked kernel
+        # (temporal_blocking_interval 4): `profile_steps` steps at n^3
+        import numpy as np
+
+        from formura_gb300.fmr import load_program
+        from formura_gb300.runtime import load_program as load_lib
+
+        p = load_program(ROOT / "examples" / "gray-scott-3d-float.fmr", intra_node_shape=[n, n, n],
+                         monitor_interval=args.profile_steps, tb_kernel=1,
+                         name="fmr_gs3d_float_prof")
+        prog = load_lib(p)
+        prog.init()
+        U0, V0 = inits.gray_scott_3d(n, n, n, seed=1)
+        prog.state["U"][...] = U0.astype(np.float32)
+        prog.state["V"][...] = V0.astype(np.float32)
+        prog.upload()
+        prog.advance(1)
+        prog.download()
+        prog.finalize()
     elif args.profile == "surrogate":
         # `profile_steps` network jumps (and one training step) on `profile_batch` instances of n x n
         from formura_gb300.surrogate import Surrogate
@@ -811,7 +831,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
     ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",
-                                          "mhd", "mhd_f64", "diff2d", "surrogate", "fmr_gs3d"],
+                                          "mhd", "mhd_f64", "diff2d", "surrogate", "fmr_gs3d",
+                                          "fmr_gs3d_float_tb"],
                     default=None,
                     help="run a small case of one kernel for an ncu capture, then exit")
     ap.add_argument("--profile-n", type=int, default=256)
