@@ -100,6 +100,8 @@ SIGNATURES = {
     "fm_snapshot_destroy": (None, [c_void_p]),
     "fm_sum_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "fm_sum_f32_as_f64": (c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "fm_tensor_map_3d": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int,
+                                 c_int]),
     "fm_tune_set": (c_int, [ctypes.c_char_p, c_int]),
     "fm_tune_get": (c_int, [ctypes.c_char_p, c_int]),
     "fm_tune_clear": (c_int, []),

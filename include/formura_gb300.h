@@ -361,6 +361,20 @@ int fm_snapshot_begin(fm_snapshot *s, const void *array, int axis, int index, vo
 int fm_snapshot_wait(fm_snapshot *s, void *host_out);
 void fm_snapshot_destroy(fm_snapshot *s);
 
+/* ---- TMA tensor maps -------------------------------------------------------------- */
+
+/*
+ * No counterpart in the reference (it has no GPU code): encodes into `map` (a
+ * 128-byte, 64-byte-aligned CUtensorMap) a tiled TMA description of a dense
+ * row-major [n0][n1][n2] array of 4- or 8-byte elements at `base`, with a box
+ * of box0 x box1 x box2 elements (each 1..256).  The generated temporally
+ * blocked kernels of .fmr programs stage the planes of their tiles with it.
+ * Requires base 16-byte aligned and n2, box2 rows of a multiple of 16 bytes;
+ * FM_ERR_UNSUPPORTED when the driver offers no encoder.
+ */
+int fm_tensor_map_3d(void *map, const void *base, int elem_bytes, int n0, int n1, int n2,
+                     int box0, int box1, int box2);
+
 /* ---- tuning ------------------------------------------------------------------ */
 
 /*
