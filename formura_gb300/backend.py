@@ -348,6 +348,24 @@ def _fmr_parts(p: Program):
                      " g_grid_tb = %d < sms ? %d : sms; }" % (plan.ntiles, plan.ntiles))
         args = ["(const %s*)g_dev[%d]" % (dict(mmp.state)[n], sidx[n]) for n in sn_tb]
         args += ["(%s*)g_next[%d]" % (a.ctype, sidx[a.store_of]) for a in aw_tb]
+        args += ["g_tm[g_dev[%d] == g_tm_base[0][%d] ? 0 : 1][%d]" % (sidx[n], sidx[n], sidx[n])
+                 for n in sn_tb]
+        args += ["g_use_tma", "g_err"]
+        # the error word of the blocked kernel's bounded TMA waits, and the tensor maps of
+        # both buffers of every state it reads (box: one plane of its tile region)
+        alloc.append('  if ((st = fm_malloc((void**)&g_err, sizeof(int)))) return fail(st, "fm_malloc(err)");')
+        alloc.append('  if ((st = fm_memset(g_err, 0, sizeof(int), g_stream))) return fail(st, "err");')
+        if plan.tma:
+            sh = p.shape
+            alloc.append("  g_use_tma = 1;")
+            for n in sn_tb:
+                i = sidx[n]
+                for b, buf in ((0, "g_dev"), (1, "g_next")):
+                    alloc.append("  g_tm_base[%d][%d] = %s[%d];" % (b, i, buf, i))
+                    alloc.append("  if (fm_tensor_map_3d(&g_tm[%d][%d], %s[%d], %d, %d, %d, %d, 1, %d, %d))"
+                                 " g_use_tma = 0;  /* no encoder: gather every tile */"
+                                 % (b, i, buf, i, plan.sizes[n], sh[0], sh[1], sh[2],
+                                    plan.RG[1], plan.RG[2]))
         run += ["  /* %d steps per pass of the blocked kernel, the rest one step per launch */" % plan.T,
                 "  for (; t + %d <= steps; t += %d) {" % (plan.T, plan.T),
                 "    fmr_level_tb<<<g_grid_tb, %d, %d, s>>>(%s);" % (TB_THREADS, plan.smem,
@@ -379,7 +397,19 @@ def _fmr_parts(p: Program):
     decls = ["static void *g_next[%d] = {0};" % max(1, len(states)),
              "static void *g_arr[%d] = {0};" % max(1, len(arrays)),
              "static int g_grid = 1;", "static int g_grid_tb = 1;"]
-    return kern, decls, alloc, run, free
+    check = []
+    if tb is not None:
+        decls += ["alignas(64) static CUtensorMap g_tm[2][%d];" % max(1, len(states)),
+                  "static void *g_tm_base[2][%d] = {{0}};" % max(1, len(states)),
+                  "static int g_use_tma = 0;", "static int *g_err = 0;"]
+        free += ["  fm_free(g_err); g_err = 0;"]
+        # after Download's stream synchronization: did a bounded wait of the blocked kernel
+        # give up since the last check?
+        check = ["  { int e = 0;",
+                 '    if ((st = fm_memcpy_d2h(&e, g_err, sizeof(int), g_stream)) || (st = fm_stream_sync(g_stream))) return fail(st, "error word");',
+                 "    if (e) { fm_memset(g_err, 0, sizeof(int), g_stream); fm_stream_sync(g_stream);",
+                 '      return fail(FM_ERR_TIMEOUT, "blocked kernel: a TMA wait gave up"); } }']
+    return kern, decls, alloc, run, free, check
 
 
 def emit_source(p: Program) -> str:
@@ -408,14 +438,17 @@ def emit_source(p: Program) -> str:
     w("#include <stdio.h>")
     w("#include <stdlib.h>")
     if fmr:
+        w("#include <cuda.h>")
         w("#include <cuda_runtime.h>")
         w('#include "fm_softfp.cuh"')
+        w('#include "fm_tc.cuh"')
+        w("#define FMR_TMAP const __grid_constant__ CUtensorMap")
     w("")
     w("#define NCELLS ((size_t)%d)" % ncells)
     w("#define FMR_EXPORT __attribute__((visibility(\"default\")))")
     w("")
     if fmr:
-        kern, decls, alloc, run, free = _fmr_parts(p)
+        kern, decls, alloc, run, free, check = _fmr_parts(p)
         w("namespace {")
         w(kern)
         w("}  // namespace")
@@ -506,6 +539,9 @@ def emit_source(p: Program) -> str:
     w("  for (int i = 0; i < kNState; ++i)")
     w('    if ((st = fm_memcpy_d2h(kHost[i], g_dev[i], kBytes[i], g_stream))) return fail(st, "download");')
     w('  if ((st = fm_stream_sync(g_stream))) return fail(st, "download sync");')
+    if fmr:
+        for line in check:
+            w(line)
     w("  return 0;")
     w("}")
     w("")

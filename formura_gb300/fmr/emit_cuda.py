@@ -521,14 +521,22 @@ def tb_eligible(mmp: MM.MMProgram) -> bool:
 
 
 class TBPlan:
-    """Geometry of the blocked kernel: stencil reach R[a] per axis (largest
-    |cursor| of a state read), halo H[a] = T * R[a] on the plane axes, the
-    plane tile (interior TI[a], region RG[a] = TI[a] + 2 H[a]) sized to the
-    shared-memory budget, the ring of NS = 2 R[0] + 2 planes per time level,
-    and the chunk XC of planes along axis 0 per tile."""
+    """Geometry of the blocked kernel.
+
+    * R[a]: stencil reach per axis (largest |cursor| of a state read).
+    * H[a]: halo per side on the plane axes, T * R[a]; with TMA staging the
+      fastest axis's halo is rounded up to a 16-byte multiple of elements.
+    * TI[a], RG[a] = TI[a] + 2 H[a]: the plane tile's interior and region,
+      sized to the shared-memory budget.
+    * Rings: level 0 keeps NS0 = NS + PD planes (PD planes prefetched by TMA),
+      levels 1..T-1 keep NS = 2 R[0] + 2 planes each; every ring plane takes PS
+      elements (the region, padded to 128 bytes).
+    * XC: planes along axis 0 per tile (chunk).
+    * tma: whether tiles away from the periodic boundary stage their input
+      planes with TMA (3 axes, 4- or 8-byte state, 16-byte aligned rows)."""
 
     def __init__(self, mmp: MM.MMProgram, T: int, budget: int = TB_SMEM_BUDGET,
-                 sms: int = 152):
+                 sms: int = 152, tma: bool = True):
         L = mmp.levels[0]
         d = mmp.dim
         self.T, self.dim, self.shape = T, d, list(mmp.shape)
@@ -541,25 +549,49 @@ class TBPlan:
         self.read = sorted({n for n, _ in L.reads_state})
         stype = dict(mmp.state)
         size = {"double": 8, "float": 4, "int": 4, "bool": 1}
-        per_pos = sum(size[stype[n]] for n in self.read) * self.NS * T
+        self.sizes = {n: size[stype[n]] for n in self.read}
+        sz = list(self.sizes.values()) or [8]
+        A = max(16 // s for s in sz) if all(s in (4, 8) for s in sz) else 0
+        self.tma = bool(tma and d == 3 and A and self.shape[2] % A == 0)
+        self.A = A if self.tma else 1
+        self.PD = 2 if self.tma else 0
+        self.NS0 = self.NS + self.PD
+        slots = self.NS0 + (T - 1) * self.NS
         H = [0] + [T * R[a] for a in range(1, d)]
+        if self.tma:
+            H[2] = -(-H[2] // A) * A
         TI = [0] * d
+        per_pos = sum(self.sizes.values()) * slots
         if d == 3:
             TI[2] = min(self.shape[2], max(8, 64 - 2 * H[2]))
+            if self.tma and TI[2] < self.shape[2]:
+                TI[2] = max(A, TI[2] // A * A)
             rg2 = TI[2] + 2 * H[2]
             rg1 = budget // max(1, per_pos * rg2)
             TI[1] = min(self.shape[1], rg1 - 2 * H[1])
+            if self.tma:
+                TI[1] = min(TI[1], 256 - 2 * H[1])  # a TMA box edge is at most 256
         else:
             TI[1] = min(self.shape[1], budget // max(1, per_pos) - 2 * H[1], 4096)
-        self.H, self.TI = H, TI
+        self.H = H
         self.ok = all(TI[a] >= 1 for a in range(1, d))
-        self.RG = [0] + [TI[a] + 2 * H[a] for a in range(1, d)]
-        self.NT = [0] + [(self.shape[a] + TI[a] - 1) // TI[a] if self.ok else 1
+        while True:
+            self.TI = TI
+            self.RG = [0] + [TI[a] + 2 * H[a] for a in range(1, d)]
+            self.plane = 1
+            for a in range(1, d):
+                self.plane *= self.RG[a]
+            self.PS = -(-self.plane // 32) * 32
+            self.smem = sum(self.sizes.values()) * slots * self.PS
+            if not self.ok or self.smem <= budget or TI[1] <= 1:
+                break
+            TI = list(TI)
+            TI[1] -= 1
+        self.ok = self.ok and self.smem <= budget
+        if self.tma and self.ok and (self.RG[1] > 256 or self.RG[2] > 256):
+            self.tma = False
+        self.NT = [0] + [(self.shape[a] + self.TI[a] - 1) // self.TI[a] if self.ok else 1
                          for a in range(1, d)]
-        self.plane = 1
-        for a in range(1, d):
-            self.plane *= self.RG[a]
-        self.smem = per_pos * self.plane
         nyz = 1
         for a in range(1, d):
             nyz *= self.NT[a]
@@ -575,24 +607,36 @@ class TBPlan:
                 best, self.XC = cost, cand
         self.nchunk = (n0 + self.XC - 1) // self.XC
         self.ntiles = self.nchunk * nyz
-        self.sizes = {n: size[stype[n]] for n in self.read}
+
+    def ring_base(self, level: int) -> int:
+        """First element of `level`'s ring within a state's rings."""
+        return 0 if level == 0 else (self.NS0 + (level - 1) * self.NS) * self.PS
+
+    def ring_slots(self, level: int) -> int:
+        return self.NS0 if level == 0 else self.NS
 
 
 class TBEmitter(LevelEmitter):
     """Kernel ``fmr_level_tb``: T steps of the program's one level per pass
     over the state.  A CTA owns a plane tile (axes 1..d-1, region = interior
-    plus the halo of T steps) and marches along axis 0 over a chunk of
-    planes.  Each time level s = 0..T-1 keeps a ring of NS planes of the
-    region in shared memory; at iteration i level 0 loads plane i (periodic
-    wrap) and level s = 1..T evaluates plane i - s (R0 + 1) of the cells that
-    are still valid at level s (s R[a] away from the region's edge) from
-    level s-1's planes within R0 of it, all of which were written in earlier
-    iterations, so one __syncthreads per iteration orders every level.  Level
-    T writes the interior of the chunk's planes.  Each cell evaluates the
-    level's operations in the per-step kernel's order on the same values, so
-    the results equal T steps of that kernel bit for bit (the reference's
-    temporal blocking unrolls the step graph the same way,
-    src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134)."""
+    plus the halo of T steps) and marches along axis 0 over a chunk of planes.
+    Each time level s = 0..T-1 keeps a ring of planes of the region in shared
+    memory; at iteration i level 0 brings plane i, and level s = 1..T
+    evaluates plane i - s (R0 + 1) on the cells it must provide (within
+    (T - s) R[a] of the interior) from level s-1's planes within R0 of it,
+    all of which were written in earlier iterations, so one __syncthreads per
+    iteration orders every level.  Level T writes the tile's interior.  Each
+    cell evaluates the level's operations in the per-step kernel's order on
+    the same values, so the results equal T steps of that kernel bit for bit
+    (the reference's temporal blocking unrolls the step graph the same way,
+    src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134).
+
+    Level 0: a tile whose region lies inside the array (no periodic wrap)
+    receives each input plane by one TMA copy per state array
+    (cp.async.bulk.tensor, issued by one thread PD planes ahead, completing on
+    the slot's mbarrier; every wait is bounded and a wait that gives up sets
+    the error word); tiles at the periodic boundary gather the plane with
+    wrapped indices."""
 
     def __init__(self, mmp, plan: TBPlan, soft_div=True, soft_mul=True, soft_cmp=True):
         super().__init__(mmp, mmp.levels[0], 0, soft_div, soft_mul, soft_cmp)
@@ -600,30 +644,36 @@ class TBEmitter(LevelEmitter):
 
     def emit(self) -> Tuple[str, List[str], List[MM.Array]]:
         L, P = self.level, self.plan
-        d, T, R, NS, RG, TI, H = P.dim, P.T, P.R, P.NS, P.RG, P.TI, P.H
+        d, T, R, RG, TI, H = P.dim, P.T, P.R, P.RG, P.TI, P.H
         stypes = dict(self.mmp.state)
         state_names = sorted({n for n, _ in L.reads_state})
         params = ["const %s *__restrict__ s_%s" % (stypes[n], n) for n in state_names]
         params += ["%s *__restrict__ w_%s" % (a.ctype, a.name) for a in L.arrays]
-        plane = P.plane
+        params += ["FMR_TMAP tm_%s" % n for n in state_names]
+        params += ["int use_tma", "int *__restrict__ fmr_err"]
+        plane, PS = P.plane, P.PS
         out: List[str] = []
         w = out.append
         n0 = self.shape[0]
+        i0 = "(x0 - %d)" % (T * R[0])  # relative plane index k = i - i0
         w("#ifdef FMR_HOST_BUILD")
         w("static unsigned char fmr_tb_smem[%d];" % max(16, P.smem))
         w("#endif")
         w("__global__ void __launch_bounds__(%d, 1) fmr_level_tb(%s) {" % (TB_THREADS, ", ".join(params)))
         w("#ifndef FMR_HOST_BUILD")
-        w("  extern __shared__ __align__(16) unsigned char fmr_tb_smem[];")
+        w("  extern __shared__ __align__(128) unsigned char fmr_tb_smem[];")
+        w("  __shared__ __align__(8) uint64_t fmr_bar[%d];" % max(1, P.NS0))
+        w("  __shared__ int fmr_fail;")
         w("#endif")
         off = 0
         for n in state_names:
-            w("  %s *const m_%s = (%s *)(fmr_tb_smem + %d);  // [level][slot][plane]" %
-              (stypes[n], n, stypes[n], off))
-            off += P.sizes[n] * NS * T * plane
-        nyz = 1
-        for a in range(1, d):
-            nyz *= P.NT[a]
+            w("  %s *const m_%s = (%s *)(fmr_tb_smem + %d);  // rings: level 0, then levels 1..T-1"
+              % (stypes[n], n, stypes[n], off))
+            off += P.sizes[n] * (P.NS0 + (T - 1) * P.NS) * PS
+        tx_bytes = sum(P.sizes[n] for n in state_names) * plane
+        w("#ifndef FMR_HOST_BUILD")
+        w("  if (threadIdx.x == 0) fmr_fail = 0;")
+        w("#endif")
         w("  for (int tile = blockIdx.x; tile < %d; tile += gridDim.x) {" % P.ntiles)
         w("    int rest = tile;")
         for a in reversed(range(1, d)):
@@ -632,76 +682,108 @@ class TBEmitter(LevelEmitter):
             w("    rest /= %d;" % P.NT[a])
         w("    const int x0 = rest * %d;" % P.XC)
         w("    const int x1 = x0 + %d < %d ? x0 + %d : %d;" % (P.XC, n0, P.XC, n0))
-
-        def wrap(e: str, n: int) -> str:
-            return "(((%s) %% %d + %d) %% %d)" % (e, n, n, n)
-
-        def pos_coords(ind: str, valid_lo: List[int], vext: List[int]):
-            """j<a> (region coordinates) of item q within the valid box."""
-            if d == 3:
-                w(ind + "const int j1 = %d + q / %d, j2 = %d + q %% %d;" %
-                  (valid_lo[1], vext[2], valid_lo[2], vext[2]))
-            else:
-                w(ind + "const int j1 = %d + q;" % valid_lo[1])
-
-        def plane_index(js: List[str]) -> str:
-            if d == 3:
-                return "(%s) * %d + (%s)" % (js[1], RG[2], js[2])
-            return js[1]
-
+        w("    const int kend = x1 + %d - %s;  // planes level 0 brings: k in [0, kend)"
+          % (T * R[0], i0))
+        if P.tma:
+            conds = " && ".join("o%d >= 0 && o%d + %d <= %d" % (a, a, RG[a], self.shape[a])
+                                for a in range(1, d))
+            w("#ifndef FMR_HOST_BUILD")
+            w("    const bool tma = use_tma && %s;" % conds)
+            w("    if (tma) {")
+            w("      if (threadIdx.x == 0) {")
+            w("        for (int b = 0; b < %d; ++b) fm::tc::mbar_init(&fmr_bar[b], 1);" % P.NS0)
+            w('        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");')
+            w("        fm::tc::fence_proxy_async_smem();")
+            w("      }")
+            w("      __syncthreads();")
+            w("      if (threadIdx.x == 0)")
+            w("        for (int k = 0; k < %d && k < kend; ++k) fmr_tb_issue(k);" % P.PD)
+            w("    }")
+            w("#else")
+            w("    const bool tma = false;")
+            w("#endif")
         w("    for (int i = x0 - %d; i < x1 + %d; ++i) {" % (T * R[0], T * (R[0] + 1)))
-        w("      const int ib = ((i %% %d) + %d) %% %d;" % (NS, NS, NS))
+        w("      const int k = i - %s;" % i0)
         # level 0
-        w("      if (i < x1 + %d) {" % (T * R[0]))
-        w("        const int gx = %s;" % wrap("i", n0))
+        w("      if (!tma && k < kend) {  // gather plane i with periodic wrap" if P.tma else
+          "      if (k < kend) {  // gather plane i with periodic wrap")
+        w("        const int gx = ((i %% %d) + %d) %% %d;" % (n0, n0, n0))
+        w("        const int sl = k %% %d;" % P.NS0)
         w("        for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % plane)
-        pos_coords("          ", [0] * d, RG)
+        if d == 3:
+            w("          const int j1 = q / %d, j2 = q %% %d;" % (RG[2], RG[2]))
+        else:
+            w("          const int j1 = q;")
         gidx = "(size_t)gx"
         for a in range(1, d):
-            w("          const int g%d = %s;" % (a, wrap("o%d + j%d" % (a, a), self.shape[a])))
+            w("          const int g%d = (((o%d + j%d) %% %d) + %d) %% %d;" %
+              (a, a, a, self.shape[a], self.shape[a], self.shape[a]))
             gidx = "(%s * %d + g%d)" % (gidx, self.shape[a], a)
         for n in state_names:
-            w("          m_%s[ib * %d + q] = s_%s[%s];" % (n, plane, n, gidx))
+            w("          m_%s[sl * %d + q] = s_%s[%s];" % (n, PS, n, gidx))
         w("        }")
         w("      }")
+        if P.tma:
+            w("#ifndef FMR_HOST_BUILD")
+            w("      if (tma) {")
+            w("        if (threadIdx.x == 0 && k + %d < kend) fmr_tb_issue(k + %d);" % (P.PD, P.PD))
+            w("        // level 1 reads up to plane i - 1: wait for its copy (once per plane)")
+            w("        if (k >= 1 && k - 1 < kend && !fmr_fail &&")
+            w("            !fm::tc::mbar_wait(&fmr_bar[(k - 1) %% %d], ((k - 1) / %d) & 1)) {"
+              % (P.NS0, P.NS0))
+            w("          fmr_fail = 1;")
+            w("          atomicExch(fmr_err, 1);")
+            w("        }")
+            w("      }")
+            w("#endif")
         has_index = {m.args[0] for m in L.micro if m.kind == "index"}
+        lag = R[0] + 1
         for s_ in range(1, T + 1):
-            lag = s_ * (R[0] + 1)
-            lo = [0] + [s_ * R[a] for a in range(1, d)]
-            vext = [0] + [RG[a] - 2 * s_ * R[a] for a in range(1, d)]
+            lo = [0] + [H[a] - (T - s_) * R[a] for a in range(1, d)]
+            vext = [0] + [TI[a] + 2 * (T - s_) * R[a] for a in range(1, d)]
             cnt = 1
             for a in range(1, d):
                 cnt *= vext[a]
-            w("      {  // level %d: plane i - %d" % (s_, lag))
-            w("        const int p = i - %d;" % lag)
-            w("        if (p >= x0 - %d && p < x1 + %d) {" % ((T - s_) * R[0], (T - s_) * R[0]))
-            base_in = (s_ - 1) * NS * plane
+            w("      {  // level %d: plane i - %d" % (s_, s_ * lag))
+            w("        const int kq = k - %d;  // its relative plane index" % (s_ * lag))
+            w("        if (kq >= %d && kq < kend - %d) {" % (s_ * R[0], s_ * R[0]))
+            w("          const int p = i - %d;" % (s_ * lag))
+            base_in = P.ring_base(s_ - 1)
+            ns_in = P.ring_slots(s_ - 1)
             slots = {}
             for c0 in range(-R[0], R[0] + 1):
                 v = "sl%s%d" % ("m" if c0 < 0 else "p", abs(c0))
                 slots[c0] = v
-                w("          const int %s = (ib + %d) %% %d;" % (v, (c0 - lag) % NS, NS))
+                w("          const int %s = (kq %+d) %% %d;" % (v, c0, ns_in))
             if s_ < T:
-                w("          const int so = (ib + %d) %% %d;" % ((-lag) % NS, NS))
+                w("          const int so = kq %% %d;" % P.NS)
             if 0 in has_index:
-                w("          const int c0 = %s;" % wrap("p", n0))
+                w("          const int c0 = ((p %% %d) + %d) %% %d;" % (n0, n0, n0))
             w("          for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % cnt)
-            pos_coords("            ", lo, vext)
+            if d == 3:
+                w("            const int j1 = %d + q / %d, j2 = %d + q %% %d;" %
+                  (lo[1], vext[2], lo[2], vext[2]))
+            else:
+                w("            const int j1 = %d + q;" % lo[1])
             for a in range(1, d):
                 if a in has_index:
-                    w("            const int c%d = %s;" % (a, wrap("o%d + j%d" % (a, a), self.shape[a])))
+                    w("            const int c%d = (((o%d + j%d) %% %d) + %d) %% %d;" %
+                      (a, a, a, self.shape[a], self.shape[a], self.shape[a]))
+
+            def pidx(js):
+                return "(%s) * %d + (%s)" % (js[1], RG[2], js[2]) if d == 3 else js[1]
 
             def load(name, cur, _b=base_in, _sl=slots):
-                js = [None] + ["j%d%s" % (a, "" if cur[a] == 0 else "%+d" % cur[a]) for a in range(1, d)]
-                return "m_%s[%d + %s * %d + %s]" % (name, _b, _sl[cur[0]], plane, plane_index(js))
+                js = [None] + ["j%d%s" % (a, "" if cur[a] == 0 else "%+d" % cur[a])
+                               for a in range(1, d)]
+                return "m_%s[%d + %s * %d + %s]" % (name, _b, _sl[cur[0]], PS, pidx(js))
 
             self._emit_ops(range(len(L.micro)), {}, w, "            ", load_state=load)
             if s_ < T:
                 for arr in L.arrays:
                     if arr.store_of in state_names:
                         w("            m_%s[%d + so * %d + %s] = a%d;" %
-                          (arr.store_of, s_ * NS * plane, plane, plane_index([None, "j1", "j2"]),
-                           arr.root))
+                          (arr.store_of, P.ring_base(s_), PS, pidx([None, "j1", "j2"]), arr.root))
             else:
                 conds = ["p >= x0"]
                 gidx = "(size_t)p"
@@ -721,17 +803,32 @@ class TBEmitter(LevelEmitter):
         w("  }")
         w("}")
         w("")
-        return "\n".join(out), state_names, L.arrays
+        src = "\n".join(out)
+        if P.tma:
+            # the copy of relative plane k into its level-0 slot, one TMA box per state array
+            iss = ["#ifndef FMR_HOST_BUILD",
+                   "#define fmr_tb_issue(KK) do { \\",
+                   "    const int kk_ = (KK); \\",
+                   "    const int gx_ = (((x0 - %d + kk_) %% %d) + %d) %% %d; \\"
+                   % (T * R[0], n0, n0, n0),
+                   "    uint64_t *bar_ = &fmr_bar[kk_ %% %d]; \\" % P.NS0,
+                   "    fm::tc::mbar_arrive_expect_tx(bar_, %du); \\" % tx_bytes]
+            for n in state_names:
+                iss.append("    fm::tc::tma_load_3d(m_%s + (kk_ %% %d) * %d, &tm_%s, o2, o1, gx_, bar_); \\"
+                           % (n, P.NS0, PS, n))
+            iss += ["  } while (0)", "#endif", ""]
+            src = "\n".join(iss) + src
+        return src, state_names, L.arrays
 
 
 def emit_tb_kernel(mmp: MM.MMProgram, T: int, soft_div: bool = True, soft_mul: bool = True,
-                   soft_cmp: bool = True, budget: int = TB_SMEM_BUDGET):
+                   soft_cmp: bool = True, budget: int = TB_SMEM_BUDGET, tma: bool = True):
     """(source, plan, state names read, arrays written) of the blocked kernel
     ``fmr_level_tb`` (T steps per pass), or None when the program is not
     eligible (`tb_eligible`) or its halo leaves no room in shared memory."""
     if T < 2 or not tb_eligible(mmp):
         return None
-    plan = TBPlan(mmp, T, budget)
+    plan = TBPlan(mmp, T, budget, tma=tma)
     if not plan.ok:
         return None
     src, sn, aw = TBEmitter(mmp, plan, soft_div, soft_mul, soft_cmp).emit()

@@ -41,6 +41,7 @@ PRELUDE = r"""
 #define __launch_bounds__(threads, blocks)
 #define __syncthreads()
 #define FMR_HOST_BUILD 1
+#define FMR_TMAP const void *
 namespace {
 struct FmHostDim { unsigned x, y, z; };
 const FmHostDim blockIdx = {0u, 0u, 0u}, threadIdx = {0u, 0u, 0u};
@@ -132,6 +133,8 @@ def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = Tru
         _, plan, sn_tb, aw_tb = tbk
         args = ["(const %s*)cur[%d]" % (stype[s], sidx[s]) for s in sn_tb]
         args += ["(%s*)nxt[%d]" % (a.ctype, sidx[a.store_of]) for a in aw_tb]
+        args += ["nullptr"] * len(sn_tb) + ["0", "&host_err"]  # no TMA on the host
+        w("  int host_err = 0;")
         w("  for (; t + %d <= steps; t += %d) {" % (plan.T, plan.T))
         w("    fmr_level_tb(%s);" % ", ".join(args))
         w("    for (int i = 0; i < %d; ++i) { void *x = cur[i]; cur[i] = nxt[i]; nxt[i] = x; }"

@@ -211,3 +211,31 @@ def test_which_programs_are_blocked():
     # FP64 with 8 steps per pass: the halo of 8 leaves no tile in shared memory
     assert backend.blocked_kernel(load_program(EX / "gray-scott-3d.fmr",
                                                temporal_blocking_interval=8, tb_kernel=1)) is None
+
+
+def test_blocked_kernel_tma_geometry():
+    """The TMA-staged tiles: 16-byte aligned origins and rows along the fastest
+    axis (a halo rounded up to 4 floats or 2 doubles), boxes of at most 256
+    elements per edge, ring planes padded to 128 bytes, and tiles away from
+    the periodic boundary present on the shapes the GPU tests use."""
+    from formura_gb300.fmr.emit_cuda import emit_tb_kernel
+
+    for fmr, shape, tb in (("gray-scott-3d-float.fmr", [12, 80, 192], 4),
+                           ("gray-scott-3d.fmr", [10, 70, 128], 2),
+                           ("gray-scott-3d-float.fmr", [256, 256, 256], 4)):
+        p = load_program(EX / fmr, intra_node_shape=shape)
+        src, plan, _, _ = emit_tb_kernel(p.compiled(), tb)
+        assert plan.tma and "cp.async.bulk" not in src  # the copies sit in fm_tc.cuh helpers
+        assert "fm::tc::tma_load_3d" in src and "fm::tc::mbar_wait" in src
+        elem = 4 if "float" in fmr else 8
+        assert (plan.H[2] * elem) % 16 == 0 and (plan.TI[2] * elem) % 16 == 0
+        assert plan.RG[1] <= 256 and plan.RG[2] <= 256 and (plan.PS * elem) % 128 == 0
+        interior = [(t1, t2) for t1 in range(plan.NT[1]) for t2 in range(plan.NT[2])
+                    if 0 <= t1 * plan.TI[1] - plan.H[1] and
+                    t1 * plan.TI[1] - plan.H[1] + plan.RG[1] <= shape[1] and
+                    0 <= t2 * plan.TI[2] - plan.H[2] and
+                    t2 * plan.TI[2] - plan.H[2] + plan.RG[2] <= shape[2]]
+        assert interior, (fmr, shape)
+    # 2D programs gather every plane
+    p = load_program(EX / "diffusion-2d.fmr", intra_node_shape=[64, 256])
+    assert not emit_tb_kernel(p.compiled(), 4)[1].tma

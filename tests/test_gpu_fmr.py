@@ -67,6 +67,11 @@ def _random_state(prog, rng):
                               temporal_blocking_interval=4, tb_kernel=1)),
     ("diffusion-2d.fmr", dict(intra_node_shape=[5, 700], monitor_interval=6,
                               temporal_blocking_interval=3, tb_kernel=1)),
+    # shapes with tiles away from the periodic boundary: their input planes arrive by TMA
+    ("gray-scott-3d-float.fmr", dict(intra_node_shape=[12, 80, 192], monitor_interval=8,
+                                     tb_kernel=1)),
+    ("gray-scott-3d.fmr", dict(intra_node_shape=[10, 70, 128], monitor_interval=4,
+                               temporal_blocking_interval=2, tb_kernel=1)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)
