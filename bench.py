@@ -352,7 +352,7 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
         errs[name] = float((x.double() - y).abs().max() / y.abs().max().clamp_min(1e-300))
     del t32, t64
     out["gray_scott_3d_generated_from_fmr"] = run_generated_variant(torch, U0, V0)
-    out["gray_scott_3d_float_blocked_from_fmr"] = run_generated_blocked_variant(torch, U0, V0, hbm)
+    out["generated_temporal_blocking"] = run_generated_blocked_variant(torch, U0, V0, hbm)
     out["surrogate_gs2d_512"] = run_surrogate_variant(torch)
     out["mhd_3d_256_fp32_bulk_fp64_energy"] = {
         "value": round(N ** 3 * 500 / sec / 1e9, 3), "unit": "GLUP/s", "steps": 500,
@@ -402,44 +402,57 @@ def run_generated_variant(torch, U0, V0):
 
 
 def run_generated_blocked_variant(torch, U0, V0, hbm):
-    """examples/gray-scott-3d-float.fmr (binary32, temporal_blocking_interval 4)
-    compiled by the front end at 256^3: the generated temporally blocked kernel
-    (4 steps per pass) against the same program run one step per launch, both
-    timed over one Formura_Advance of 2000 steps on the resident state, and
-    bit-equality of the two after those steps."""
+    """Temporal blocking of programs compiled by the front end, at 256^3 in
+    binary32 with temporal_blocking_interval 4: the generated blocked kernel
+    (4 steps per pass; tiles away from the periodic boundary staged by TMA)
+    against the same program one step per launch, each timed over one
+    Formura_Advance of 2000 steps on the resident state, and bit-equality of
+    the two.  examples/heat-3d-float.fmr is memory-bound (every operation a
+    float one); examples/gray-scott-3d-float.fmr divides by dx = 0.01, a
+    double constant, as the reference's generated C does, so it stays bound
+    by the FP64 pipe and blocking cannot pay there."""
     import numpy as np
 
     from formura_gb300 import backend
     from formura_gb300.fmr import load_program
     from formura_gb300.runtime import load_program as load_lib
 
-    res = {}
-    finals = []
-    for tbk, label in ((1, "blocked"), (-1, "per_step")):
-        p = load_program(ROOT / "examples" / "gray-scott-3d-float.fmr", tb_kernel=tbk,
-                         name="fmr_gs3d_float_%s" % label)
-        plan = backend.blocked_kernel(p)
-        prog = load_lib(p)
-        prog.init()
-        prog.state["U"][...] = U0.astype(np.float32)
-        prog.state["V"][...] = V0.astype(np.float32)
-        prog.upload()
-        prog.advance(1)  # warm-up
-        prog.upload()
-        sec = _event_time(torch, lambda: prog.advance(1))
-        prog.download()
-        finals.append((prog.state["U"].copy(), prog.state["V"].copy()))
-        res[label + "_glups"] = round(N ** 3 * p.steps_per_forward / sec / 1e9, 2)
-        if plan is not None:
-            pl = plan[1]
-            res["tile"] = {"interior": pl.TI[1:], "region": pl.RG[1:], "x_chunk": pl.XC,
-                           "tiles": pl.ntiles, "smem_bytes": pl.smem}
-        prog.finalize()
-    same = all(np.array_equal(a, b) for a, b in zip(finals[0], finals[1]))
-    return {"value": res["blocked_glups"], "unit": "GLUP/s", "steps": 2000, "tb": 4,
-            "per_step_glups": res["per_step_glups"], "bit_equal_blocked_vs_per_step": same,
-            "hbm_roofline_at_tb_glups": round(hbm / (16.0 / 4), 1), "tile": res.get("tile"),
+    out = {}
+    for prog_name, bytes_per_cell, init in (
+            ("heat-3d-float", 8, lambda: {"u": U0.astype(np.float32)}),
+            ("gray-scott-3d-float", 16, lambda: {"U": U0.astype(np.float32),
+                                                 "V": V0.astype(np.float32)})):
+        res, finals = {}, []
+        for tbk, label in ((1, "blocked"), (-1, "per_step")):
+            p = load_program(ROOT / "examples" / (prog_name + ".fmr"), tb_kernel=tbk,
+                             name="fmr_%s_%s" % (prog_name.replace("-", "_"), label))
+            plan = backend.blocked_kernel(p)
+            prog = load_lib(p)
+            prog.init()
+            for k, v in init().items():
+                prog.state[k][...] = v
+            prog.upload()
+            prog.advance(1)  # warm-up
+            prog.upload()
+            sec = _event_time(torch, lambda: prog.advance(1))
+            prog.download()
+            finals.append([prog.state[k].copy() for k in sorted(prog.state)])
+            res[label] = round(N ** 3 * p.steps_per_forward / sec / 1e9, 2)
+            if plan is not None:
+                pl = plan[1]
+                res["tile"] = {"interior": pl.TI[1:], "region": pl.RG[1:], "x_chunk": pl.XC,
+                               "tiles": pl.ntiles, "smem_bytes": pl.smem, "tma": pl.tma}
+            prog.finalize()
+        out[prog_name] = {
+            "value": res["blocked"], "unit": "GLUP/s", "steps": 2000, "tb": 4,
+            "per_step_glups": res["per_step"],
+            "bit_equal_blocked_vs_per_step": all(np.array_equal(a, b)
+                                                 for a, b in zip(finals[0], finals[1])),
+            "hbm_roofline_per_step_glups": round(hbm / bytes_per_cell, 1),
+            "hbm_roofline_at_tb_glups": round(hbm / (bytes_per_cell / 4), 1),
+            "tile": res.get("tile"),
             "kernel": "fmr_level_tb (generated, 4 steps per pass) vs fmr_level_0"}
+    return out
 
 
 def run_surrogate_variant(torch):
@@ -777,22 +790,24 @@ def run_profile_case(args):
         prog.advance(1)
         prog.download()
         prog.finalize()
-    elif args.profile == "fmr_gs3d_float_tb":
-        # examples/gray-scott-3d-float.fmr through the front end, blocked kernel
-        # (temporal_blocking_interval 4): `profile_steps` steps at n^3
+    elif args.profile in ("fmr_gs3d_float_tb", "fmr_heat_float_tb"):
+        # examples/gray-scott-3d-float.fmr or heat-3d-float.fmr through the front end,
+        # blocked kernel (temporal_blocking_interval 4): `profile_steps` steps at n^3
         import numpy as np
 
         from formura_gb300.fmr import load_program
         from formura_gb300.runtime import load_program as load_lib
 
-        p = load_program(ROOT / "examples" / "gray-scott-3d-float.fmr", intra_node_shape=[n, n, n],
+        src = "gray-scott-3d-float" if args.profile == "fmr_gs3d_float_tb" else "heat-3d-float"
+        p = load_program(ROOT / "examples" / (src + ".fmr"), intra_node_shape=[n, n, n],
                          monitor_interval=args.profile_steps, tb_kernel=1,
-                         name="fmr_gs3d_float_prof")
+                         name="fmr_%s_prof" % src.replace("-", "_"))
         prog = load_lib(p)
         prog.init()
         U0, V0 = inits.gray_scott_3d(n, n, n, seed=1)
-        prog.state["U"][...] = U0.astype(np.float32)
-        prog.state["V"][...] = V0.astype(np.float32)
+        for name, a in (("U", U0), ("V", V0), ("u", U0)):
+            if name in prog.state:
+                prog.state[name][...] = a.astype(np.float32)
         prog.upload()
         prog.advance(1)
         prog.download()
@@ -832,7 +847,7 @@ def main():
                     help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
     ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",
                                           "mhd", "mhd_f64", "diff2d", "surrogate", "fmr_gs3d",
-                                          "fmr_gs3d_float_tb"],
+                                          "fmr_gs3d_float_tb", "fmr_heat_float_tb"],
                     default=None,
                     help="run a small case of one kernel for an ncu capture, then exit")
     ap.add_argument("--profile-n", type=int, default=256)

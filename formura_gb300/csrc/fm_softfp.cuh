@@ -472,5 +472,68 @@ FM_SOFT_HD bool le_zero_s(double x) {
   return (a << 1) <= 0xffe0000000000000ull && ((a >> 63) != 0ull || (a << 1) == 0ull);
 }
 
+// ---- binary32 <-> binary64 conversions on the integer pipes ------------------
+//
+// A binary32 program divided or multiplied by a binary64 constant (C promotes
+// the float operand, as Formura's generated code does for its double literals)
+// runs as (float)op((double)x, c).  The widening is exact; the narrowing rounds
+// to nearest even.  Both are assembled from the IEEE fields: normal inputs (and
+// zeros) inline, everything else — subnormal, infinite, NaN, and narrowing
+// results outside the binary32 normal range — by the hardware conversion out
+// of line.
+#if defined(__CUDA_ARCH__)
+static __device__ __noinline__ double f2d_slow(float x) { return (double)x; }
+static __device__ __noinline__ float d2f_slow(double x) { return __double2float_rn(x); }
+#elif defined(FM_SOFT_SLOW_SENTINEL)
+inline double f2d_slow(float) { return sentinel(); }
+inline float d2f_slow(double) { return (float)sentinel(); }
+#else
+inline double f2d_slow(float x) { return (double)x; }
+inline float d2f_slow(double x) { return (float)x; }
+#endif
+
+FM_SOFT_HD uint32_t f32_bits(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(x);
+#else
+  uint32_t b;
+  memcpy(&b, &x, 4);
+  return b;
+#endif
+}
+FM_SOFT_HD float f32_from_bits(uint32_t b) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(b);
+#else
+  float x;
+  memcpy(&x, &b, 4);
+  return x;
+#endif
+}
+
+// (double)x, exactly: biased exponent + (1023 - 127), significand moved up 29 bits.
+FM_SOFT_HD double f2d_s(float x) {
+  const uint32_t b = f32_bits(x);
+  const uint32_t e = (b >> 23) & 0xffu;
+  if ((b << 1) == 0u) return from_words(b & 0x80000000u, 0u);  // +-0
+  if (e - 1u >= 254u) return f2d_slow(x);
+  return from_words((b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3), b << 29);
+}
+
+// (float)x rounded to nearest even: the top 23 significand bits, rounded on the
+// 29 dropped bits; the integer addition of the round-up carries a significand
+// that overflows into the exponent (and from the largest binade to infinity,
+// the correctly rounded result).
+FM_SOFT_HD float d2f_s(double x) {
+  const uint32_t h = hi_word(x), l = lo_word(x);
+  const uint32_t e = (h >> 20) & 0x7ffu;
+  if (((h << 1) | l) == 0u) return f32_from_bits(h & 0x80000000u);  // +-0
+  if (e - 897u > 253u) return d2f_slow(x);  // binary32 subnormal or beyond its range
+  uint32_t f = (h & 0x80000000u) | ((e - 896u) << 23) | ((h & 0xfffffu) << 3) | (l >> 29);
+  const uint32_t rest = l & 0x1fffffffu;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (f & 1u))) f += 1u;
+  return f32_from_bits(f);
+}
+
 }  // namespace soft
 }  // namespace fm

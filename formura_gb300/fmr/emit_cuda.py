@@ -22,6 +22,10 @@ results, csrc/fm_softfp.cuh), because the FP64 pipe is the scarce one:
     per divisor node shared by all its quotients;
   * ``fmax``/``fmin`` chains (``>?``, ``<?``, ``<%``) and ``< <= > >= == !=``
     of two doubles: ``max_s``/``min_s`` and the ordered-key comparisons.
+A float node whose C expression promotes a float operand against a double
+constant that is exactly a float (``1``, ``0.5``, ``2``...) is evaluated in
+float: the same bits (double rounding of binary32 operations through
+binary64 is innocuous), without the FP64 pipe.
 """
 from __future__ import annotations
 
@@ -61,6 +65,13 @@ def _normal_double(v) -> bool:
         return False
     a = abs(v)
     return math.isfinite(a) and a >= 2.2250738585072014e-308
+
+
+def _float_exact(v) -> bool:
+    """A finite double constant that binary32 represents exactly."""
+    if not isinstance(v, float) or not math.isfinite(v):
+        return False
+    return float(struct.unpack("<f", struct.pack("<f", v))[0]) == v
 
 
 def _pow2_exponent(v):
@@ -155,7 +166,42 @@ class LevelEmitter:
                 op, a, b = m.args
                 ta, tb = L.micro[a].ctype, L.micro[b].ctype
                 dd = t == "double" and ta == "double" and tb == "double"
-                if op == "**":
+                fa = ta == "float" and tb == "double" and b in const_vals and _float_exact(const_vals[b])
+                fb = tb == "float" and ta == "double" and a in const_vals and _float_exact(const_vals[a])
+                if op in ("+", "-", "*", "/") and t == "float" and (fa or fb):
+                    # C evaluates float (op) double in double and rounds to float; with the
+                    # constant exactly a float that equals the float operation: a binary64
+                    # (53-bit) result of two binary32 (24-bit) operands rounded again to
+                    # binary32 is the correctly rounded binary32 result, since 53 >= 2*24 + 2
+                    # (S. A. Figueroa, "When is double rounding innocuous?", SIGNUM
+                    # Newsletter 30(3), 1995).  Keeps float programs off the FP64 pipe.
+                    xa = n(a) if ta == "float" else MM.c_literal(const_vals[a], "float")
+                    xb = n(b) if tb == "float" else MM.c_literal(const_vals[b], "float")
+                    w(ind + "const float %s = (%s %s %s);" % (name, xa, op, xb))
+                elif (t == "float" and ta == "float" and tb == "double" and b in const_vals and
+                      _normal_double(const_vals[b]) and
+                      ((op == "/" and self.soft_div and const_vals[b] > 0) or
+                       (op == "*" and self.soft_mul))):
+                    # (float)((double)x op c) with the widening exact, the binary64 operation
+                    # correctly rounded and the narrowing to nearest even, all on the
+                    # integer pipes (fm_softfp.cuh): the same bits as the promoted C
+                    cv = const_vals[b]
+                    xd = "fm::soft::f2d_s(%s)" % n(a)
+                    k2 = _pow2_exponent(cv)
+                    if k2 is not None:
+                        e = "fm::soft::scale_pow2(%s, %d)" % (xd, -k2 if op == "/" else k2)
+                    elif op == "/":
+                        e = "fm::soft::div_const_s(%s, fm::soft::DivConstS%s)" % (xd, div_const_fields(cv))
+                    else:
+                        e = "fm::soft::mul_const_s(%s, fm::soft::MulConstS%s)" % (xd, mul_const_fields(cv))
+                    w(ind + "const float %s = fm::soft::d2f_s(%s);" % (name, e))
+                elif (t == "float" and op == "*" and self.soft_mul and tb == "float" and
+                      ta == "double" and a in const_vals and _normal_double(const_vals[a])):
+                    cv = const_vals[a]
+                    w(ind + "const float %s = fm::soft::d2f_s(fm::soft::mul_const_s("
+                            "fm::soft::f2d_s(%s), fm::soft::MulConstS%s));"
+                      % (name, n(b), mul_const_fields(cv)))
+                elif op == "**":
                     w(ind + "const %s %s = pow((double)%s, (double)%s);" % (t, name, n(a), n(b)))
                 elif (op == "/" and self.soft_div and dd and b in const_vals and
                       _pow2_exponent(const_vals[b]) is not None):

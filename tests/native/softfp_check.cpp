@@ -55,4 +55,12 @@ void softfp_div_reciprocal_words(double d, unsigned *r_hi, unsigned *r_lo) {
   *r_hi = c.r_hi;
   *r_lo = c.r_lo;
 }
+
+void softfp_f2d(const float *x, long n, double *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::f2d_s(x[i]);
+}
+
+void softfp_d2f(const double *x, long n, float *out) {
+  for (long i = 0; i < n; ++i) out[i] = fm::soft::d2f_s(x[i]);
+}
 }

@@ -154,6 +154,7 @@ TB_CASES = [
     ("gray-scott-3d.fmr", [16, 16, 16]), ("gray-scott-3d.fmr", [5, 7, 33]),
     ("diffusion-2d.fmr", [40, 64]), ("diffusion-2d.fmr", [7, 300]),
     ("fmr-libm.fmr", [13, 17]), ("gray-scott-3d-float.fmr", [1, 4, 3]),
+    ("heat-3d-float.fmr", [10, 40, 72]), ("heat-3d-float.fmr", [3, 5, 9]),
 ]
 
 

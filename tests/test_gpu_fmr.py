@@ -72,6 +72,9 @@ def _random_state(prog, rng):
                                      tb_kernel=1)),
     ("gray-scott-3d.fmr", dict(intra_node_shape=[10, 70, 128], monitor_interval=4,
                                temporal_blocking_interval=2, tb_kernel=1)),
+    ("heat-3d-float.fmr", dict(intra_node_shape=[20, 100, 192], monitor_interval=8)),
+    ("heat-3d-float.fmr", dict(intra_node_shape=[7, 9, 20], monitor_interval=12,
+                               temporal_blocking_interval=3)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)

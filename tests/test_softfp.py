@@ -34,6 +34,9 @@ def _build(tmp_path_factory, name, defines=()):
     L.softfp_min.argtypes = [dp, dp, ctypes.c_long, dp]
     L.softfp_le_zero.argtypes = [dp, ctypes.c_long, ctypes.POINTER(ctypes.c_ubyte)]
     L.softfp_cmp.argtypes = [dp, dp, ctypes.c_long, ctypes.POINTER(ctypes.c_ubyte)]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.softfp_f2d.argtypes = [fp, ctypes.c_long, dp]
+    L.softfp_d2f.argtypes = [dp, ctypes.c_long, fp]
     up = ctypes.POINTER(ctypes.c_ulonglong)
     L.softfp_recip115.argtypes = [up, ctypes.c_long, up]
     L.softfp_div_reciprocal_words.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_uint),
@@ -274,3 +277,53 @@ def test_comparisons_match_ieee(lib):
         assert np.array_equal((got & 1) != 0, xs < ys)
         assert np.array_equal((got & 2) != 0, xs <= ys)
         assert np.array_equal((got & 4) != 0, xs == ys)
+
+
+def test_float_double_conversions_match_ieee(lib):
+    """f2d_s (exact widening) and d2f_s (round to nearest even) against the
+    host's conversions: every float exponent, random significands, doubles
+    at and around binary32 rounding midpoints (ties to even both ways), the
+    largest binade rounding to infinity, the subnormal boundary and specials.
+    With the slow path replaced by the sentinel, every binary32-normal input
+    must still convert on the fast path."""
+    rng = np.random.default_rng(5)
+    fp = ctypes.POINTER(ctypes.c_float)
+    # widening
+    bits = (rng.integers(0, 2 ** 32, 400000, dtype=np.uint64)).astype(np.uint32)
+    special = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, 1e-45, -1e-45,
+                        1.17549435e-38, 3.4028235e38, -3.4028235e38], dtype=np.float32)
+    xf = np.concatenate([bits.view(np.float32), special])
+    out = np.empty(xf.size, dtype=np.float64)
+    lib.softfp_f2d(xf.ctypes.data_as(fp), xf.size, _p(out))
+    want = xf.astype(np.float64)
+    e = (xf.view(np.uint32) >> 23) & 0xFF
+    normal = ((e >= 1) & (e <= 254)) | (xf == 0)
+    got_bits, want_bits = out.view(np.uint64), want.view(np.uint64)
+    slow = got_bits == SENTINEL
+    assert not slow[normal].any()
+    ok = (got_bits == want_bits) | slow | (np.isnan(out) & np.isnan(want))
+    assert ok.all(), xf[~ok][:5]
+    # narrowing: random doubles over the binary32 range and beyond, and exact midpoints
+    m = rng.integers(0, 2 ** 52, 300000, dtype=np.uint64)
+    ex = rng.integers(1023 - 160, 1023 + 140, 300000, dtype=np.uint64)
+    sg = rng.integers(0, 2, 300000, dtype=np.uint64) << np.uint64(63)
+    xd = (sg | (ex << np.uint64(52)) | m).view(np.float64)
+    f = rng.integers(1, 2 ** 31, 100000, dtype=np.uint64).astype(np.uint32).view(np.float32)
+    f = f[np.isfinite(f)].astype(np.float64)
+    mid = f.view(np.uint64) | np.uint64(1 << 28)  # exactly half a binary32 ulp above
+    near = [mid, mid + np.uint64(1), mid - np.uint64(1)]
+    edges = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 3.4028235677973366e38,
+                      3.4028235677973362e38, 3.402823669209385e38, 1.1754943508222875e-38,
+                      1.1754942106924411e-38, 1e-300, -1e300], dtype=np.float64)
+    xd = np.concatenate([xd] + [a.view(np.float64) for a in near] + [edges])
+    out = np.empty(xd.size, dtype=np.float32)
+    lib.softfp_d2f(_p(xd), xd.size, out.ctypes.data_as(fp))
+    with np.errstate(over="ignore"):
+        want = xd.astype(np.float32)
+    got_bits, want_bits = out.view(np.uint32), want.view(np.uint32)
+    slow = np.isnan(out) & ~np.isnan(want)  # the sentinel narrows to a NaN
+    wn = np.abs(want.astype(np.float64))
+    in_range = (wn >= 1.1754943508222875e-38) & np.isfinite(want) | (xd == 0)
+    assert not slow[in_range & (np.abs(xd) < 3.4028235677973366e38)].any()
+    ok = (got_bits == want_bits) | slow | (np.isnan(out) & np.isnan(want))
+    assert ok.all(), xd[~ok][:5]
