@@ -289,7 +289,6 @@ def _work_elems(p: Program) -> str:
     return "NCELLS"
 
 
-TB_THREADS = 256
 
 
 def blocked_kernel(p: Program):
@@ -316,7 +315,7 @@ def blocked_kernel(p: Program):
 
 def _fmr_parts(p: Program):
     """Kernels, device buffers and the step loop of a form-"fmr" program."""
-    from .fmr.emit_cuda import emit_kernels
+    from .fmr.emit_cuda import TB_THREADS, emit_kernels
 
     mmp = p.compiled()
     kern, levels = emit_kernels(mmp, march_chunk=p.march_chunk, march_pair=p.march_pair)

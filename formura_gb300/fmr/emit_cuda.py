@@ -549,7 +549,7 @@ class LevelEmitter:
 # Temporal blocking of single-level programs
 
 TB_SMEM_BUDGET = 200 * 1024  # bytes of shared memory a blocked kernel may take
-TB_THREADS = 256
+TB_THREADS = 512
 
 
 def tb_eligible(mmp: MM.MMProgram) -> bool:
@@ -600,7 +600,7 @@ class TBPlan:
         A = max(16 // s for s in sz) if all(s in (4, 8) for s in sz) else 0
         self.tma = bool(tma and d == 3 and A and self.shape[2] % A == 0)
         self.A = A if self.tma else 1
-        self.PD = 2 if self.tma else 0
+        self.PD = 2  # planes brought ahead of their first use (TMA or cp.async)
         self.NS0 = self.NS + self.PD
         slots = self.NS0 + (T - 1) * self.NS
         H = [0] + [T * R[a] for a in range(1, d)]
@@ -730,10 +730,36 @@ class TBEmitter(LevelEmitter):
         w("    const int x1 = x0 + %d < %d ? x0 + %d : %d;" % (P.XC, n0, P.XC, n0))
         w("    const int kend = x1 + %d - %s;  // planes level 0 brings: k in [0, kend)"
           % (T * R[0], i0))
+        gx_of = lambda kk: "(((x0 - %d + (%s)) %% %d) + %d) %% %d" % (T * R[0], kk, n0, n0, n0)
+
+        def gather(kk: str, ind: str, asynchronous: bool):
+            """Plane kk (relative) of every state into its level-0 slot, wrapped."""
+            w(ind + "{")
+            w(ind + "  const int gx = %s;" % gx_of(kk))
+            w(ind + "  const int sl = (%s) %% %d;" % (kk, P.NS0))
+            w(ind + "  for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % plane)
+            if d == 3:
+                w(ind + "    const int j1 = q / %d, j2 = q %% %d;" % (RG[2], RG[2]))
+            else:
+                w(ind + "    const int j1 = q;")
+            gi = "(size_t)gx"
+            for a in range(1, d):
+                w(ind + "    const int g%d = (((o%d + j%d) %% %d) + %d) %% %d;" %
+                  (a, a, a, self.shape[a], self.shape[a], self.shape[a]))
+                gi = "(%s * %d + g%d)" % (gi, self.shape[a], a)
+            for n in state_names:
+                if asynchronous:
+                    w(ind + "    fmr_cp_async%d(m_%s + sl * %d + q, s_%s + %s);" %
+                      (P.sizes[n], n, PS, n, gi))
+                else:
+                    w(ind + "    m_%s[sl * %d + q] = s_%s[%s];" % (n, PS, n, gi))
+            w(ind + "  }")
+            w(ind + "}")
+
+        w("#ifndef FMR_HOST_BUILD")
         if P.tma:
             conds = " && ".join("o%d >= 0 && o%d + %d <= %d" % (a, a, RG[a], self.shape[a])
                                 for a in range(1, d))
-            w("#ifndef FMR_HOST_BUILD")
             w("    const bool tma = use_tma && %s;" % conds)
             w("    if (tma) {")
             w("      if (threadIdx.x == 0) {")
@@ -744,34 +770,26 @@ class TBEmitter(LevelEmitter):
             w("      __syncthreads();")
             w("      if (threadIdx.x == 0)")
             w("        for (int k = 0; k < %d && k < kend; ++k) fmr_tb_issue(k);" % P.PD)
-            w("    }")
-            w("#else")
+            w("    } else {")
+        else:
             w("    const bool tma = false;")
-            w("#endif")
+            w("    {")
+        w("      for (int kk = 0; kk < %d; ++kk) {  // cp.async of the first planes, one group each"
+          % P.PD)
+        w("        if (kk < kend)")
+        gather("kk", "        ", True)
+        w("        fmr_cp_async_commit();")
+        w("      }")
+        w("    }")
+        w("#endif")
         w("    for (int i = x0 - %d; i < x1 + %d; ++i) {" % (T * R[0], T * (R[0] + 1)))
         w("      const int k = i - %s;" % i0)
-        # level 0
-        w("      if (!tma && k < kend) {  // gather plane i with periodic wrap" if P.tma else
-          "      if (k < kend) {  // gather plane i with periodic wrap")
-        w("        const int gx = ((i %% %d) + %d) %% %d;" % (n0, n0, n0))
-        w("        const int sl = k %% %d;" % P.NS0)
-        w("        for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % plane)
-        if d == 3:
-            w("          const int j1 = q / %d, j2 = q %% %d;" % (RG[2], RG[2]))
-        else:
-            w("          const int j1 = q;")
-        gidx = "(size_t)gx"
-        for a in range(1, d):
-            w("          const int g%d = (((o%d + j%d) %% %d) + %d) %% %d;" %
-              (a, a, a, self.shape[a], self.shape[a], self.shape[a]))
-            gidx = "(%s * %d + g%d)" % (gidx, self.shape[a], a)
-        for n in state_names:
-            w("          m_%s[sl * %d + q] = s_%s[%s];" % (n, PS, n, gidx))
-        w("        }")
-        w("      }")
+        w("#ifdef FMR_HOST_BUILD")
+        w("      if (k < kend)")
+        gather("k", "      ", False)
+        w("#else")
+        w("      if (tma) {")
         if P.tma:
-            w("#ifndef FMR_HOST_BUILD")
-            w("      if (tma) {")
             w("        if (threadIdx.x == 0 && k + %d < kend) fmr_tb_issue(k + %d);" % (P.PD, P.PD))
             w("        // level 1 reads up to plane i - 1: wait for its copy (once per plane)")
             w("        if (k >= 1 && k - 1 < kend && !fmr_fail &&")
@@ -780,8 +798,12 @@ class TBEmitter(LevelEmitter):
             w("          fmr_fail = 1;")
             w("          atomicExch(fmr_err, 1);")
             w("        }")
-            w("      }")
-            w("#endif")
+        w("      } else {")
+        w("        if (k + %d < kend)" % P.PD)
+        gather("k + %d" % P.PD, "        ", True)
+        w("        fmr_cp_async_commit();")
+        w("      }")
+        w("#endif")
         has_index = {m.args[0] for m in L.micro if m.kind == "index"}
         lag = R[0] + 1
         for s_ in range(1, T + 1):
@@ -844,12 +866,33 @@ class TBEmitter(LevelEmitter):
             w("          }")
             w("        }")
             w("      }")
+        w("#ifndef FMR_HOST_BUILD")
+        w("      // the gathered plane k has landed (at most the %d newest groups pending)" % P.PD)
+        w("      if (!tma) fmr_cp_async_wait<%d>();" % P.PD)
+        w("#endif")
         w("      __syncthreads();")
         w("    }")
         w("  }")
         w("}")
         w("")
         src = "\n".join(out)
+        helpers = ["#ifndef FMR_HOST_BUILD",
+                   "__device__ __forceinline__ void fmr_cp_async4(void *dst, const void *src) {",
+                   '  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::'
+                   ' "r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src) : "memory");',
+                   "}",
+                   "__device__ __forceinline__ void fmr_cp_async8(void *dst, const void *src) {",
+                   '  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::'
+                   ' "r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src) : "memory");',
+                   "}",
+                   "__device__ __forceinline__ void fmr_cp_async_commit() {",
+                   '  asm volatile("cp.async.commit_group;" ::: "memory");',
+                   "}",
+                   "template <int N> __device__ __forceinline__ void fmr_cp_async_wait() {",
+                   '  asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory");',
+                   "}",
+                   "#endif", ""]
+        src = "\n".join(helpers) + src
         if P.tma:
             # the copy of relative plane k into its level-0 slot, one TMA box per state array
             iss = ["#ifndef FMR_HOST_BUILD",
