@@ -720,6 +720,9 @@ class TBEmitter(LevelEmitter):
         w("#ifndef FMR_HOST_BUILD")
         w("  if (threadIdx.x == 0) fmr_fail = 0;")
         w("#endif")
+        w("  const int fmr_tx = threadIdx.x % 64, fmr_ty = threadIdx.x / 64;")
+        w("  const int fmr_cs = blockDim.x < 64 ? blockDim.x : 64;")
+        w("  const int fmr_rs = blockDim.x < 64 ? 1 : blockDim.x / 64;")
         w("  for (int tile = blockIdx.x; tile < %d; tile += gridDim.x) {" % P.ntiles)
         w("    int rest = tile;")
         for a in reversed(range(1, d)):
@@ -827,12 +830,18 @@ class TBEmitter(LevelEmitter):
                 w("          const int so = kq %% %d;" % P.NS)
             if 0 in has_index:
                 w("          const int c0 = ((p %% %d) + %d) %% %d;" % (n0, n0, n0))
-            w("          for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % cnt)
-            if d == 3:
-                w("            const int j1 = %d + q / %d, j2 = %d + q %% %d;" %
-                  (lo[1], vext[2], lo[2], vext[2]))
+            if d == 3 and RG[2] <= 64:
+                # 64 threads along the fastest axis (a warp reads whole row segments), the
+                # rest along the rows: no division per cell
+                w("          for (int j1 = %d + fmr_ty; j1 < %d; j1 += fmr_rs)" % (lo[1], lo[1] + vext[1]))
+                w("          for (int j2 = %d + fmr_tx; j2 < %d; j2 += fmr_cs) {" % (lo[2], lo[2] + vext[2]))
             else:
-                w("            const int j1 = %d + q;" % lo[1])
+                w("          for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % cnt)
+                if d == 3:
+                    w("            const int j1 = %d + q / %d, j2 = %d + q %% %d;" %
+                      (lo[1], vext[2], lo[2], vext[2]))
+                else:
+                    w("            const int j1 = %d + q;" % lo[1])
             for a in range(1, d):
                 if a in has_index:
                     w("            const int c%d = (((o%d + j%d) %% %d) + %d) %% %d;" %
