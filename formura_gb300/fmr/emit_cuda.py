@@ -549,7 +549,7 @@ class LevelEmitter:
 # Temporal blocking of single-level programs
 
 TB_SMEM_BUDGET = 200 * 1024  # bytes of shared memory a blocked kernel may take
-TB_THREADS = 512
+TB_THREADS = 1024
 
 
 def tb_eligible(mmp: MM.MMProgram) -> bool:
