@@ -720,9 +720,14 @@ class TBEmitter(LevelEmitter):
         w("#ifndef FMR_HOST_BUILD")
         w("  if (threadIdx.x == 0) fmr_fail = 0;")
         w("#endif")
+        w("#ifdef FMR_HOST_BUILD")
         w("  const int fmr_tx = threadIdx.x % 64, fmr_ty = threadIdx.x / 64;")
         w("  const int fmr_cs = blockDim.x < 64 ? blockDim.x : 64;")
         w("  const int fmr_rs = blockDim.x < 64 ? 1 : blockDim.x / 64;")
+        w("#else  // the launch's block: %d threads, 64 along the fastest axis" % TB_THREADS)
+        w("  const int fmr_tx = threadIdx.x & 63, fmr_ty = threadIdx.x >> 6;")
+        w("  constexpr int fmr_cs = 64, fmr_rs = %d;" % (TB_THREADS // 64))
+        w("#endif")
         w("  for (int tile = blockIdx.x; tile < %d; tile += gridDim.x) {" % P.ntiles)
         w("    int rest = tile;")
         for a in reversed(range(1, d)):
