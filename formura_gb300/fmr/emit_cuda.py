@@ -117,7 +117,7 @@ class LevelEmitter:
 
     def _emit_ops(self, which, alias: Dict[int, str], w, ind: str, pfx: str = "a",
                   lane: str = "", ext_prep: Optional[Dict[int, str]] = None,
-                  load_state=None) -> Dict[int, str]:
+                  load_state=None, load_array=None) -> Dict[int, str]:
         """C statements for the micro ops in `which` (topological order), one
         `const` temporary <pfx><i> each; an op in `alias` is bound to that C
         expression (a value carried from the previous cell, or the other cell
@@ -151,8 +151,9 @@ class LevelEmitter:
                 w(ind + "const %s %s = %s;" % (t, name, src))
             elif k == "loadM":
                 arr = self.mmp.arrays[m.args[1]]
-                w(ind + "const %s %s = r_%s[%s];" % (t, name, arr.name,
-                                                    self.idx_expr(m.args[0], lane)))
+                src = (load_array(m.args[1], m.args[0]) if load_array is not None else
+                       "r_%s[%s]" % (arr.name, self.idx_expr(m.args[0], lane)))
+                w(ind + "const %s %s = %s;" % (t, name, src))
             elif k == "index":
                 w(ind + "const %s %s = (%s)%s;" % (t, name, t, _wrap_name(m.args[0], 0, lane)))
             elif k == "uni":
@@ -553,73 +554,137 @@ TB_THREADS = 1024
 
 
 def tb_eligible(mmp: MM.MMProgram) -> bool:
-    """A program can be temporally blocked here when its step is one level
-    that reads only the state (no other manifest array) and writes exactly
-    the next value of every state variable, on 2 or 3 axes: then T steps are
-    the level applied T times."""
-    if mmp.dim not in (2, 3) or len(mmp.levels) != 1:
+    """A program can be temporally blocked here when it has 2 or 3 axes and
+    every state variable has exactly one store (its next value): then T steps
+    are the step's levels applied T times, each (step, level) a stage of the
+    blocked kernel's pipeline."""
+    if mmp.dim not in (2, 3) or not mmp.levels:
         return False
-    L = mmp.levels[0]
-    if L.reads_arrays:
-        return False
-    stores = [a.store_of for a in L.arrays]
-    return None not in stores and sorted(stores) == sorted(n for n, _ in mmp.state)
+    stores = [a.store_of for L in mmp.levels for a in L.arrays if a.store_of is not None]
+    return sorted(stores) == sorted(n for n, _ in mmp.state)
 
 
 class TBPlan:
-    """Geometry of the blocked kernel.
+    """Geometry of the blocked kernel over the stages (t, k) = (time step t of
+    the pass, level k of the step), stage index g = t * K + k.
 
-    * R[a]: stencil reach per axis (largest |cursor| of a state read).
-    * H[a]: halo per side on the plane axes, T * R[a]; with TMA staging the
-      fastest axis's halo is rounded up to a 16-byte multiple of elements.
-    * TI[a], RG[a] = TI[a] + 2 H[a]: the plane tile's interior and region,
-      sized to the shared-memory budget.
-    * Rings: level 0 keeps NS0 = NS + PD planes (PD planes prefetched by TMA),
-      levels 1..T-1 keep NS = 2 R[0] + 2 planes each; every ring plane takes PS
-      elements (the region, padded to 128 bytes).
-    * XC: planes along axis 0 per tile (chunk).
-    * tma: whether tiles away from the periodic boundary stage their input
-      planes with TMA (3 axes, 4- or 8-byte state, 16-byte aligned rows)."""
+    * A ring is one array's recent planes in shared memory: ("in", state) for
+      the pass's input state, (g, node) for array `node` produced by stage g
+      and read by a later stage (a manifest intermediate of the same step, or
+      a store that becomes the state of the next step).  A state read in step
+      t is the ring of its store in step t-1 (the input ring when t = 0).
+    * lag[g]: stage g evaluates plane i - lag[g] at iteration i; it reads ring
+      planes within its x-reach R0 of that plane, all written in earlier
+      iterations (lag[g] >= lag[producer] + R0 + 1), so one barrier per
+      iteration orders every stage.
+    * Margins, from the end backwards: a stage whose arrays are the final
+      stores (step T-1) is computed on the interior; a producer on its
+      readers' boxes widened by their reach.  m[g][a] along each axis (axis 0:
+      planes before and after the chunk), H[a] = the input ring's margin (the
+      halo; along the fastest axis rounded up to 16 bytes for TMA).
+    * NS[ring] = planes a ring keeps: the span of its readers' planes; the
+      input ring keeps PD more (planes brought ahead of their first use).
+    * TI, RG = TI + 2 H: the plane tile's interior and region, sized to the
+      shared-memory budget; PS = ring plane stride (region padded to 128 B).
+    * XC: planes along axis 0 per tile; tma: whether tiles away from the
+      periodic boundary load the input planes with TMA."""
 
     def __init__(self, mmp: MM.MMProgram, T: int, budget: int = TB_SMEM_BUDGET,
                  sms: int = 152, tma: bool = True):
-        L = mmp.levels[0]
         d = mmp.dim
         self.T, self.dim, self.shape = T, d, list(mmp.shape)
-        R = [0] * d
-        for _, cur in L.reads_state:
-            for a, c in enumerate(cur):
-                R[a] = max(R[a], abs(c))
-        self.R = R
-        self.NS = 2 * R[0] + 2
-        self.read = sorted({n for n, _ in L.reads_state})
+        levels = mmp.levels
+        K = len(levels)
+        self.K = K
+        self.nstage = T * K
         stype = dict(mmp.state)
         size = {"double": 8, "float": 4, "int": 4, "bool": 1}
+        level_of = {a.node: k for k, L in enumerate(levels) for a in L.arrays}
+        store_of = {a.store_of: (k, a.node) for k, L in enumerate(levels) for a in L.arrays
+                    if a.store_of is not None}
+        self.elem = {}  # ring -> C type
+        # reads[g] = {ring: (reach per axis)} and the ring of each (kind, key) read
+        self.reads = []
+        self.src = []  # per stage: {("S", name) or ("M", node): ring}
+        for g in range(self.nstage):
+            t, k = divmod(g, K)
+            L = levels[k]
+            rmap, reach = {}, {}
+            for name, cur in L.reads_state:
+                ring = ("in", name) if t == 0 else (g - K + store_of[name][0] - k, store_of[name][1])
+                rmap[("S", name)] = ring
+                self.elem[ring] = stype[name]
+                r = reach.setdefault(ring, [0] * d)
+                for a, c in enumerate(cur):
+                    r[a] = max(r[a], abs(c))
+            for node, cur in L.reads_arrays:
+                ring = (t * K + level_of[node], node)
+                rmap[("M", node)] = ring
+                self.elem[ring] = mmp.arrays[node].ctype
+                r = reach.setdefault(ring, [0] * d)
+                for a, c in enumerate(cur):
+                    r[a] = max(r[a], abs(c))
+            self.src.append(rmap)
+            self.reads.append(reach)
+        # lags, forwards
+        lag = [0] * self.nstage
+        for g in range(self.nstage):
+            lag[g] = max([0] + [(0 if ring[0] == "in" else lag[ring[0]]) + r[0] + 1
+                                for ring, r in self.reads[g].items()])
+        self.lag = lag
+        # margins, backwards
+        final = {g for g in range(self.nstage)
+                 if g // K == T - 1 and any(a.store_of for a in levels[g % K].arrays)}
+        m = [[None] * d for _ in range(self.nstage)]
+        for g in final:
+            m[g] = [0] * d
+        min_in = [0] * d
+        for g in reversed(range(self.nstage)):
+            if m[g][0] is None:
+                m[g] = [0] * d  # an array no later stage reads (not expected)
+            for ring, r in self.reads[g].items():
+                need = [m[g][a] + r[a] for a in range(d)]
+                if ring[0] == "in":
+                    min_in = [max(x, y) for x, y in zip(min_in, need)]
+                else:
+                    p = ring[0]
+                    m[p] = [need[a] if m[p][a] is None else max(m[p][a], need[a]) for a in range(d)]
+        self.m = m
+        self.min_in = min_in
+        self.read = sorted({ring[1] for reach in self.reads for ring in reach if ring[0] == "in"})
         self.sizes = {n: size[stype[n]] for n in self.read}
         sz = list(self.sizes.values()) or [8]
         A = max(16 // s for s in sz) if all(s in (4, 8) for s in sz) else 0
         self.tma = bool(tma and d == 3 and A and self.shape[2] % A == 0)
         self.A = A if self.tma else 1
         self.PD = 2  # planes brought ahead of their first use (TMA or cp.async)
-        self.NS0 = self.NS + self.PD
-        slots = self.NS0 + (T - 1) * self.NS
-        H = [0] + [T * R[a] for a in range(1, d)]
+        # ring planes kept
+        span = {}
+        for g in range(self.nstage):
+            for ring, r in self.reads[g].items():
+                pl = 0 if ring[0] == "in" else lag[ring[0]]
+                span[ring] = max(span.get(ring, 0), lag[g] - pl + r[0] + 1)
+        # the input rings share one plane count (one slot index and one mbarrier per plane)
+        ns_in = max([n for ring, n in span.items() if ring[0] == "in"] or [0]) + self.PD
+        self.NS = {ring: (ns_in if ring[0] == "in" else n) for ring, n in span.items()}
+        self.rings = sorted(self.NS, key=lambda r: (-1, r[1]) if r[0] == "in" else (r[0], r[1]))
+        H = [min_in[0]] + [min_in[a] for a in range(1, d)]
         if self.tma:
             H[2] = -(-H[2] // A) * A
+        self.H = H
+        bytes_per_pos = sum(size[self.elem[r]] * self.NS[r] for r in self.rings)
         TI = [0] * d
-        per_pos = sum(self.sizes.values()) * slots
         if d == 3:
             TI[2] = min(self.shape[2], max(8, 64 - 2 * H[2]))
             if self.tma and TI[2] < self.shape[2]:
                 TI[2] = max(A, TI[2] // A * A)
             rg2 = TI[2] + 2 * H[2]
-            rg1 = budget // max(1, per_pos * rg2)
+            rg1 = budget // max(1, bytes_per_pos * rg2)
             TI[1] = min(self.shape[1], rg1 - 2 * H[1])
             if self.tma:
                 TI[1] = min(TI[1], 256 - 2 * H[1])  # a TMA box edge is at most 256
         else:
-            TI[1] = min(self.shape[1], budget // max(1, per_pos) - 2 * H[1], 4096)
-        self.H = H
+            TI[1] = min(self.shape[1], budget // max(1, bytes_per_pos) - 2 * H[1], 4096)
         self.ok = all(TI[a] >= 1 for a in range(1, d))
         while True:
             self.TI = TI
@@ -628,7 +693,7 @@ class TBPlan:
             for a in range(1, d):
                 self.plane *= self.RG[a]
             self.PS = -(-self.plane // 32) * 32
-            self.smem = sum(self.sizes.values()) * slots * self.PS
+            self.smem = bytes_per_pos * self.PS
             if not self.ok or self.smem <= budget or TI[1] <= 1:
                 break
             TI = list(TI)
@@ -638,12 +703,17 @@ class TBPlan:
             self.tma = False
         self.NT = [0] + [(self.shape[a] + self.TI[a] - 1) // self.TI[a] if self.ok else 1
                          for a in range(1, d)]
+        self.offset = {}
+        off = 0
+        for r in self.rings:
+            self.offset[r] = off
+            off += size[self.elem[r]] * self.NS[r] * self.PS
         nyz = 1
         for a in range(1, d):
             nyz *= self.NT[a]
         # planes per tile: the chunk that minimises waves x (chunk + pipeline fill) over
         # one resident CTA per SM (the rings take most of an SM's shared memory)
-        fill = T * (2 * R[0] + 1)
+        fill = max(lag[g] for g in final) + 2 * H[0] - 1 if final else 0  # iterations - chunk
         n0 = self.shape[0]
         best, self.XC = None, n0
         for cand in range(1, n0 + 1):
@@ -653,73 +723,66 @@ class TBPlan:
                 best, self.XC = cost, cand
         self.nchunk = (n0 + self.XC - 1) // self.XC
         self.ntiles = self.nchunk * nyz
-
-    def ring_base(self, level: int) -> int:
-        """First element of `level`'s ring within a state's rings."""
-        return 0 if level == 0 else (self.NS0 + (level - 1) * self.NS) * self.PS
-
-    def ring_slots(self, level: int) -> int:
-        return self.NS0 if level == 0 else self.NS
+        self.final = sorted(final)
 
 
 class TBEmitter(LevelEmitter):
-    """Kernel ``fmr_level_tb``: T steps of the program's one level per pass
-    over the state.  A CTA owns a plane tile (axes 1..d-1, region = interior
-    plus the halo of T steps) and marches along axis 0 over a chunk of planes.
-    Each time level s = 0..T-1 keeps a ring of planes of the region in shared
-    memory; at iteration i level 0 brings plane i, and level s = 1..T
-    evaluates plane i - s (R0 + 1) on the cells it must provide (within
-    (T - s) R[a] of the interior) from level s-1's planes within R0 of it,
-    all of which were written in earlier iterations, so one __syncthreads per
-    iteration orders every level.  Level T writes the tile's interior.  Each
-    cell evaluates the level's operations in the per-step kernel's order on
-    the same values, so the results equal T steps of that kernel bit for bit
-    (the reference's temporal blocking unrolls the step graph the same way,
-    src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134).
+    """Kernel ``fmr_level_tb``: T steps of the program per pass over the state.
+    A CTA owns a plane tile (axes 1..d-1, region = interior plus the halo of T
+    steps) and marches along axis 0 over a chunk of planes.  Every stage (a
+    level of one of the T steps) evaluates, at iteration i, its plane
+    i - lag on the cells it must provide, reading the rings of the arrays it
+    needs (planes written in earlier iterations, so one __syncthreads per
+    iteration orders every stage) and writing its own arrays' rings; the
+    final step's stores go to the output arrays on the tile's interior.  Each
+    cell evaluates a level's operations in the per-step kernel's order on the
+    same values, so the results equal T steps of the per-step kernels bit for
+    bit (the reference's temporal blocking unrolls the step graph the same
+    way, src/Formura/OrthotopeMachine/TemporalBlocking.hs:49-134).
 
-    Level 0: a tile whose region lies inside the array (no periodic wrap)
-    receives each input plane by one TMA copy per state array
+    Input planes: a tile whose region lies inside the array (no periodic
+    wrap) receives each input plane by one TMA copy per state array
     (cp.async.bulk.tensor, issued by one thread PD planes ahead, completing on
     the slot's mbarrier; every wait is bounded and a wait that gives up sets
     the error word); tiles at the periodic boundary gather the plane with
-    wrapped indices."""
+    wrapped indices by per-thread cp.async, also PD planes ahead."""
 
     def __init__(self, mmp, plan: TBPlan, soft_div=True, soft_mul=True, soft_cmp=True):
         super().__init__(mmp, mmp.levels[0], 0, soft_div, soft_mul, soft_cmp)
         self.plan = plan
 
     def emit(self) -> Tuple[str, List[str], List[MM.Array]]:
-        L, P = self.level, self.plan
-        d, T, R, RG, TI, H = P.dim, P.T, P.R, P.RG, P.TI, P.H
+        P = self.plan
+        d, T, K, RG, TI, H = P.dim, P.T, P.K, P.RG, P.TI, P.H
         stypes = dict(self.mmp.state)
-        state_names = sorted({n for n, _ in L.reads_state})
+        state_names = list(P.read)
+        outputs = [a for g in P.final for a in self.mmp.levels[g % K].arrays if a.store_of]
         params = ["const %s *__restrict__ s_%s" % (stypes[n], n) for n in state_names]
-        params += ["%s *__restrict__ w_%s" % (a.ctype, a.name) for a in L.arrays]
+        params += ["%s *__restrict__ w_%s" % (a.ctype, a.name) for a in outputs]
         params += ["FMR_TMAP tm_%s" % n for n in state_names]
         params += ["int use_tma", "int *__restrict__ fmr_err"]
         plane, PS = P.plane, P.PS
+        NS0 = P.NS[("in", state_names[0])] if state_names else 1
         out: List[str] = []
         w = out.append
         n0 = self.shape[0]
-        i0 = "(x0 - %d)" % (T * R[0])  # relative plane index k = i - i0
+        i0 = "(x0 - %d)" % H[0]  # relative plane index k = i - i0
         w("#ifdef FMR_HOST_BUILD")
         w("static unsigned char fmr_tb_smem[%d];" % max(16, P.smem))
         w("#endif")
         w("__global__ void __launch_bounds__(%d, 1) fmr_level_tb(%s) {" % (TB_THREADS, ", ".join(params)))
         w("#ifndef FMR_HOST_BUILD")
         w("  extern __shared__ __align__(128) unsigned char fmr_tb_smem[];")
-        w("  __shared__ __align__(8) uint64_t fmr_bar[%d];" % max(1, P.NS0))
+        w("  __shared__ __align__(8) uint64_t fmr_bar[%d];" % max(1, NS0))
         w("  __shared__ int fmr_fail;")
         w("#endif")
-        off = 0
-        for n in state_names:
-            w("  %s *const m_%s = (%s *)(fmr_tb_smem + %d);  // rings: level 0, then levels 1..T-1"
-              % (stypes[n], n, stypes[n], off))
-            off += P.sizes[n] * (P.NS0 + (T - 1) * P.NS) * PS
+        rname = {}
+        for r in P.rings:
+            nm = "m_%s" % r[1] if r[0] == "in" else "m%d_%d" % (r[0], r[1])
+            rname[r] = nm
+            w("  %s *const %s = (%s *)(fmr_tb_smem + %d);  // ring of %d planes"
+              % (P.elem[r], nm, P.elem[r], P.offset[r], P.NS[r]))
         tx_bytes = sum(P.sizes[n] for n in state_names) * plane
-        w("#ifndef FMR_HOST_BUILD")
-        w("  if (threadIdx.x == 0) fmr_fail = 0;")
-        w("#endif")
         w("#ifdef FMR_HOST_BUILD")
         w("  const int fmr_tx = threadIdx.x % 64, fmr_ty = threadIdx.x / 64;")
         w("  const int fmr_cs = blockDim.x < 64 ? blockDim.x : 64;")
@@ -727,6 +790,7 @@ class TBEmitter(LevelEmitter):
         w("#else  // the launch's block: %d threads, 64 along the fastest axis" % TB_THREADS)
         w("  const int fmr_tx = threadIdx.x & 63, fmr_ty = threadIdx.x >> 6;")
         w("  constexpr int fmr_cs = 64, fmr_rs = %d;" % (TB_THREADS // 64))
+        w("  if (threadIdx.x == 0) fmr_fail = 0;")
         w("#endif")
         w("  for (int tile = blockIdx.x; tile < %d; tile += gridDim.x) {" % P.ntiles)
         w("    int rest = tile;")
@@ -736,15 +800,14 @@ class TBEmitter(LevelEmitter):
             w("    rest /= %d;" % P.NT[a])
         w("    const int x0 = rest * %d;" % P.XC)
         w("    const int x1 = x0 + %d < %d ? x0 + %d : %d;" % (P.XC, n0, P.XC, n0))
-        w("    const int kend = x1 + %d - %s;  // planes level 0 brings: k in [0, kend)"
-          % (T * R[0], i0))
-        gx_of = lambda kk: "(((x0 - %d + (%s)) %% %d) + %d) %% %d" % (T * R[0], kk, n0, n0, n0)
+        w("    const int kend = x1 + %d - %s;  // input planes: k in [0, kend)" % (H[0], i0))
+        gx_of = lambda kk: "(((x0 - %d + (%s)) %% %d) + %d) %% %d" % (H[0], kk, n0, n0, n0)
 
         def gather(kk: str, ind: str, asynchronous: bool):
-            """Plane kk (relative) of every state into its level-0 slot, wrapped."""
+            """Input plane kk (relative) of every state into its slot, wrapped."""
             w(ind + "{")
             w(ind + "  const int gx = %s;" % gx_of(kk))
-            w(ind + "  const int sl = (%s) %% %d;" % (kk, P.NS0))
+            w(ind + "  const int sl = (%s) %% %d;" % (kk, NS0))
             w(ind + "  for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % plane)
             if d == 3:
                 w(ind + "    const int j1 = q / %d, j2 = q %% %d;" % (RG[2], RG[2]))
@@ -757,10 +820,10 @@ class TBEmitter(LevelEmitter):
                 gi = "(%s * %d + g%d)" % (gi, self.shape[a], a)
             for n in state_names:
                 if asynchronous:
-                    w(ind + "    fmr_cp_async%d(m_%s + sl * %d + q, s_%s + %s);" %
-                      (P.sizes[n], n, PS, n, gi))
+                    w(ind + "    fmr_cp_async%d(%s + sl * %d + q, s_%s + %s);" %
+                      (P.sizes[n], rname[("in", n)], PS, n, gi))
                 else:
-                    w(ind + "    m_%s[sl * %d + q] = s_%s[%s];" % (n, PS, n, gi))
+                    w(ind + "    %s[sl * %d + q] = s_%s[%s];" % (rname[("in", n)], PS, n, gi))
             w(ind + "  }")
             w(ind + "}")
 
@@ -771,7 +834,7 @@ class TBEmitter(LevelEmitter):
             w("    const bool tma = use_tma && %s;" % conds)
             w("    if (tma) {")
             w("      if (threadIdx.x == 0) {")
-            w("        for (int b = 0; b < %d; ++b) fm::tc::mbar_init(&fmr_bar[b], 1);" % P.NS0)
+            w("        for (int b = 0; b < %d; ++b) fm::tc::mbar_init(&fmr_bar[b], 1);" % NS0)
             w('        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");')
             w("        fm::tc::fence_proxy_async_smem();")
             w("      }")
@@ -790,7 +853,8 @@ class TBEmitter(LevelEmitter):
         w("      }")
         w("    }")
         w("#endif")
-        w("    for (int i = x0 - %d; i < x1 + %d; ++i) {" % (T * R[0], T * (R[0] + 1)))
+        last = max(P.lag[g] for g in P.final)
+        w("    for (int i = x0 - %d; i < x1 + %d; ++i) {" % (H[0], last))
         w("      const int k = i - %s;" % i0)
         w("#ifdef FMR_HOST_BUILD")
         w("      if (k < kend)")
@@ -799,10 +863,10 @@ class TBEmitter(LevelEmitter):
         w("      if (tma) {")
         if P.tma:
             w("        if (threadIdx.x == 0 && k + %d < kend) fmr_tb_issue(k + %d);" % (P.PD, P.PD))
-            w("        // level 1 reads up to plane i - 1: wait for its copy (once per plane)")
+            w("        // the first reader of input plane k - 1 runs in this iteration: wait for it")
             w("        if (k >= 1 && k - 1 < kend && !fmr_fail &&")
             w("            !fm::tc::mbar_wait(&fmr_bar[(k - 1) %% %d], ((k - 1) / %d) & 1)) {"
-              % (P.NS0, P.NS0))
+              % (NS0, NS0))
             w("          fmr_fail = 1;")
             w("          atomicExch(fmr_err, 1);")
             w("        }")
@@ -812,39 +876,47 @@ class TBEmitter(LevelEmitter):
         w("        fmr_cp_async_commit();")
         w("      }")
         w("#endif")
-        has_index = {m.args[0] for m in L.micro if m.kind == "index"}
-        lag = R[0] + 1
-        for s_ in range(1, T + 1):
-            lo = [0] + [H[a] - (T - s_) * R[a] for a in range(1, d)]
-            vext = [0] + [TI[a] + 2 * (T - s_) * R[a] for a in range(1, d)]
-            cnt = 1
-            for a in range(1, d):
-                cnt *= vext[a]
-            w("      {  // level %d: plane i - %d" % (s_, s_ * lag))
-            w("        const int kq = k - %d;  // its relative plane index" % (s_ * lag))
-            w("        if (kq >= %d && kq < kend - %d) {" % (s_ * R[0], s_ * R[0]))
-            w("          const int p = i - %d;" % (s_ * lag))
-            base_in = P.ring_base(s_ - 1)
-            ns_in = P.ring_slots(s_ - 1)
+
+        def pidx(js):
+            return "(%s) * %d + (%s)" % (js[1], RG[2], js[2]) if d == 3 else js[1]
+
+        for g in range(P.nstage):
+            t, kl = divmod(g, K)
+            L = self.mmp.levels[kl]
+            self.level = L
+            lo = [0] + [H[a] - P.m[g][a] for a in range(1, d)]
+            hi = [0] + [H[a] + TI[a] + P.m[g][a] for a in range(1, d)]
+            xs = H[0] - P.m[g][0]
+            w("      {  // stage %d: step %d, level %d: plane i - %d" % (g, t, kl, P.lag[g]))
+            w("        const int kq = k - %d;  // its relative plane index" % P.lag[g])
+            w("        if (kq >= %d && kq < kend - %d) {" % (xs, xs))
+            w("          const int p = i - %d;" % P.lag[g])
             slots = {}
-            for c0 in range(-R[0], R[0] + 1):
-                v = "sl%s%d" % ("m" if c0 < 0 else "p", abs(c0))
-                slots[c0] = v
-                w("          const int %s = (kq %+d) %% %d;" % (v, c0, ns_in))
-            if s_ < T:
-                w("          const int so = kq %% %d;" % P.NS)
+            for ring, r in P.reads[g].items():
+                for c0 in range(-r[0], r[0] + 1):
+                    v = "sl%d_%s%d" % (len(slots), "m" if c0 < 0 else "p", abs(c0))
+                    slots[(ring, c0)] = v
+                    w("          const int %s = (kq %+d) %% %d;" % (v, c0, P.NS[ring]))
+            own = [a for a in L.arrays if (g, a.node) in P.NS]
+            if own:
+                w("          const int so = kq %% %d;" % min(P.NS[(g, a.node)] for a in own))
+                ns_own = {a.node: P.NS[(g, a.node)] for a in own}
+                for a in own:
+                    w("          const int so_%d = kq %% %d;" % (a.node, ns_own[a.node]))
+            has_index = {mi.args[0] for mi in L.micro if mi.kind == "index"}
             if 0 in has_index:
                 w("          const int c0 = ((p %% %d) + %d) %% %d;" % (n0, n0, n0))
             if d == 3 and RG[2] <= 64:
-                # 64 threads along the fastest axis (a warp reads whole row segments), the
-                # rest along the rows: no division per cell
-                w("          for (int j1 = %d + fmr_ty; j1 < %d; j1 += fmr_rs)" % (lo[1], lo[1] + vext[1]))
-                w("          for (int j2 = %d + fmr_tx; j2 < %d; j2 += fmr_cs) {" % (lo[2], lo[2] + vext[2]))
+                w("          for (int j1 = %d + fmr_ty; j1 < %d; j1 += fmr_rs)" % (lo[1], hi[1]))
+                w("          for (int j2 = %d + fmr_tx; j2 < %d; j2 += fmr_cs) {" % (lo[2], hi[2]))
             else:
+                cnt = 1
+                for a in range(1, d):
+                    cnt *= hi[a] - lo[a]
                 w("          for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % cnt)
                 if d == 3:
                     w("            const int j1 = %d + q / %d, j2 = %d + q %% %d;" %
-                      (lo[1], vext[2], lo[2], vext[2]))
+                      (lo[1], hi[2] - lo[2], lo[2], hi[2] - lo[2]))
                 else:
                     w("            const int j1 = %d + q;" % lo[1])
             for a in range(1, d):
@@ -852,31 +924,35 @@ class TBEmitter(LevelEmitter):
                     w("            const int c%d = (((o%d + j%d) %% %d) + %d) %% %d;" %
                       (a, a, a, self.shape[a], self.shape[a], self.shape[a]))
 
-            def pidx(js):
-                return "(%s) * %d + (%s)" % (js[1], RG[2], js[2]) if d == 3 else js[1]
-
-            def load(name, cur, _b=base_in, _sl=slots):
+            def ring_load(ring, cur, _sl=slots):
                 js = [None] + ["j%d%s" % (a, "" if cur[a] == 0 else "%+d" % cur[a])
                                for a in range(1, d)]
-                return "m_%s[%d + %s * %d + %s]" % (name, _b, _sl[cur[0]], PS, pidx(js))
+                return "%s[%s * %d + %s]" % (rname[ring], _sl[(ring, cur[0])], PS, pidx(js))
 
-            self._emit_ops(range(len(L.micro)), {}, w, "            ", load_state=load)
-            if s_ < T:
-                for arr in L.arrays:
-                    if arr.store_of in state_names:
-                        w("            m_%s[%d + so * %d + %s] = a%d;" %
-                          (arr.store_of, P.ring_base(s_), PS, pidx([None, "j1", "j2"]), arr.root))
-            else:
-                conds = ["p >= x0"]
+            src = P.src[g]
+            self._emit_ops(range(len(L.micro)), {}, w, "            ",
+                           load_state=lambda name, cur, _s=src: ring_load(_s[("S", name)], cur),
+                           load_array=lambda node, cur, _s=src: ring_load(_s[("M", node)], cur))
+            for a in own:
+                w("            %s[so_%d * %d + %s] = a%d;" %
+                  (rname[(g, a.node)], a.node, PS, pidx([None, "j1", "j2"]), a.root))
+            if g in P.final:
+                # the tile's interior only: the stage's box is wider when a later stage of the
+                # same step reads its other arrays
+                conds = ["p >= x0", "p < x1"]
                 gidx = "(size_t)p"
                 for a in range(1, d):
+                    if P.m[g][a]:
+                        conds.append("j%d >= %d && j%d < %d" % (a, H[a], a, H[a] + TI[a]))
                     conds.append("o%d + j%d < %d" % (a, a, self.shape[a]))
                     gidx = "(%s * %d + (o%d + j%d))" % (gidx, self.shape[a], a, a)
-                w("            if (%s) {" % " && ".join(conds))
-                w("              const size_t gi = %s;" % gidx)
-                for arr in L.arrays:
-                    w("              w_%s[gi] = a%d;" % (arr.name, arr.root))
-                w("            }")
+                stores = [a for a in L.arrays if a.store_of]
+                if stores:
+                    w("            if (%s) {" % " && ".join(conds))
+                    w("              const size_t gi = %s;" % gidx)
+                    for a in stores:
+                        w("              w_%s[gi] = a%d;" % (a.name, a.root))
+                    w("            }")
             w("          }")
             w("        }")
             w("      }")
@@ -908,20 +984,20 @@ class TBEmitter(LevelEmitter):
                    "#endif", ""]
         src = "\n".join(helpers) + src
         if P.tma:
-            # the copy of relative plane k into its level-0 slot, one TMA box per state array
+            # the copy of relative input plane k into its slot, one TMA box per state array
             iss = ["#ifndef FMR_HOST_BUILD",
                    "#define fmr_tb_issue(KK) do { \\",
                    "    const int kk_ = (KK); \\",
                    "    const int gx_ = (((x0 - %d + kk_) %% %d) + %d) %% %d; \\"
-                   % (T * R[0], n0, n0, n0),
-                   "    uint64_t *bar_ = &fmr_bar[kk_ %% %d]; \\" % P.NS0,
+                   % (H[0], n0, n0, n0),
+                   "    uint64_t *bar_ = &fmr_bar[kk_ %% %d]; \\" % NS0,
                    "    fm::tc::mbar_arrive_expect_tx(bar_, %du); \\" % tx_bytes]
             for n in state_names:
-                iss.append("    fm::tc::tma_load_3d(m_%s + (kk_ %% %d) * %d, &tm_%s, o2, o1, gx_, bar_); \\"
-                           % (n, P.NS0, PS, n))
+                iss.append("    fm::tc::tma_load_3d(%s + (kk_ %% %d) * %d, &tm_%s, o2, o1, gx_, bar_); \\"
+                           % (rname[("in", n)], NS0, PS, n))
             iss += ["  } while (0)", "#endif", ""]
             src = "\n".join(iss) + src
-        return src, state_names, L.arrays
+        return src, state_names, outputs
 
 
 def emit_tb_kernel(mmp: MM.MMProgram, T: int, soft_div: bool = True, soft_mul: bool = True,
@@ -932,7 +1008,7 @@ def emit_tb_kernel(mmp: MM.MMProgram, T: int, soft_div: bool = True, soft_mul: b
     if T < 2 or not tb_eligible(mmp):
         return None
     plan = TBPlan(mmp, T, budget, tma=tma)
-    if not plan.ok:
+    if not plan.ok or not plan.read:
         return None
     src, sn, aw = TBEmitter(mmp, plan, soft_div, soft_mul, soft_cmp).emit()
     return src, plan, sn, aw

@@ -203,3 +203,32 @@ class HostKernels:
         a, lo, hi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self.lib.fmr_host_store_counts(ctypes.byref(a), ctypes.byref(lo), ctypes.byref(hi))
         return a.value, lo.value, hi.value
+
+
+def asan_run(mmp, steps: int, tb: int = 1, tb_budget: int = 0):
+    """Build the host kernels of `mmp` with AddressSanitizer into a standalone
+    program, run `steps` steps on a fixed state, and return (exit status,
+    sanitizer report).  Any access outside an array or outside the blocked
+    kernel's shared-memory stand-in is reported, so a schedule that would read
+    or write out of bounds on the GPU fails here, on the CPU."""
+    src = host_source(mmp, tb=tb, tb_budget=tb_budget)
+    n = int(np.prod(mmp.shape))
+    lines = [src, "#include <stdio.h>", "int main() {"]
+    for j, (_, t) in enumerate(mmp.state):
+        lines.append("  static %s b%d[%d];" % (t, j, n))
+        lines.append("  for (int i = 0; i < %d; ++i) b%d[i] = (%s)(0.3 + 0.001 * (i %% 97));" % (n, j, t))
+    lines.append("  void *st[%d] = {%s};" % (len(mmp.state), ", ".join("b%d" % j for j in range(len(mmp.state)))))
+    lines.append("  return fmr_host_run(%d, st);" % steps)
+    lines.append("}")
+    key = hashlib.sha256(("\n".join(lines) + (CSRC / "fm_softfp.cuh").read_text()).encode())
+    BUILD.mkdir(parents=True, exist_ok=True)
+    exe = BUILD / ("asan_%s" % key.hexdigest()[:16])
+    if not exe.exists():
+        cpp = exe.with_suffix(".cpp")
+        cpp.write_text("\n".join(lines) + "\n")
+        tmp = Path(str(exe) + ".tmp")
+        subprocess.run(["g++", "-std=c++17", "-O0", "-g", "-fsanitize=address", "-ffp-contract=off",
+                        "-w", "-I", str(CSRC), "-o", str(tmp), str(cpp), "-lm"], check=True)
+        tmp.replace(exe)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    return r.returncode, r.stderr

@@ -155,6 +155,9 @@ TB_CASES = [
     ("diffusion-2d.fmr", [40, 64]), ("diffusion-2d.fmr", [7, 300]),
     ("fmr-libm.fmr", [13, 17]), ("gray-scott-3d-float.fmr", [1, 4, 3]),
     ("heat-3d-float.fmr", [10, 40, 72]), ("heat-3d-float.fmr", [3, 5, 9]),
+    # several levels per step (manifest intermediates read by later levels)
+    ("fmr-limiter.fmr", [24, 40]), ("fmr-limiter.fmr", [9, 17]), ("fmr-features.fmr", [13, 33]),
+    ("fmr-3d-advection.fmr", [8, 12, 20]), ("fmr-3d-advection.fmr", [5, 3, 33]),
 ]
 
 
@@ -183,10 +186,15 @@ def test_blocked_kernel_matches_c_oracle(fmr, shape, tb, budget):
 def test_blocked_kernel_writes_every_cell_once_per_pass(fmr, shape):
     p = load_program(EX / fmr, intra_node_shape=shape)
     mmp = p.compiled()
-    hk = HostKernels(mmp, tb=3, tb_budget=24000, count_stores=True) if _fits(mmp, 3, 24000) \
-        else HostKernels(mmp, tb=3, count_stores=True)
+    if _fits(mmp, 3, 24000):
+        hk = HostKernels(mmp, tb=3, tb_budget=24000, count_stores=True)
+    elif _fits(mmp, 3, 200 * 1024):
+        hk = HostKernels(mmp, tb=3, count_stores=True)
+    else:
+        pytest.skip("no tile fits in shared memory")
     hk.run(_state(p, 3), 3)  # one pass
-    assert hk.store_counts() == (len(mmp.arrays), 1, 1)
+    # the state arrays only: intermediate arrays live in the shared-memory rings
+    assert hk.store_counts() == (len([a for a in mmp.arrays.values() if a.store_of]), 1, 1)
 
 
 def _fits(mmp, tb, budget):
@@ -196,14 +204,14 @@ def _fits(mmp, tb, budget):
 
 
 def test_which_programs_are_blocked():
-    """Single-level programs (the step reads only the state and writes every
-    state's next value) are blocked; programs with manifest intermediate
-    arrays keep one launch per step, as does a halo that leaves no tile."""
+    """Programs on 2 or 3 axes whose states each have one store are blocked,
+    single-level or not; 1D programs keep one launch per step, as does a
+    halo that leaves no tile in shared memory."""
     from formura_gb300 import backend
     from formura_gb300.fmr.emit_cuda import tb_eligible
 
     assert tb_eligible(load_program(EX / "gray-scott-3d-float.fmr").compiled())
-    assert not tb_eligible(load_program(EX / "fmr-limiter.fmr").compiled())
+    assert tb_eligible(load_program(EX / "fmr-limiter.fmr").compiled())
     assert not tb_eligible(load_program(EX / "fmr-1d-float.fmr").compiled())
     p = load_program(EX / "gray-scott-3d-float.fmr")
     assert p.temporal_blocking_interval == 4 and backend.blocked_kernel(p) is not None
@@ -240,3 +248,47 @@ def test_blocked_kernel_tma_geometry():
     # 2D programs gather every plane
     p = load_program(EX / "diffusion-2d.fmr", intra_node_shape=[64, 256])
     assert not emit_tb_kernel(p.compiled(), 4)[1].tma
+
+
+ASAN_CASES = [("fmr-limiter.fmr", [24, 40], 2, 0), ("fmr-features.fmr", [13, 33], 3, 0),
+              ("fmr-3d-advection.fmr", [8, 12, 20], 2, 0), ("heat-3d-float.fmr", [6, 20, 40], 4, 48000),
+              ("gray-scott-3d.fmr", [5, 7, 33], 2, 0), ("diffusion-2d.fmr", [7, 300], 3, 0)]
+
+
+@pytest.mark.parametrize("fmr,shape,tb,budget", ASAN_CASES)
+def test_blocked_kernel_in_bounds_under_address_sanitizer(fmr, shape, tb, budget):
+    """Every array and shared-memory access of the blocked kernel stays in
+    bounds (AddressSanitizer build of the host kernels), for single- and
+    multi-level programs, ragged tiles and small tile budgets."""
+    from fmr_host import asan_run
+
+    p = load_program(EX / fmr, intra_node_shape=shape)
+    status, report = asan_run(p.compiled(), 2 * tb + 1, tb=tb, tb_budget=budget)
+    assert status == 0 and "AddressSanitizer" not in report, report[:2000]
+
+
+@pytest.mark.skipif(not (REF / "examples" / "pearson-2d.fmr").exists(), reason="reference tree absent")
+@pytest.mark.parametrize("name", ["pearson-2d.fmr", "pearson.fmr", "lotka-volterra.fmr", "move.fmr"])
+def test_blocked_kernel_reference_examples(name):
+    """The reference's multi-level example programs through the blocked
+    kernel (3 steps per pass) on the host: bit for bit the C oracle, and in
+    bounds under AddressSanitizer."""
+    from formura_gb300.fmr import compile_source
+    from formura_gb300.fmr import parser as P
+    from formura_gb300.fmr.emit_cuda import emit_tb_kernel
+    from fmr_host import asan_run
+
+    src = (REF / "examples" / name).read_text()
+    shape = [12, 20, 16][:P.parse(src).dimension]
+    mmp = compile_source(src, tuple(shape))
+    if emit_tb_kernel(mmp, 3) is None:
+        pytest.skip("not blocked")
+    o = fmr_c.FmrOracle(src, shape)
+    rng = np.random.default_rng(0)
+    s0 = {n: rng.random(shape) * 0.1 for n, _ in o.mmp.state}
+    got = HostKernels(mmp, tb=3).run(s0, 7)
+    want = o.run(s0, 7)
+    for n in want:
+        assert np.array_equal(got[n].view(np.uint8), want[n].view(np.uint8)), n
+    status, report = asan_run(mmp, 7, tb=3)
+    assert status == 0 and "AddressSanitizer" not in report, report[:2000]

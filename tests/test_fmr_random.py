@@ -146,3 +146,21 @@ def test_random_program_blocked_kernel_matches_c_oracle(seed):
         for name in s0:
             assert np.array_equal(got[name].view(np.uint8), want[name].view(np.uint8)), \
                 (name, budget, src)
+
+
+@pytest.mark.parametrize("seed", blocked_cases(12)[:6])
+def test_random_program_blocked_kernel_in_bounds(seed):
+    """The blocked kernels of random programs access nothing out of bounds
+    (AddressSanitizer build of the host kernels, small tiles)."""
+    from fmr_host import asan_run
+
+    from formura_gb300.fmr.emit_cuda import emit_tb_kernel
+
+    src, shape, _, _, float_q = case(seed)
+    tb = 2 + seed % 3
+    mmp = compile_source(src, shape)
+    budget = next((b for b in (48000, 200 * 1024) if emit_tb_kernel(mmp, tb, budget=b)), None)
+    if budget is None:
+        pytest.skip("no tile fits in shared memory")
+    status, report = asan_run(mmp, 2 * tb + 1, tb=tb, tb_budget=budget)
+    assert status == 0 and "AddressSanitizer" not in report, report[:2000]

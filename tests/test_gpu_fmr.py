@@ -75,6 +75,11 @@ def _random_state(prog, rng):
     ("heat-3d-float.fmr", dict(intra_node_shape=[20, 100, 192], monitor_interval=8)),
     ("heat-3d-float.fmr", dict(intra_node_shape=[7, 9, 20], monitor_interval=12,
                                temporal_blocking_interval=3)),
+    # blocked programs of several levels per step (manifest intermediates in rings)
+    ("fmr-limiter.fmr", dict(monitor_interval=4, temporal_blocking_interval=2, tb_kernel=1)),
+    ("fmr-features.fmr", dict(monitor_interval=6, temporal_blocking_interval=3, tb_kernel=1)),
+    ("fmr-3d-advection.fmr", dict(intra_node_shape=[16, 40, 128], monitor_interval=4,
+                                  temporal_blocking_interval=2, tb_kernel=1)),
 ])
 def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     p = load_program(EX / fmr, **kw)
