@@ -713,7 +713,8 @@ class TBPlan:
             nyz *= self.NT[a]
         # planes per tile: the chunk that minimises waves x (chunk + pipeline fill) over
         # one resident CTA per SM (the rings take most of an SM's shared memory)
-        fill = max(lag[g] for g in final) + 2 * H[0] - 1 if final else 0  # iterations - chunk
+        # iterations per tile = chunk + input halo H[0] + the final stages' lag
+        fill = max(lag[g] for g in final) + H[0] if final else 0
         n0 = self.shape[0]
         best, self.XC = None, n0
         for cand in range(1, n0 + 1):
