@@ -790,7 +790,7 @@ def run_profile_case(args):
         prog.advance(1)
         prog.download()
         prog.finalize()
-    elif args.profile in ("fmr_gs3d_float_tb", "fmr_heat_float_tb"):
+    elif args.profile in ("fmr_gs3d_float_tb", "fmr_heat_float_tb", "fmr_heat_float"):
         # examples/gray-scott-3d-float.fmr or heat-3d-float.fmr through the front end,
         # blocked kernel (temporal_blocking_interval 4): `profile_steps` steps at n^3
         import numpy as np
@@ -799,9 +799,10 @@ def run_profile_case(args):
         from formura_gb300.runtime import load_program as load_lib
 
         src = "gray-scott-3d-float" if args.profile == "fmr_gs3d_float_tb" else "heat-3d-float"
+        tbk = -1 if args.profile == "fmr_heat_float" else 1  # one step per launch, or blocked
         p = load_program(ROOT / "examples" / (src + ".fmr"), intra_node_shape=[n, n, n],
-                         monitor_interval=args.profile_steps, tb_kernel=1,
-                         name="fmr_%s_prof" % src.replace("-", "_"))
+                         monitor_interval=args.profile_steps, tb_kernel=tbk,
+                         name="fmr_%s_prof%d" % (src.replace("-", "_"), tbk + 1))
         prog = load_lib(p)
         prog.init()
         U0, V0 = inits.gray_scott_3d(n, n, n, seed=1)
@@ -847,7 +848,8 @@ def main():
                     help="skip the other forms (FP32 TB, ensemble, diffusion, MHD)")
     ap.add_argument("--profile", choices=["gs3d_f64", "gs3d_f32k", "gs3d_f32k_tb", "ensemble",
                                           "mhd", "mhd_f64", "diff2d", "surrogate", "fmr_gs3d",
-                                          "fmr_gs3d_float_tb", "fmr_heat_float_tb"],
+                                          "fmr_gs3d_float_tb", "fmr_heat_float_tb",
+                                          "fmr_heat_float"],
                     default=None,
                     help="run a small case of one kernel for an ncu capture, then exit")
     ap.add_argument("--profile-n", type=int, default=256)
