@@ -456,6 +456,9 @@ class LevelEmitter:
              lambda: {i: "a%d" % j for i, j in from_a_all.items()})
         w("    }")
         # the rest of the chunk
+        # unrolled so that the loads of several cells are in flight together (the loop is
+        # bound by load latency otherwise: float heat-3d at 256^3, long-scoreboard stalls)
+        w("#pragma unroll 4")
         w("    for (int c0 = x0 + 1; c0 < x1; ++c0) {")
         w("      const size_t idx = (size_t)c0 * %dull + (size_t)col;" % ncol)
         self._wrap_lines(w, "      ", {0})
