@@ -456,9 +456,14 @@ class LevelEmitter:
              lambda: {i: "a%d" % j for i, j in from_a_all.items()})
         w("    }")
         # the rest of the chunk
-        # unrolled so that the loads of several cells are in flight together (the loop is
-        # bound by load latency otherwise: float heat-3d at 256^3, long-scoreboard stalls)
-        w("#pragma unroll 4")
+        # A light cell (at most 16 arithmetic operations) is bound by load latency: unrolled
+        # by 4, the loads of several cells are in flight together (float heat-3d at 256^3:
+        # 273 -> 402 GLUP/s).  Heavier cells are bound by arithmetic and lose occupancy to
+        # the unrolled registers (gray-scott-3d: 17.4 -> 13.6), so they keep one cell.
+        arith = sum(1 for i in need if i not in carried and
+                    L.micro[i].kind in ("bin", "uni", "nary", "ite"))
+        if arith <= 16:
+            w("#pragma unroll 4")
         w("    for (int c0 = x0 + 1; c0 < x1; ++c0) {")
         w("      const size_t idx = (size_t)c0 * %dull + (size_t)col;" % ncol)
         self._wrap_lines(w, "      ", {0})
