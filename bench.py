@@ -440,8 +440,8 @@ def run_generated_blocked_variant(torch, U0, V0, hbm):
             res[label] = round(N ** 3 * p.steps_per_forward / sec / 1e9, 2)
             if plan is not None:
                 pl = plan[1]
-                res["tile"] = {"interior": pl.TI[1:], "region": pl.RG[1:], "x_chunk": pl.XC,
-                               "tiles": pl.ntiles, "smem_bytes": pl.smem, "tma": pl.tma}
+                res["tile"] = {"interior": pl.TI[1:], "region": pl.RG[1:], "planes_per_block": pl.XC,
+                               "column_planes": pl.ntiles, "smem_bytes": pl.smem, "tma": pl.tma}
             prog.finalize()
         out[prog_name] = {
             "value": res["blocked"], "unit": "GLUP/s", "steps": 2000, "tb": 4,

@@ -719,19 +719,12 @@ class TBPlan:
         nyz = 1
         for a in range(1, d):
             nyz *= self.NT[a]
-        # planes per tile: the chunk that minimises waves x (chunk + pipeline fill) over
-        # one resident CTA per SM (the rings take most of an SM's shared memory)
-        # iterations per tile = chunk + input halo H[0] + the final stages' lag
-        fill = max(lag[g] for g in final) + H[0] if final else 0
+        # the kernel splits the nyz * n0 column-planes into one contiguous run per CTA;
+        # XC is the run's length (planes per CTA)
         n0 = self.shape[0]
-        best, self.XC = None, n0
-        for cand in range(1, n0 + 1):
-            tiles = nyz * ((n0 + cand - 1) // cand)
-            cost = ((tiles + sms - 1) // sms) * (cand + fill)
-            if best is None or cost < best:
-                best, self.XC = cost, cand
-        self.nchunk = (n0 + self.XC - 1) // self.XC
-        self.ntiles = self.nchunk * nyz
+        self.ntiles = nyz * n0
+        self.XC = -(-self.ntiles // sms)
+        self.nchunk = -(-n0 // self.XC)
         self.final = sorted(final)
 
 
@@ -801,14 +794,20 @@ class TBEmitter(LevelEmitter):
         w("  constexpr int fmr_cs = 64, fmr_rs = %d;" % (TB_THREADS // 64))
         w("  if (threadIdx.x == 0) fmr_fail = 0;")
         w("#endif")
-        w("  for (int tile = blockIdx.x; tile < %d; tile += gridDim.x) {" % P.ntiles)
-        w("    int rest = tile;")
+        # The nyz * n0 column-planes are split into gridDim.x contiguous runs; a CTA marches
+        # its run, refilling the pipeline only where the run crosses into the next column.
+        w("  const long long fmr_total = %dll;" % P.ntiles)
+        w("  int fmr_q = (int)(fmr_total * blockIdx.x / gridDim.x);")
+        w("  const int fmr_qend = (int)(fmr_total * (blockIdx.x + 1) / gridDim.x);")
+        w("  while (fmr_q < fmr_qend) {")
+        w("    int rest = fmr_q / %d;  // the (y, z) column" % n0)
+        w("    const int x0 = fmr_q - rest * %d;" % n0)
+        w("    const int x1 = x0 + (fmr_qend - fmr_q) < %d ? x0 + (fmr_qend - fmr_q) : %d;" % (n0, n0))
+        w("    fmr_q += x1 - x0;")
         for a in reversed(range(1, d)):
             w("    const int o%d = (rest %% %d) * %d - %d;  // region origin along axis %d"
               % (a, P.NT[a], TI[a], H[a], a))
             w("    rest /= %d;" % P.NT[a])
-        w("    const int x0 = rest * %d;" % P.XC)
-        w("    const int x1 = x0 + %d < %d ? x0 + %d : %d;" % (P.XC, n0, P.XC, n0))
         w("    const int kend = x1 + %d - %s;  // input planes: k in [0, kend)" % (H[0], i0))
         gx_of = lambda kk: "(((x0 - %d + (%s)) %% %d) + %d) %% %d" % (H[0], kk, n0, n0, n0)
 
@@ -917,7 +916,11 @@ class TBEmitter(LevelEmitter):
                 w("          const int c0 = ((p %% %d) + %d) %% %d;" % (n0, n0, n0))
             if d == 3 and RG[2] <= 64:
                 w("          for (int j1 = %d + fmr_ty; j1 < %d; j1 += fmr_rs)" % (lo[1], hi[1]))
+                w("#ifdef FMR_HOST_BUILD")
                 w("          for (int j2 = %d + fmr_tx; j2 < %d; j2 += fmr_cs) {" % (lo[2], hi[2]))
+                w("#else  // at most 64 columns: one per thread")
+                w("          if (const int j2 = %d + fmr_tx; j2 < %d) {" % (lo[2], hi[2]))
+                w("#endif")
             else:
                 cnt = 1
                 for a in range(1, d):

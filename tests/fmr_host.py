@@ -44,8 +44,9 @@ PRELUDE = r"""
 #define FMR_TMAP const void *
 namespace {
 struct FmHostDim { unsigned x, y, z; };
-const FmHostDim blockIdx = {0u, 0u, 0u}, threadIdx = {0u, 0u, 0u};
-const FmHostDim gridDim = {1u, 1u, 1u}, blockDim = {1u, 1u, 1u};
+// blockIdx and gridDim change only for the blocked kernel, whose blocks run one after another
+FmHostDim blockIdx = {0u, 0u, 0u}, gridDim = {1u, 1u, 1u};
+const FmHostDim threadIdx = {0u, 0u, 0u}, blockDim = {1u, 1u, 1u};
 }  // namespace
 """
 
@@ -80,14 +81,16 @@ extern "C" void fmr_host_store_counts(int *arrays, int *lo, int *hi) {
 
 
 def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = True,
-                count_stores: bool = False, tb: int = 1, tb_budget: int = 0) -> str:
+                count_stores: bool = False, tb: int = 1, tb_budget: int = 0, tb_grid: int = 5) -> str:
     """Host C++ of the generated kernels plus a step loop; `soft` False emits
     the plain IEEE operations instead of the integer-pipe forms.  With
     `count_stores` every store of a kernel also counts, per array and cell, how
     often it was written (read back by fmr_host_store_counts).  With tb >= 2
     the temporally blocked kernel runs tb steps per pass (the rest of the
     steps one per pass), as the generated host code does; `tb_budget` > 0
-    shrinks its shared-memory budget (smaller tiles, more of them)."""
+    shrinks its shared-memory budget (smaller tiles, more of them), and its
+    `tb_grid` blocks run one after another, each marching its own contiguous
+    run of column-planes (runs that start and end inside a column)."""
     kern, levels = emit_kernels(mmp, soft_div=soft, soft_mul=soft, soft_cmp=soft,
                                 march_chunk=march_chunk, march_pair=march_pair)
     tbk = None
@@ -136,7 +139,10 @@ def host_source(mmp, march_chunk: int = 0, march_pair: int = 0, soft: bool = Tru
         args += ["nullptr"] * len(sn_tb) + ["0", "&host_err"]  # no TMA on the host
         w("  int host_err = 0;")
         w("  for (; t + %d <= steps; t += %d) {" % (plan.T, plan.T))
-        w("    fmr_level_tb(%s);" % ", ".join(args))
+        w("    gridDim.x = %du;" % tb_grid)
+        w("    for (unsigned b = 0; b < %du; ++b) { blockIdx.x = b; fmr_level_tb(%s); }"
+          % (tb_grid, ", ".join(args)))
+        w("    gridDim.x = 1u; blockIdx.x = 0u;")
         w("    for (int i = 0; i < %d; ++i) { void *x = cur[i]; cur[i] = nxt[i]; nxt[i] = x; }"
           % len(states))
         w("  }")
