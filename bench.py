@@ -410,7 +410,8 @@ def run_generated_blocked_variant(torch, U0, V0, hbm):
     the two.  examples/heat-3d-float.fmr is memory-bound (every operation a
     float one); examples/gray-scott-3d-float.fmr divides by dx = 0.01, a
     double constant, as the reference's generated C does, so it stays bound
-    by the FP64 pipe and blocking cannot pay there."""
+    by the FP64 pipe and blocking cannot pay there: by default (tb_kernel 0)
+    only the light one is blocked."""
     import numpy as np
 
     from formura_gb300 import backend
@@ -451,6 +452,10 @@ def run_generated_blocked_variant(torch, U0, V0, hbm):
             "hbm_roofline_per_step_glups": round(hbm / bytes_per_cell, 1),
             "hbm_roofline_at_tb_glups": round(hbm / (bytes_per_cell / 4), 1),
             "tile": res.get("tile"),
+            # the kernel a program gets by default (tb_kernel 0): blocked only when light
+            "default_kernel": ("blocked" if backend.blocked_kernel(
+                load_program(ROOT / "examples" / (prog_name + ".fmr"))) is not None
+                else "per_step"),
             "kernel": "fmr_level_tb (generated, 4 steps per pass) vs fmr_level_0"}
     return out
 

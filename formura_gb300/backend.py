@@ -80,8 +80,9 @@ class Program:
     # and an even extent of axis 1; measured slower on gray-scott-3d), 0 or 1 = one cell
     march_pair: int = 0
     # form "fmr": the temporally blocked kernel (temporal_blocking_interval steps per pass,
-    # emit_cuda.TBEmitter) for single-level programs: 0 = when its plane region (tile plus
-    # halo) holds at most twice the cells it writes, 1 = whenever the program allows it,
+    # emit_cuda.TBEmitter): 0 = when the step is light and binary32 (emit_cuda.tb_profitable)
+    # and its plane region (tile plus halo) holds at most twice the cells it writes,
+    # 1 = whenever the program allows it,
     # -1 = never (one step per launch; temporal_blocking_interval then only rounds M)
     tb_kernel: int = 0
 
@@ -295,7 +296,7 @@ def blocked_kernel(p: Program):
     """The temporally blocked kernel of a form-"fmr" program, as
     emit_cuda.emit_tb_kernel returns it, when the program takes one (see
     Program.tb_kernel), else None."""
-    from .fmr.emit_cuda import emit_tb_kernel
+    from .fmr.emit_cuda import emit_tb_kernel, tb_profitable
 
     T = int(p.temporal_blocking_interval)
     if p.form != "fmr" or p.tb_kernel < 0 or T < 2:
@@ -308,7 +309,8 @@ def blocked_kernel(p: Program):
     for a in range(1, plan.dim):
         cells *= plan.RG[a]
         tile *= plan.TI[a]
-    if p.tb_kernel == 0 and cells > 2 * tile:  # the halo would double the work per plane
+    if p.tb_kernel == 0 and (cells > 2 * tile  # the halo would double the work per plane
+                             or not tb_profitable(p.compiled())):
         return None
     return r
 

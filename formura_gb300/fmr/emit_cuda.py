@@ -462,7 +462,7 @@ class LevelEmitter:
         # the unrolled registers (gray-scott-3d: 17.4 -> 13.6), so they keep one cell.
         arith = sum(1 for i in need if i not in carried and
                     L.micro[i].kind in ("bin", "uni", "nary", "ite"))
-        if arith <= 16:
+        if arith <= LIGHT_ARITH:
             w("#pragma unroll 4")
         w("    for (int c0 = x0 + 1; c0 < x1; ++c0) {")
         w("      const size_t idx = (size_t)c0 * %dull + (size_t)col;" % ncol)
@@ -556,6 +556,28 @@ class LevelEmitter:
 
 # ---------------------------------------------------------------------------
 # Temporal blocking of single-level programs
+
+LIGHT_ARITH = 16  # arithmetic operations of a light level (bound by loads, not arithmetic)
+
+
+def arith_ops(level) -> int:
+    """Arithmetic operations of one level's cell (binary, unary, n-ary, select)."""
+    return sum(1 for mi in level.micro if mi.kind in ("bin", "uni", "nary", "ite"))
+
+
+def tb_profitable(mmp: MM.MMProgram) -> bool:
+    """Whether blocking pays off: the program is binary32 throughout and light
+    (at most 24 arithmetic operations per cell and step), so one step per pass
+    is bound by memory traffic, which blocking divides by T.  A heavier or
+    binary64 step is bound by arithmetic already (binary64 runs on the slow
+    FP64 or integer pipes), and T unrolled copies of a heavy step outgrow the
+    instruction cache: float gray-scott-3d at 256^3 ran 6 GLUP/s blocked against
+    16.4 one step per pass, float heat-3d 476 against 403."""
+    if any(t != "float" for _, t in mmp.state):
+        return False
+    if any(a.ctype != "float" for a in mmp.arrays.values()):
+        return False
+    return sum(arith_ops(L) for L in mmp.levels) <= 24
 
 TB_SMEM_BUDGET = 200 * 1024  # bytes of shared memory a blocked kernel may take
 TB_THREADS = 1024
@@ -707,6 +729,22 @@ class TBPlan:
             TI = list(TI)
             TI[1] -= 1
         self.ok = self.ok and self.smem <= budget
+        if self.ok:
+            # balanced edges: the same number of tiles along each axis, none of them mostly
+            # outside the array (a tile costs its whole region however little of it is written)
+            TI = list(TI)
+            for a in range(1, d):
+                ti = -(-self.shape[a] // -(-self.shape[a] // TI[a]))
+                if self.tma and a == 2:
+                    ti = -(-ti // A) * A
+                TI[a] = min(TI[a], ti)
+            self.TI = TI
+            self.RG = [0] + [TI[a] + 2 * H[a] for a in range(1, d)]
+            self.plane = 1
+            for a in range(1, d):
+                self.plane *= self.RG[a]
+            self.PS = -(-self.plane // 32) * 32
+            self.smem = bytes_per_pos * self.PS
         if self.tma and self.ok and (self.RG[1] > 256 or self.RG[2] > 256):
             self.tma = False
         self.NT = [0] + [(self.shape[a] + self.TI[a] - 1) // self.TI[a] if self.ok else 1
@@ -811,11 +849,48 @@ class TBEmitter(LevelEmitter):
         w("    const int kend = x1 + %d - %s;  // input planes: k in [0, kend)" % (H[0], i0))
         gx_of = lambda kk: "(((x0 - %d + (%s)) %% %d) + %d) %% %d" % (H[0], kk, n0, n0, n0)
 
+        nq = -(-plane // TB_THREADS)  # gathered cells per thread and plane (device build)
+        pstride = 1
+        for a in range(1, d):
+            pstride *= self.shape[a]
+        w("#ifndef FMR_HOST_BUILD")
+        w("    // in-plane offsets of this thread's gathered cells (wrapped), fixed for the piece")
+        w("    int fmr_go[%d];" % nq)
+        w("#pragma unroll")
+        w("    for (int r = 0; r < %d; ++r) {" % nq)
+        w("      const int q = threadIdx.x + r * %d;" % TB_THREADS)
+        if d == 3:
+            w("      const int j1 = q / %d, j2 = q %% %d;" % (RG[2], RG[2]))
+        else:
+            w("      const int j1 = q;")
+        go = "0"
+        for a in range(1, d):
+            w("      const int g%d = (((o%d + j%d) %% %d) + %d) %% %d;" %
+              (a, a, a, self.shape[a], self.shape[a], self.shape[a]))
+            go = "(%s * %d + g%d)" % (go, self.shape[a], a)
+        w("      fmr_go[r] = %s;" % go)
+        w("    }")
+        w("#endif")
+
         def gather(kk: str, ind: str, asynchronous: bool):
             """Input plane kk (relative) of every state into its slot, wrapped."""
             w(ind + "{")
             w(ind + "  const int gx = %s;" % gx_of(kk))
             w(ind + "  const int sl = (%s) %% %d;" % (kk, NS0))
+            if asynchronous:  # device build: the offsets computed for the piece
+                w(ind + "  const size_t gb = (size_t)gx * %d;" % pstride)
+                w("#pragma unroll")
+                w(ind + "  for (int r = 0; r < %d; ++r) {" % nq)
+                w(ind + "    const int q = threadIdx.x + r * %d;" % TB_THREADS)
+                w(ind + "    if (r + 1 < %d || q < %d) {  // only the last round can run past the plane"
+                  % (nq, plane))
+                for n in state_names:
+                    w(ind + "      fmr_cp_async%d(%s + sl * %d + q, s_%s + gb + fmr_go[r]);" %
+                      (P.sizes[n], rname[("in", n)], PS, n))
+                w(ind + "    }")
+                w(ind + "  }")
+                w(ind + "}")
+                return
             w(ind + "  for (int q = threadIdx.x; q < %d; q += blockDim.x) {" % plane)
             if d == 3:
                 w(ind + "    const int j1 = q / %d, j2 = q %% %d;" % (RG[2], RG[2]))
@@ -915,11 +990,19 @@ class TBEmitter(LevelEmitter):
             if 0 in has_index:
                 w("          const int c0 = ((p %% %d) + %d) %% %d;" % (n0, n0, n0))
             if d == 3 and RG[2] <= 64:
-                w("          for (int j1 = %d + fmr_ty; j1 < %d; j1 += fmr_rs)" % (lo[1], hi[1]))
                 w("#ifdef FMR_HOST_BUILD")
+                w("          for (int j1 = %d + fmr_ty; j1 < %d; j1 += fmr_rs)" % (lo[1], hi[1]))
                 w("          for (int j2 = %d + fmr_tx; j2 < %d; j2 += fmr_cs) {" % (lo[2], hi[2]))
                 w("#else  // at most 64 columns: one per thread")
-                w("          if (const int j2 = %d + fmr_tx; j2 < %d) {" % (lo[2], hi[2]))
+                if arith_ops(L) <= LIGHT_ARITH:
+                    w("#pragma unroll  // a light cell: the loads of its rows in flight together")
+                else:
+                    w("#pragma unroll 1  // a heavy cell: one copy of its code")
+                w("          for (int fmr_r = 0; fmr_r < %d; ++fmr_r)"
+                  % -(-(hi[1] - lo[1]) // (TB_THREADS // 64)))
+                w("          if (const int j1 = %d + fmr_ty + %d * fmr_r, j2 = %d + fmr_tx;"
+                  % (lo[1], TB_THREADS // 64, lo[2]))
+                w("              j1 < %d && j2 < %d) {" % (hi[1], hi[2]))
                 w("#endif")
             else:
                 cnt = 1

@@ -214,8 +214,13 @@ def test_which_programs_are_blocked():
     assert tb_eligible(load_program(EX / "fmr-limiter.fmr").compiled())
     assert not tb_eligible(load_program(EX / "fmr-1d-float.fmr").compiled())
     p = load_program(EX / "gray-scott-3d-float.fmr")
-    assert p.temporal_blocking_interval == 4 and backend.blocked_kernel(p) is not None
+    # by default a heavy step (56 arithmetic operations) stays one step per launch ...
+    assert p.temporal_blocking_interval == 4 and backend.blocked_kernel(p) is None
+    assert backend.blocked_kernel(load_program(EX / "gray-scott-3d-float.fmr", tb_kernel=1)) is not None
     assert backend.blocked_kernel(load_program(EX / "gray-scott-3d-float.fmr", tb_kernel=-1)) is None
+    # ... and a light binary32 one (13) is blocked
+    assert backend.blocked_kernel(load_program(EX / "heat-3d-float.fmr")) is not None
+    assert backend.blocked_kernel(load_program(EX / "heat-3d-float.fmr", tb_kernel=-1)) is None
     assert backend.blocked_kernel(load_program(EX / "gray-scott-3d.fmr")) is None  # interval 1
     # FP64 with 8 steps per pass: the halo of 8 leaves no tile in shared memory
     assert backend.blocked_kernel(load_program(EX / "gray-scott-3d.fmr",
