@@ -282,7 +282,9 @@ def run_variants(torch, prog, U_fp64_final, U0, V0, peaks):
         "hbm_roofline_at_tb_glups": round(hbm / (32.0 / tune["tb"]), 1),
         "frac_of_hbm_roofline_at_tb": round(g / (hbm / (32.0 / tune["tb"])), 3),
         "kernel": ["gs3d_f32k_tb (one row per warp)", "gs3d_f32k_tbr<4 rows, 8 warps>",
-                   "gs3d_f32k_tbr<2 rows, 16 warps>"][tune["kernel"]],
+                   "gs3d_f32k_tbr<2 rows, 16 warps>",
+                   "gs3d_f32k_tbp (one row per warp, (u, v) as packed binary32 pairs)"
+                   ][tune["kernel"]],
         "tuned": {"timings_s_per_step": tune["timings"]}}
     del U, V, cU, cV, w, Uw, Vw
     # -- uneven ensemble of 512 2D Gray-Scott instances, 5000 steps, one launch

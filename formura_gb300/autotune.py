@@ -117,7 +117,7 @@ def _apply_ensemble(res: dict) -> None:
 
 
 GS3D_F32K_CANDIDATES: Tuple[Tuple[int, int], ...] = tuple(
-    (kern, tb) for kern in (0, 1, 2) for tb in (1, 2, 3, 4))  # (gs3d_f32k.kernel, tb)
+    (kern, tb) for kern in (0, 1, 2, 3) for tb in (1, 2, 3, 4))  # (gs3d_f32k.kernel, tb)
 
 
 def tune_gs3d_f32k(n: Tuple[int, int, int] = (256, 256, 256), sample_steps: int = 24,

@@ -264,6 +264,146 @@ __global__ void __launch_bounds__(kE *kE, 1)
   }
 }
 
+// gs3d_f32k_tbp<T>: the 32x32-thread pipeline of gs3d_f32k_tb with U and V of
+// a cell held as one binary32 pair and advanced by packed FADD2/FMUL2/FFMA2
+// instructions (the fast form applies the same operation sequence to both
+// fields), so each packed instruction does the work of two scalar ones; the
+// shared-memory planes interleave (u, v) so that a y neighbour is one 64-bit
+// load.  Per cell and level: 11 packed operations for the two Laplacians,
+// 3 scalar products for u*v*v and its negation, 3 packed for the reaction
+// and 4 packed for the Kahan update, against 37 scalar operations.
+//
+// Equalities used (all exact in IEEE binary32, round to nearest even):
+//   (1 - u, -v)      = fma((-1, -1), (u, v), (1, -0))
+//   F(1-u) - uvv     = fma(F, 1-u, -uvv);   -Fk v + uvv = fma(Fk, -v, uvv)
+//   -(uv * v)        = uv * (-v)
+//   the Kahan compensation is carried negated between levels:
+//   -((t - u) - y)   = y - (t - u)   (rounding is symmetric under negation)
+// so the results equal gs3d_f32k_tb's and the oracle's bit for bit.
+template <int T>
+__global__ void __launch_bounds__(kE *kE, 1)
+    gs3d_f32k_tbp(const float *__restrict__ U, const float *__restrict__ V,
+                  const float *__restrict__ cU, const float *__restrict__ cV,
+                  float *__restrict__ Un, float *__restrict__ Vn, float *__restrict__ cUn,
+                  float *__restrict__ cVn, int nx, int ny, int nz, int xchunk, int nty,
+                  int ntz, int ntiles, Gs32f c) {
+  constexpr int O = kE - 2 * T;
+  // s_w[level][parity][row][lane] = (u, v); levels 0..T-1 feed levels 1..T
+  extern __shared__ float2 s_w[];
+  const int lane = threadIdx.x & 31;
+  const int row = threadIdx.x >> 5;
+  const size_t sx = (size_t)ny * nz;
+  const float2 kF = make_float2(c.F, c.Fk), kD = make_float2(c.cu, c.cv);
+  const float2 kDt = make_float2(c.dt, c.dt);
+  const float2 kM1 = make_float2(-1.0f, -1.0f), kOne = make_float2(1.0f, -0.0f);
+  Pieces pcs(nty * ntz, nx, xchunk);
+  int pc, x0, x1;
+  while (pcs.next(nty * ntz, nx, xchunk, ntiles, pc, x0, x1)) {
+    const int tz = pc % ntz;
+    const int ty = pc / ntz;
+    const int gy_out = ty * O + row - T;
+    const int gz_out = tz * O + lane - T;
+    const size_t col = (size_t)wrap_any(gy_out, ny) * nz + wrap_any(gz_out, nz);
+    const bool writer = row >= T && row < T + O && lane >= T && lane < T + O &&
+                        gy_out < ny && gz_out < nz;
+    float2 w[T][3];  // level s window of (u, v): planes (newest-2, newest-1, newest)
+    float2 nc[T];    // level s compensation at its newest plane, negated
+#pragma unroll
+    for (int s = 0; s < T; ++s) {
+      w[s][0] = w[s][1] = w[s][2] = make_float2(0.0f, 0.0f);
+      nc[s] = make_float2(0.0f, 0.0f);
+    }
+    constexpr int kPF = 2;
+    float pu[kPF], pv[kPF], pcu[kPF], pcv[kPF];
+#pragma unroll
+    for (int k = 0; k < kPF; ++k) {
+      const int ip = x0 - T + k;
+      const size_t g = (size_t)wrap_any(ip, nx) * sx + col;
+      pu[k] = __ldg(U + g);
+      pv[k] = __ldg(V + g);
+      pcu[k] = __ldg(cU + g);
+      pcv[k] = __ldg(cV + g);
+    }
+#pragma unroll 6
+    for (int i = x0 - T; i < x1 + T; ++i) {
+      const int par = i & 1;
+      const float2 in = make_float2(pu[0], pv[0]);
+      const float2 in_c = make_float2(pcu[0], pcv[0]);
+#pragma unroll
+      for (int k = 0; k + 1 < kPF; ++k) {
+        pu[k] = pu[k + 1];
+        pv[k] = pv[k + 1];
+        pcu[k] = pcu[k + 1];
+        pcv[k] = pcv[k + 1];
+      }
+      if (i + kPF < x1 + T) {
+        int ip = i + kPF;
+        if (nx >= 8)
+          ip = ip < 0 ? ip + nx : (ip >= nx ? ip - nx : ip);
+        else
+          ip = wrap_any(ip, nx);
+        const size_t g = (size_t)ip * sx + col;
+        pu[kPF - 1] = __ldg(U + g);
+        pv[kPF - 1] = __ldg(V + g);
+        pcu[kPF - 1] = __ldg(cU + g);
+        pcv[kPF - 1] = __ldg(cV + g);
+      }
+      w[0][0] = w[0][1];
+      w[0][1] = w[0][2];
+      w[0][2] = in;
+      s_w[((0 * 2 + par) * kE + row) * kE + lane] = in;
+      float2 carry = nc[0];  // level 0's negated compensation at plane i-1
+      nc[0] = fm::f2mul(in_c, kM1);
+#pragma unroll
+      for (int s = 1; s <= T; ++s) {
+        const float2 m = w[s - 1][1];
+        float2 zm, zp;
+        zm.x = __shfl_up_sync(0xffffffffu, m.x, 1);
+        zm.y = __shfl_up_sync(0xffffffffu, m.y, 1);
+        zp.x = __shfl_down_sync(0xffffffffu, m.x, 1);
+        zp.y = __shfl_down_sync(0xffffffffu, m.y, 1);
+        const float2 cin = carry;
+        if (row >= s && row < kE - s) {  // warp-uniform
+          const int base = ((s - 1) * 2 + (par ^ 1)) * kE;
+          const float2 ym = s_w[(base + row - 1) * kE + lane];
+          const float2 yp = s_w[(base + row + 1) * kE + lane];
+          using fm::f2add;
+          using fm::f2sub;
+          const float2 lx = f2sub(f2sub(w[s - 1][2], m), f2sub(m, w[s - 1][0]));
+          const float2 ly = f2sub(f2sub(yp, m), f2sub(m, ym));
+          const float2 lz = f2sub(f2sub(zp, m), f2sub(m, zm));
+          const float2 lap = f2add(f2add(lx, ly), lz);
+          const float uv = m.x * m.y;
+          const float2 nuvv = make_float2(uv * -m.y, uv * m.y);  // (-uvv, uvv)
+          const float2 wv = fm::f2fma(kM1, m, kOne);              // (1 - u, -v)
+          const float2 d = fm::f2fma(kD, lap, fm::f2fma(kF, wv, nuvv));
+          const float2 y = fm::f2fma(kDt, d, cin);
+          const float2 t = f2add(m, y);
+          const float2 ncn = f2sub(y, f2sub(t, m));
+          if (s < T) {
+            carry = nc[s];
+            nc[s] = ncn;
+            w[s][0] = w[s][1];
+            w[s][1] = w[s][2];
+            w[s][2] = t;
+            s_w[((s * 2 + par) * kE + row) * kE + lane] = t;
+          } else {
+            const int p = i - T;
+            if (writer && p >= x0) {
+              const size_t g = (size_t)p * sx + col;
+              Un[g] = t.x;
+              Vn[g] = t.y;
+              cUn[g] = -ncn.x;
+              cVn[g] = -ncn.y;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // gs3d_f32k_tbr<T, RY, W>: the same pipeline with register blocking along y
 // and each face difference computed once.
 //
@@ -490,17 +630,18 @@ int launch_tbr(int nx, int ny, int nz, const float *u, const float *v, const flo
 template <int T>
 int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const float *cu,
               const float *cv, float *un, float *vn, float *cun, float *cvn, const Gs32f &c,
-              cudaStream_t s) {
-  auto kern = gs3d_f32k_tb<T>;
+              bool packed, cudaStream_t s) {
+  auto kern = packed ? gs3d_f32k_tbp<T> : gs3d_f32k_tb<T>;
   constexpr int O = kE - 2 * T;
   const size_t smem = (size_t)2 * T * 2 * kE * kE * sizeof(float);
-  static bool attr_set[64] = {false};
+  static bool attr_set[2][64] = {};  // per kernel (scalar, packed) and device
+  bool *set = attr_set[packed ? 1 : 0];
   int dev = 0;
   FM_TRY_CUDA(cudaGetDevice(&dev));
-  if (dev < 64 && !attr_set[dev]) {
+  if (dev < 64 && !set[dev]) {
     FM_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
-    attr_set[dev] = true;
+    set[dev] = true;
   }
   int sms = 0;
   int st = fm::device_sm_count(&sms);
@@ -517,8 +658,8 @@ int launch_tb(int nx, int ny, int nz, const float *u, const float *v, const floa
     return FM_ERR_UNSUPPORTED;
   }
   const int grid = (int)std::min<long long>(ntiles, resident);
-  kern<<<grid, kE * kE, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz, xc,
-                                               nty, ntz, (int)ntiles, c);
+  kern<<<grid, kE * kE, smem, s>>>(u, v, cu, cv, un, vn, cun, cvn, nx, ny, nz, xc, nty, ntz,
+                                   (int)ntiles, c);
   FM_TRY_CUDA(cudaGetLastError());
   return FM_OK;
 }
@@ -547,9 +688,11 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   const size_t n = (size_t)nx * ny * nz;
   float *cur[4] = {U, V, cU, cV};
   float *nxt[4] = {work, work + n, work + 2 * n, work + 3 * n};
-  // 0: one row per warp (32x32 threads, the default: fastest measured); 1: the
-  // register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread, 16 warps
-  const int kern = fm::tune_get("gs3d_f32k.kernel", 0);
+  // 0: one row per warp (32x32 threads); 1: the
+  // register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread, 16 warps;
+  // 3: one row per warp with (u, v) advanced as packed binary32 pairs (the default: fastest
+  // measured, 250 against 238 GLUP/s at 256^3, tb 3)
+  const int kern = fm::tune_get("gs3d_f32k.kernel", 3);
   int done = 0;
   while (done < steps) {
     const int t = std::min(tb, steps - done);
@@ -569,8 +712,9 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
       done += t;
       continue;
     }
-#define FM_TB(TT) \
-  launch_tb<TT>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, s)
+#define FM_TB(TT)                                                                          \
+  launch_tb<TT>(nx, ny, nz, cur[0], cur[1], cur[2], cur[3], nxt[0], nxt[1], nxt[2], nxt[3], c, \
+                kern == 3, s)
     st = t == 1 ? FM_TB(1) : t == 2 ? FM_TB(2) : t == 3 ? FM_TB(3) : FM_TB(4);
 #undef FM_TB
     if (st) return st;

@@ -393,6 +393,9 @@ int fm_tensor_map_3d(void *map, const void *base, int elem_bytes, int n0, int n1
  *                      per SM; default) or 4 (2 CTAs per SM)
  *   "gs3d_f64.xchunk"  x planes per CTA tile (0 = automatic)
  *   "gs3d_f32k.tb"     default temporal-blocking depth of fm_gs3d_f32k_tb_forward (1..4)
+ *   "gs3d_f32k.kernel" form of fm_gs3d_f32k_tb_forward: 0 one row per warp, 1 and 2
+ *                      register-blocked (4 or 2 rows per thread), 3 one row per warp with
+ *                      (u, v) advanced as packed binary32 pairs (default)
  *   "gs3d_f32k.xchunk" x planes per tile of the temporally blocked kernel (0 = automatic)
  *   "gs2d_ens.tile"    default ensemble kernel: 1 wavefront strips (default), 32 or 64
  *                      shared-memory tiles of that edge

@@ -164,7 +164,7 @@ def test_gs3d_f32k_dag_bit_exact(cuda_device, shape, steps):
         assert np.array_equal(g, w)
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 2])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
 @pytest.mark.parametrize("tb", [1, 2, 3, 4])
 @pytest.mark.parametrize("shape,steps", [((32, 32, 32), 13), ((20, 24, 64), 8), ((7, 45, 33), 5),
                                          ((64, 64, 64), 12), ((9, 70, 100), 7), ((5, 3, 2), 6)])
@@ -190,7 +190,7 @@ def test_gs3d_f32k_tb_bit_exact(cuda_device, shape, steps, tb, kernel):
         assert np.array_equal(g, w)
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 2])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
 def test_gs3d_f32k_tb_xchunk_variants(cuda_device, kernel):
     lib = _lib.lib()
     U0, V0 = inits.gray_scott_3d(40, 32, 32, seed=9, ncubes=2, side=8)
