@@ -271,15 +271,15 @@ __global__ void __launch_bounds__(kE *kE, 1)
 // shared-memory planes interleave (u, v) so that a y neighbour is one 64-bit
 // load.  Per cell and level: 11 packed operations for the two Laplacians,
 // 3 scalar products for u*v*v and its negation, 3 packed for the reaction
-// and 4 packed for the Kahan update, against 37 scalar operations.
+// and 5 packed for the Kahan update, against 37 scalar operations.
 //
 // Equalities used (all exact in IEEE binary32, round to nearest even):
 //   (1 - u, -v)      = fma((-1, -1), (u, v), (1, -0))
 //   F(1-u) - uvv     = fma(F, 1-u, -uvv);   -Fk v + uvv = fma(Fk, -v, uvv)
 //   -(uv * v)        = uv * (-v)
-//   the Kahan compensation is carried negated between levels:
-//   -((t - u) - y)   = y - (t - u)   (rounding is symmetric under negation)
-// so the results equal gs3d_f32k_tb's and the oracle's bit for bit.
+//   -c               = c * (-1)      (the addend of the Kahan fma)
+// all exact including the signs of zeros, so the results (compensations
+// included) equal gs3d_f32k_tb's and the oracle's bit for bit.
 template <int T>
 __global__ void __launch_bounds__(kE *kE, 1)
     gs3d_f32k_tbp(const float *__restrict__ U, const float *__restrict__ V,
@@ -307,11 +307,11 @@ __global__ void __launch_bounds__(kE *kE, 1)
     const bool writer = row >= T && row < T + O && lane >= T && lane < T + O &&
                         gy_out < ny && gz_out < nz;
     float2 w[T][3];  // level s window of (u, v): planes (newest-2, newest-1, newest)
-    float2 nc[T];    // level s compensation at its newest plane, negated
+    float2 cc[T];    // level s compensation at its newest plane
 #pragma unroll
     for (int s = 0; s < T; ++s) {
       w[s][0] = w[s][1] = w[s][2] = make_float2(0.0f, 0.0f);
-      nc[s] = make_float2(0.0f, 0.0f);
+      cc[s] = make_float2(0.0f, 0.0f);
     }
     constexpr int kPF = 2;
     float pu[kPF], pv[kPF], pcu[kPF], pcv[kPF];
@@ -352,8 +352,8 @@ __global__ void __launch_bounds__(kE *kE, 1)
       w[0][1] = w[0][2];
       w[0][2] = in;
       s_w[((0 * 2 + par) * kE + row) * kE + lane] = in;
-      float2 carry = nc[0];  // level 0's negated compensation at plane i-1
-      nc[0] = fm::f2mul(in_c, kM1);
+      float2 carry = cc[0];  // level 0's compensation at plane i-1
+      cc[0] = in_c;
 #pragma unroll
       for (int s = 1; s <= T; ++s) {
         const float2 m = w[s - 1][1];
@@ -377,12 +377,12 @@ __global__ void __launch_bounds__(kE *kE, 1)
           const float2 nuvv = make_float2(uv * -m.y, uv * m.y);  // (-uvv, uvv)
           const float2 wv = fm::f2fma(kM1, m, kOne);              // (1 - u, -v)
           const float2 d = fm::f2fma(kD, lap, fm::f2fma(kF, wv, nuvv));
-          const float2 y = fm::f2fma(kDt, d, cin);
+          const float2 y = fm::f2fma(kDt, d, fm::f2mul(cin, kM1));
           const float2 t = f2add(m, y);
-          const float2 ncn = f2sub(y, f2sub(t, m));
+          const float2 cn = f2sub(f2sub(t, m), y);
           if (s < T) {
-            carry = nc[s];
-            nc[s] = ncn;
+            carry = cc[s];
+            cc[s] = cn;
             w[s][0] = w[s][1];
             w[s][1] = w[s][2];
             w[s][2] = t;
@@ -393,8 +393,8 @@ __global__ void __launch_bounds__(kE *kE, 1)
               const size_t g = (size_t)p * sx + col;
               Un[g] = t.x;
               Vn[g] = t.y;
-              cUn[g] = -ncn.x;
-              cVn[g] = -ncn.y;
+              cUn[g] = cn.x;
+              cVn[g] = cn.y;
             }
           }
         }
@@ -691,7 +691,7 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   // 0: one row per warp (32x32 threads); 1: the
   // register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread, 16 warps;
   // 3: one row per warp with (u, v) advanced as packed binary32 pairs (the default: fastest
-  // measured, 250 against 238 GLUP/s at 256^3, tb 3)
+  // measured, 247 against 238 GLUP/s at 256^3, tb 3)
   const int kern = fm::tune_get("gs3d_f32k.kernel", 3);
   int done = 0;
   while (done < steps) {
