@@ -184,12 +184,17 @@ def compare(got, want):
     (relative to |want| per cell, cells where want == 0 by absolute error)."""
     import numpy as np
 
-    got = np.asarray(got, dtype=np.float64)
-    want = np.asarray(want, dtype=np.float64)
+    got = np.ascontiguousarray(got)
+    want = np.ascontiguousarray(want, dtype=got.dtype)
+    # bit patterns of the state itself: +0 and -0 differ
+    ut = {4: np.uint32, 8: np.uint64}[got.dtype.itemsize]
+    same = bool(np.array_equal(got.view(ut), want.view(ut)))
+    got = got.astype(np.float64)
+    want = want.astype(np.float64)
     diff = np.abs(got - want)
     den = np.abs(want)
     rel = np.where(den > 0, diff / np.where(den > 0, den, 1.0), diff)
-    return {"bit_exact": bool(np.array_equal(got, want)),
+    return {"bit_exact": same,
             "max_rel_err": float(rel.max()) if rel.size else 0.0,
             "max_abs_err": float(diff.max()) if diff.size else 0.0}
 

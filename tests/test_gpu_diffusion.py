@@ -6,6 +6,7 @@ import torch
 from formura_gb300 import inits, kernels
 from formura_gb300.runtime import load_program
 from oracle import oracle
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -24,7 +25,7 @@ def test_diff2d_bit_exact(cuda_device, shape, steps):
     d0 = inits.diffusion_2d(*shape, seed=17)
     got = run(d0, steps, cuda_device)
     want = oracle.diff2d_f64(d0, steps, 0.4, 1.0)
-    assert np.array_equal(got, want)
+    assert same_bits(got, want)
 
 
 def test_diffusion_program_drop_in(cuda_device):
@@ -35,7 +36,7 @@ def test_diffusion_program_drop_in(cuda_device):
     prog.forward()
     assert prog.navi.time_step == 1000
     want = oracle.diff2d_f64(d0, 1000, 0.4, 1.0)
-    assert np.array_equal(prog.state["dens"], want)
+    assert same_bits(prog.state["dens"], want)
     tot = prog.conserved_totals()
     assert abs(tot[0] - d0.sum()) < 1e-9 * d0.sum()
 
@@ -57,6 +58,6 @@ def test_diffusion_temporal_blocking_bit_exact(cuda_device, tb, shape, steps):
         d = torch.from_numpy(d0).cuda()
         kernels.diff2d_f64_forward(d, torch.empty_like(d), 0.1, steps)
         want = oracle.diff2d_f64(d0, steps, Dt=0.1, Dx=1.0)
-        assert np.array_equal(d.cpu().numpy(), want)
+        assert same_bits(d.cpu().numpy(), want)
     finally:
         L.fm_tune_clear()

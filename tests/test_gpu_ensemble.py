@@ -8,6 +8,7 @@ import torch
 
 from formura_gb300 import inits, kernels
 from oracle import oracle
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -42,8 +43,8 @@ def test_ensemble_bit_exact(cuda_device, tile, tb):
     for i, n in enumerate(sizes):
         o = e.offsets[i]
         uo, vo = oracle_instance(U0[o:o + n * n], V0[o:o + n * n], n, F[i], k[i], steps)
-        assert np.array_equal(U[o:o + n * n].reshape(n, n), uo), (i, n)
-        assert np.array_equal(V[o:o + n * n].reshape(n, n), vo), (i, n)
+        assert same_bits(U[o:o + n * n].reshape(n, n), uo), (i, n)
+        assert same_bits(V[o:o + n * n].reshape(n, n), vo), (i, n)
     e.close()
 
 
@@ -55,7 +56,7 @@ def test_ensemble_graph_replay_matches(cuda_device):
     i = 3
     n, o = sizes[i], e1.offsets[i]
     uo, vo = oracle_instance(U0[o:o + n * n], V0[o:o + n * n], n, F[i], k[i], 80)
-    assert np.array_equal(Ub[o:o + n * n].reshape(n, n), uo)
+    assert same_bits(Ub[o:o + n * n].reshape(n, n), uo)
     e1.close()
     e2.close()
 
@@ -74,4 +75,4 @@ def test_single_instance_kernel_matches_oracle(cuda_device):
     kernels.gs2d_f32_forward(U, V, torch.empty_like(U), torch.empty_like(V),
                              kernels.gs_params(0.04, 0.06, DU, DV, DT, DX), 25)
     uo, vo = oracle.gs2d_f32(u0, v0, 25, 0.04, 0.06, DU, DV, DT, DX)
-    assert np.array_equal(U.cpu().numpy(), uo) and np.array_equal(V.cpu().numpy(), vo)
+    assert same_bits(U.cpu().numpy(), uo) and same_bits(V.cpu().numpy(), vo)

@@ -12,6 +12,7 @@ import torch
 from formura_gb300 import _lib, backend, inits, kernels
 from formura_gb300.runtime import FormuraProgram
 from oracle import oracle
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -33,7 +34,7 @@ def test_gs3d_f64_bit_exact(cuda_device, shape, steps):
     U0, V0 = inits.gray_scott_3d(*shape, seed=21, ncubes=3, side=8)
     U, V = run_f64(U0, V0, steps, cuda_device)
     Uo, Vo = oracle.gs3d_f64(U0, V0, steps, **GS)
-    assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
+    assert same_bits(U, Uo) and same_bits(V, Vo)
 
 
 @pytest.mark.parametrize("kernel,div,mul,xchunk,ry", [
@@ -53,7 +54,7 @@ def test_gs3d_f64_every_variant_bit_exact(cuda_device, kernel, div, mul, xchunk,
             U0, V0 = inits.gray_scott_3d(*shape, seed=31, ncubes=3, side=8)
             U, V = run_f64(U0, V0, steps, cuda_device)
             Uo, Vo = oracle.gs3d_f64(U0, V0, steps, **GS)
-            assert np.array_equal(U, Uo) and np.array_equal(V, Vo), (shape, kernel, div)
+            assert same_bits(U, Uo) and same_bits(V, Vo), (shape, kernel, div)
     finally:
         lib.fm_tune_clear()
 
@@ -77,7 +78,7 @@ def test_gs3d_f64_bit_exact_other_constants(cuda_device, arith):
     prm = dict(F=0.03, k=0.055, Du=1e-4, Dv=3e-5, dt=0.07, dx=0.0371)
     U, V = run_f64(U0, V0, 9, cuda_device, prm)
     Uo, Vo = oracle.gs3d_f64(U0, V0, 9, **prm)
-    assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
+    assert same_bits(U, Uo) and same_bits(V, Vo)
 
 
 def test_gs3d_f64_subnormal_front(cuda_device, arith):
@@ -88,7 +89,7 @@ def test_gs3d_f64_subnormal_front(cuda_device, arith):
     V0[2, 3, 5] = 0.25
     U, V = run_f64(U0, V0, 6, cuda_device)
     Uo, Vo = oracle.gs3d_f64(U0, V0, 6, **GS)
-    assert np.array_equal(U, Uo) and np.array_equal(V, Vo)
+    assert same_bits(U, Uo) and same_bits(V, Vo)
 
 
 def test_gs3d_f64_full_size_properties(cuda_device, arith):
@@ -106,7 +107,7 @@ def test_gs3d_f64_full_size_properties(cuda_device, arith):
     # grid for 2 steps is cheap enough
     Uo, Vo = oracle.gs3d_f64(U0, V0, 2, **GS)
     U2, V2 = run_f64(U0, V0, 2, cuda_device)
-    assert np.array_equal(U2, Uo) and np.array_equal(V2, Vo)
+    assert same_bits(U2, Uo) and same_bits(V2, Vo)
     one = np.ones((n, n, n))
     zero = np.zeros((n, n, n))
     u, v = run_f64(one, zero, 3, cuda_device)
@@ -125,7 +126,7 @@ def test_gs3d_program_forward_matches_oracle(cuda_device, tmp_path):
     prog.forward()
     assert prog.navi.time_step == 40
     Uo, Vo = oracle.gs3d_f64(U0, V0, 40, **GS)
-    assert np.array_equal(prog.state["U"], Uo) and np.array_equal(prog.state["V"], Vo)
+    assert same_bits(prog.state["U"], Uo) and same_bits(prog.state["V"], Vo)
     tot = prog.conserved_totals()
     np.testing.assert_allclose(tot, [Uo.sum(), Vo.sum()], rtol=1e-13)
     # resident path: upload once, advance twice, download
@@ -134,7 +135,7 @@ def test_gs3d_program_forward_matches_oracle(cuda_device, tmp_path):
     prog.download()
     assert prog.navi.time_step == 80
     Uo, Vo = oracle.gs3d_f64(Uo, Vo, 40, **GS)
-    assert np.array_equal(prog.state["U"], Uo)
+    assert same_bits(prog.state["U"], Uo)
     prog.finalize()
 
 
@@ -161,7 +162,7 @@ def test_gs3d_f32k_dag_bit_exact(cuda_device, shape, steps):
     Z = np.zeros(shape, np.float32)
     want = oracle.gs3d_f32_kahan(U0.astype(np.float32), V0.astype(np.float32), Z, Z, steps, **GS)
     for g, w in zip(got, want):
-        assert np.array_equal(g, w)
+        assert same_bits(g, w)
 
 
 @pytest.mark.parametrize("kernel", [0, 1, 2, 3])
@@ -187,7 +188,7 @@ def test_gs3d_f32k_tb_bit_exact(cuda_device, shape, steps, tb, kernel):
     want = oracle.gs3d_f32k_fast(U0.astype(np.float32), V0.astype(np.float32), cU0, cV0, steps,
                                  **GS)
     for g, w in zip(got, want):  # bit patterns: signed zeros of the compensations included
-        assert np.array_equal(g.view(np.uint32), np.asarray(w, np.float32).view(np.uint32))
+        assert same_bits(g, w)
 
 
 @pytest.mark.parametrize("kernel", [0, 1, 2, 3])
@@ -202,8 +203,7 @@ def test_gs3d_f32k_tb_xchunk_variants(cuda_device, kernel):
             lib.fm_tune_set(b"gs3d_f32k.xchunk", xc)
             got = run_f32k(U0, V0, 8, 4, cuda_device)
             for g, w in zip(got, want):
-                assert np.array_equal(g.view(np.uint32),
-                                      np.asarray(w, np.float32).view(np.uint32)), xc
+                assert same_bits(g, w), xc
     finally:
         lib.fm_tune_clear()
 

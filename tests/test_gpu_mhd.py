@@ -10,6 +10,7 @@ import torch
 
 from formura_gb300 import inits, kernels
 from oracle import oracle
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -29,7 +30,7 @@ def test_mhd_f64_bit_exact(cuda_device, n, steps):
     _, got = gpu_run(f0, steps, torch.float64)
     want = oracle.mhd_f64(f0, steps)
     for name, g, w in zip(inits.MHD_FIELDS, got, want):
-        assert np.array_equal(g, w), name
+        assert same_bits(g, w), name
 
 
 def test_mhd_f64_strong_perturbation_bit_exact(cuda_device):
@@ -46,7 +47,7 @@ def test_mhd_f64_strong_perturbation_bit_exact(cuda_device):
     assert all(np.isfinite(w).all() for w in want)
     assert (want[0] == -0.9).any(), "density floor not exercised"
     for name, g, w in zip(inits.MHD_FIELDS, got, want):
-        assert np.array_equal(g, w), name
+        assert same_bits(g, w), name
 
 
 def test_mhd_f64_signed_zeros_bit_exact(cuda_device):
