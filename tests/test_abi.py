@@ -8,6 +8,7 @@ import pytest
 
 from formura_gb300 import _lib, backend
 from formura_gb300.build import INCLUDE, LIB
+from tests.bits import same_bits
 
 DECL = re.compile(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(fm_\w+)\s*\(", re.M)
 
@@ -227,7 +228,7 @@ def test_reference_style_driver_runs_on_gpu(tmp_path, cuda_device, fmr):
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.split("\n")[:5] == ["t = %d" % t for t in (20, 40, 60, 80, 100)]
     got = np.fromfile(tmp_path / "out.bin", dtype=np.float64).reshape(64, 96)
-    assert np.array_equal(got, oracle.diff2d_f64(d0, 100, 0.4, 1.0))
+    assert same_bits(got, oracle.diff2d_f64(d0, 100, 0.4, 1.0))
 
 
 def test_reference_diffusion_driver_compiles_unmodified(tmp_path):

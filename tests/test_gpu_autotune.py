@@ -7,6 +7,7 @@ import torch
 
 from formura_gb300 import _lib, autotune, inits, kernels
 from oracle import oracle
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -41,7 +42,7 @@ def test_tune_ensemble_pick_runs_bit_exact_and_is_cached(cuda_device, private_ca
         o = int(e.offsets[i])
         uo, _ = oracle.gs2d_f32(U0[o:o + n * n].reshape(n, n), V0[o:o + n * n].reshape(n, n),
                                 steps, F[i], k[i], 2e-5, 1e-5, 1.0, 0.01)
-        assert np.array_equal(Uc[o:o + n * n].reshape(n, n), uo), i
+        assert same_bits(Uc[o:o + n * n].reshape(n, n), uo), i
     e.close()
 
     # second call: a cache hit, nothing is built or timed
@@ -64,7 +65,7 @@ def test_tune_gs3d_f32k_pick_runs_bit_exact_and_is_cached(cuda_device, private_c
     kernels.gs3d_f32k_tb_forward(U, V, cU, cV, w, kernels.gs_params(**GS), 11)  # tuned tb
     Z = np.zeros(shape, np.float32)
     want = oracle.gs3d_f32k_fast(U0.astype(np.float32), V0.astype(np.float32), Z, Z, 11, **GS)
-    assert np.array_equal(U.cpu().numpy(), want[0]) and np.array_equal(V.cpu().numpy(), want[1])
+    assert same_bits(U.cpu().numpy(), want[0]) and same_bits(V.cpu().numpy(), want[1])
 
     def no_run(*a, **kw):
         raise AssertionError("cache miss: the tuner timed a candidate again")

@@ -20,6 +20,7 @@ from formura_gb300 import _lib, inits, kernels
 from formura_gb300._lib import FormuraError
 from formura_gb300.runtime import load_program
 from oracle import oracle
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -60,7 +61,7 @@ def test_diffusion_barrier_timeout_then_recovers(cuda_device, tb):
         # the same call with the default limit: no error, bit-exact
         d = torch.from_numpy(d0).cuda()
         kernels.diff2d_f64_forward(d, torch.empty_like(d), 0.1, 400)
-        assert np.array_equal(d.cpu().numpy(), oracle.diff2d_f64(d0, 400, Dt=0.1, Dx=1.0))
+        assert same_bits(d.cpu().numpy(), oracle.diff2d_f64(d0, 400, Dt=0.1, Dx=1.0))
     finally:
         L.fm_tune_clear()
 
@@ -92,8 +93,8 @@ def test_ensemble_barrier_timeout_then_recovers(cuda_device, use_graph):
             o = int(e.offsets[i])
             uo, vo = oracle.gs2d_f32(U0[o:o + n * n].reshape(n, n), V0[o:o + n * n].reshape(n, n),
                                      steps, F[i], k[i], 2e-5, 1e-5, 1.0, 0.01)
-            assert np.array_equal(Uc[o:o + n * n].reshape(n, n), uo), i
-            assert np.array_equal(Vc[o:o + n * n].reshape(n, n), vo), i
+            assert same_bits(Uc[o:o + n * n].reshape(n, n), uo), i
+            assert same_bits(Vc[o:o + n * n].reshape(n, n), vo), i
     finally:
         e.close()
 

@@ -13,6 +13,7 @@ from formura_gb300 import inits, kernels
 from formura_gb300.fmr import load_program
 from formura_gb300.runtime import load_program as load_lib
 from oracle import fmr_c
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -98,7 +99,7 @@ def test_generated_program_matches_c_oracle(cuda_device, tmp_path, fmr, kw):
     assert prog.navi.time_step == 2 * p.steps_per_forward
     want = fmr_c.FmrOracle(p.fmr_source, p.shape).run(s0, 2 * p.steps_per_forward)
     for name in s0:
-        assert np.array_equal(prog.state[name], want[name]), name
+        assert same_bits(prog.state[name], want[name]), name
 
 
 def test_generated_gs3d_equals_hand_kernel(cuda_device, tmp_path):
@@ -115,8 +116,8 @@ def test_generated_gs3d_equals_hand_kernel(cuda_device, tmp_path):
     V = torch.from_numpy(V0).cuda()
     kernels.gs3d_f64_forward(U, V, torch.empty_like(U), torch.empty_like(V),
                              kernels.gs_params(**GS), 30)
-    assert np.array_equal(prog.state["U"], U.cpu().numpy())
-    assert np.array_equal(prog.state["V"], V.cpu().numpy())
+    assert same_bits(prog.state["U"], U.cpu().numpy())
+    assert same_bits(prog.state["V"], V.cpu().numpy())
     tot = prog.conserved_totals()
     np.testing.assert_allclose(tot, [prog.state["U"].sum(), prog.state["V"].sum()], rtol=1e-12)
 
@@ -154,4 +155,4 @@ def test_blocked_float_gs3d_equals_per_step_kernels(cuda_device, tmp_path):
         prog.forward()
         outs.append((prog.state["U"].copy(), prog.state["V"].copy()))
         prog.finalize()
-    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    assert same_bits(outs[0][0], outs[1][0]) and same_bits(outs[0][1], outs[1][1])

@@ -15,6 +15,7 @@ import pytest
 from formura_gb300 import backend, inits
 from formura_gb300.fmr import load_program
 from formura_gb300.runtime import load_program as load_lib
+from tests.bits import same_bits
 
 pytestmark = pytest.mark.gpu
 
@@ -48,7 +49,7 @@ def test_plane_is_taken_when_begun(cuda_device, tmp_path, axis, index):
     prog.advance(2)              # the state changes before the plane is collected
     got = prog.monitor_wait()
     for n in ("U", "V"):
-        assert np.array_equal(got[n], want[n]), n
+        assert same_bits(got[n], want[n]), n
     prog.download()
     assert not np.array_equal(_plane(prog.state["U"], axis, index), want["U"])
 
@@ -90,4 +91,4 @@ def test_monitor_of_generated_program_with_mixed_types(cuda_device, tmp_path):
     got = prog.monitor_wait()
     assert got["p"].dtype == np.float64 and got["q"].dtype == np.float32
     for n in ("p", "q"):
-        assert np.array_equal(got[n], want[n])
+        assert same_bits(got[n], want[n])
