@@ -269,9 +269,10 @@ __global__ void __launch_bounds__(kE *kE, 1)
 // instructions (the fast form applies the same operation sequence to both
 // fields), so each packed instruction does the work of two scalar ones; the
 // shared-memory planes interleave (u, v) so that a y neighbour is one 64-bit
-// load.  Per cell and level: 11 packed operations for the two Laplacians,
-// 3 scalar products for u*v*v and its negation, 3 packed for the reaction
-// and 5 packed for the Kahan update, against 37 scalar operations.
+// load, and (T <= 3) so is a z neighbour, read from the row's own plane.
+// Per cell and level: 11 packed operations for the two Laplacians, 3 scalar
+// products for u*v*v and its negation, 3 packed for the reaction and 5 packed
+// for the Kahan update, against 37 scalar operations.
 //
 // Equalities used (all exact in IEEE binary32, round to nearest even):
 //   (1 - u, -v)      = fma((-1, -1), (u, v), (1, -0))
@@ -292,6 +293,11 @@ __global__ void __launch_bounds__(kE *kE, 1)
   extern __shared__ float2 s_w[];
   const int lane = threadIdx.x & 31;
   const int row = threadIdx.x >> 5;
+  // z neighbours: for T <= 3 from the row's own copy of the level's plane in
+  // shared memory (two 64-bit loads instead of four shuffles: 260 against 247
+  // GLUP/s at T = 3); at T = 4 the extra registers spill, so shuffles
+  constexpr bool ZS = T <= 3;
+  const int lane_m = lane > 0 ? lane - 1 : 0, lane_p = lane < 31 ? lane + 1 : 31;
   const size_t sx = (size_t)ny * nz;
   const float2 kF = make_float2(c.F, c.Fk), kD = make_float2(c.cu, c.cv);
   const float2 kDt = make_float2(c.dt, c.dt);
@@ -358,15 +364,24 @@ __global__ void __launch_bounds__(kE *kE, 1)
       for (int s = 1; s <= T; ++s) {
         const float2 m = w[s - 1][1];
         float2 zm, zp;
-        zm.x = __shfl_up_sync(0xffffffffu, m.x, 1);
-        zm.y = __shfl_up_sync(0xffffffffu, m.y, 1);
-        zp.x = __shfl_down_sync(0xffffffffu, m.x, 1);
-        zp.y = __shfl_down_sync(0xffffffffu, m.y, 1);
+        if constexpr (!ZS) {
+          zm.x = __shfl_up_sync(0xffffffffu, m.x, 1);
+          zm.y = __shfl_up_sync(0xffffffffu, m.y, 1);
+          zp.x = __shfl_down_sync(0xffffffffu, m.x, 1);
+          zp.y = __shfl_down_sync(0xffffffffu, m.y, 1);
+        }
         const float2 cin = carry;
         if (row >= s && row < kE - s) {  // warp-uniform
           const int base = ((s - 1) * 2 + (par ^ 1)) * kE;
           const float2 ym = s_w[(base + row - 1) * kE + lane];
           const float2 yp = s_w[(base + row + 1) * kE + lane];
+          if constexpr (ZS) {
+            // the row's own copy of the plane in shared memory (written by this
+            // warp one iteration earlier); lanes 0 and 31 read a clamped index
+            // (they are outside every level s >= 1)
+            zm = s_w[(base + row) * kE + lane_m];
+            zp = s_w[(base + row) * kE + lane_p];
+          }
           using fm::f2add;
           using fm::f2sub;
           const float2 lx = f2sub(f2sub(w[s - 1][2], m), f2sub(m, w[s - 1][0]));
@@ -691,7 +706,7 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   // 0: one row per warp (32x32 threads); 1: the
   // register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread, 16 warps;
   // 3: one row per warp with (u, v) advanced as packed binary32 pairs (the default: fastest
-  // measured, 247 against 238 GLUP/s at 256^3, tb 3)
+  // measured, 260 against 238 GLUP/s at 256^3, tb 3)
   const int kern = fm::tune_get("gs3d_f32k.kernel", 3);
   int done = 0;
   while (done < steps) {
