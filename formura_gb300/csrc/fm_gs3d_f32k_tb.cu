@@ -41,6 +41,9 @@ struct Gs32f {
   float F, Fk, cu, cv, dt;
 };
 
+// -x by flipping the sign bit (exact for every x, zeros and NaNs included)
+__device__ __forceinline__ float neg(float x) { return __int_as_float(__float_as_int(x) ^ 0x80000000); }
+
 __device__ __forceinline__ int wrap_any(int i, int n) {
   i %= n;
   return i < 0 ? i + n : i;
@@ -270,17 +273,15 @@ __global__ void __launch_bounds__(kE *kE, 1)
 // fields), so each packed instruction does the work of two scalar ones; the
 // shared-memory planes interleave (u, v) so that a y neighbour is one 64-bit
 // load, and (T <= 3) so is a z neighbour, read from the row's own plane.
-// Per cell and level: 11 packed operations for the two Laplacians, 3 scalar
-// products for u*v*v and its negation, 3 packed for the reaction and 5 packed
-// for the Kahan update, against 37 scalar operations.
+// Per cell and level: 11 packed operations for the two Laplacians, 2 packed
+// and 3 scalar for the reaction and 4 packed for the Kahan update, against 37
+// scalar operations.
 //
-// Equalities used (all exact in IEEE binary32, round to nearest even):
-//   (1 - u, -v)      = fma((-1, -1), (u, v), (1, -0))
-//   F(1-u) - uvv     = fma(F, 1-u, -uvv);   -Fk v + uvv = fma(Fk, -v, uvv)
-//   -(uv * v)        = uv * (-v)
-//   -c               = c * (-1)      (the addend of the Kahan fma)
-// all exact including the signs of zeros, so the results (compensations
-// included) equal gs3d_f32k_tb's and the oracle's bit for bit.
+// Each half performs exactly the scalar form's operations: the Laplacian and
+// the Kahan update elementwise, the reaction as fma((F, -Fk), (1 - u, v),
+// (-uvv, uvv)) with 1 - u and u*v*v scalar and the negations (of uvv and of the
+// incoming compensation) by sign-bit flips, so the results (compensations and
+// signs of zeros included) equal gs3d_f32k_tb's and the oracle's bit for bit.
 template <int T>
 __global__ void __launch_bounds__(kE *kE, 1)
     gs3d_f32k_tbp(const float *__restrict__ U, const float *__restrict__ V,
@@ -299,9 +300,8 @@ __global__ void __launch_bounds__(kE *kE, 1)
   constexpr bool ZS = T <= 3;
   const int lane_m = lane > 0 ? lane - 1 : 0, lane_p = lane < 31 ? lane + 1 : 31;
   const size_t sx = (size_t)ny * nz;
-  const float2 kF = make_float2(c.F, c.Fk), kD = make_float2(c.cu, c.cv);
+  const float2 kF = make_float2(c.F, -c.Fk), kD = make_float2(c.cu, c.cv);
   const float2 kDt = make_float2(c.dt, c.dt);
-  const float2 kM1 = make_float2(-1.0f, -1.0f), kOne = make_float2(1.0f, -0.0f);
   Pieces pcs(nty * ntz, nx, xchunk);
   int pc, x0, x1;
   while (pcs.next(nty * ntz, nx, xchunk, ntiles, pc, x0, x1)) {
@@ -388,11 +388,14 @@ __global__ void __launch_bounds__(kE *kE, 1)
           const float2 ly = f2sub(f2sub(yp, m), f2sub(m, ym));
           const float2 lz = f2sub(f2sub(zp, m), f2sub(m, zm));
           const float2 lap = f2add(f2add(lx, ly), lz);
-          const float uv = m.x * m.y;
-          const float2 nuvv = make_float2(uv * -m.y, uv * m.y);  // (-uvv, uvv)
-          const float2 wv = fm::f2fma(kM1, m, kOne);              // (1 - u, -v)
+          // the reaction and the Kahan addend as the scalar form writes them; the
+          // sign flips are integer operations, off the FMA pipe that the pair
+          // operations keep busy
+          const float uvv = (m.x * m.y) * m.y;
+          const float2 nuvv = make_float2(neg(uvv), uvv);         // (-uvv, uvv)
+          const float2 wv = make_float2(1.0f - m.x, m.y);         // (1 - u, v)
           const float2 d = fm::f2fma(kD, lap, fm::f2fma(kF, wv, nuvv));
-          const float2 y = fm::f2fma(kDt, d, fm::f2mul(cin, kM1));
+          const float2 y = fm::f2fma(kDt, d, make_float2(neg(cin.x), neg(cin.y)));
           const float2 t = f2add(m, y);
           const float2 cn = f2sub(f2sub(t, m), y);
           if (s < T) {
@@ -706,7 +709,7 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   // 0: one row per warp (32x32 threads); 1: the
   // register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread, 16 warps;
   // 3: one row per warp with (u, v) advanced as packed binary32 pairs (the default: fastest
-  // measured, 260 against 238 GLUP/s at 256^3, tb 3)
+  // measured, 270 against 238 GLUP/s at 256^3, tb 3)
   const int kern = fm::tune_get("gs3d_f32k.kernel", 3);
   int done = 0;
   while (done < steps) {

@@ -1,15 +1,14 @@
 """The exact rewrites behind the packed-pair FP32 blocked kernel
 (gs3d_f32k_tbp in formura_gb300/csrc/fm_gs3d_f32k_tb.cu), checked on the host.
 
-The kernel advances a cell's (u, v) as one binary32 pair, so it rewrites the
-scalar fast-form step (gs3d_f32k_tb's cell_step, oracle.gs3d_f32k_fast) into
+The kernel advances a cell's (u, v) as one binary32 pair, so it writes the
+scalar fast-form step (gs3d_f32k_tb's cell_step, oracle.gs3d_f32k_fast) as
 operations that are the same for both halves:
-  (1 - u, -v)   = fma((-1, -1), (u, v), (1, -0))
-  (-uvv, uvv)   = (uv * (-v), uv * v)
-  inner         = fma((F, Fk), (1 - u, -v), (-uvv, uvv))
-  the Kahan addend            -c = c * (-1).
-Each pair operation rounds like its scalar counterpart (measured on the GPU),
-so the rewrite is exact iff it is exact in scalar IEEE binary32.  This test
+  inner = fma((F, -Fk), (1 - u, v), (-uvv, uvv))
+with 1 - u and u*v*v scalar, and the negations (of uvv, of Fk, and of the
+incoming compensation in the Kahan fma) as sign-bit flips.  Each pair
+operation rounds like its scalar counterpart (measured on the GPU), so the
+form is exact iff it is exact in scalar IEEE binary32.  This test
 evaluates both forms in C (fmaf is the correctly rounded fused operation,
 -ffp-contract=off keeps every other operation separately rounded) over three
 chained steps on random and edge-case operands and requires identical bits,
@@ -39,15 +38,19 @@ static void scalar_step(float u, float v, float lu, float lv, float cu_in, float
   const float yv = fmaf(dt, dV, -cv_in), tv = v + yv;
   o[0] = tu; o[1] = tv; o[2] = (tu - u) - yu; o[3] = (tv - v) - yv;
 }
-/* The same step as the packed kernel writes it, one half at a time. */
+/* -x by flipping the sign bit, as the kernel does */
+static float neg(float x) { uint32_t b; memcpy(&b, &x, 4); b ^= 0x80000000u; memcpy(&x, &b, 4); return x; }
+/* The same step as the packed kernel writes it, one half at a time: the pair
+   constants (F, -Fk), the pair (1 - u, v), the pair (-uvv, uvv). */
 static void pair_step(float u, float v, float lu, float lv, float cu_in, float cv_in,
                       float F, float Fk, float cu, float cv, float dt, float *o) {
-  const float uv = u * v;
-  const float nuvv_x = uv * -v, nuvv_y = uv * v;
-  const float w_x = fmaf(-1.0f, u, 1.0f), w_y = fmaf(-1.0f, v, -0.0f);
-  const float in_x = fmaf(F, w_x, nuvv_x), in_y = fmaf(Fk, w_y, nuvv_y);
+  const float uvv = (u * v) * v;
+  const float nuvv_x = neg(uvv), nuvv_y = uvv;
+  const float w_x = 1.0f - u, w_y = v;
+  const float kF_x = F, kF_y = neg(Fk);
+  const float in_x = fmaf(kF_x, w_x, nuvv_x), in_y = fmaf(kF_y, w_y, nuvv_y);
   const float d_x = fmaf(cu, lu, in_x), d_y = fmaf(cv, lv, in_y);
-  const float y_x = fmaf(dt, d_x, cu_in * -1.0f), y_y = fmaf(dt, d_y, cv_in * -1.0f);
+  const float y_x = fmaf(dt, d_x, neg(cu_in)), y_y = fmaf(dt, d_y, neg(cv_in));
   const float t_x = u + y_x, t_y = v + y_y;
   o[0] = t_x; o[1] = t_y; o[2] = (t_x - u) - y_x; o[3] = (t_y - v) - y_y;
 }
