@@ -273,9 +273,10 @@ __global__ void __launch_bounds__(kE *kE, 1)
 // fields), so each packed instruction does the work of two scalar ones; the
 // shared-memory planes interleave (u, v) so that a y neighbour is one 64-bit
 // load, and (T <= 3) so is a z neighbour, read from the row's own plane.
-// Per cell and level: 11 packed operations for the two Laplacians, 2 packed
-// and 3 scalar for the reaction and 4 packed for the Kahan update, against 37
-// scalar operations.
+// Per cell and level: 10 packed operations for the two Laplacians (the x face
+// below a cell is the one above the previous plane's cell, carried in a
+// register), 2 packed and 3 scalar for the reaction and 4 packed for the Kahan
+// update, against 37 scalar operations.
 //
 // Each half performs exactly the scalar form's operations: the Laplacian and
 // the Kahan update elementwise, the reaction as fma((F, -Fk), (1 - u, v),
@@ -312,11 +313,14 @@ __global__ void __launch_bounds__(kE *kE, 1)
     const size_t col = (size_t)wrap_any(gy_out, ny) * nz + wrap_any(gz_out, nz);
     const bool writer = row >= T && row < T + O && lane >= T && lane < T + O &&
                         gy_out < ny && gz_out < nz;
-    float2 w[T][3];  // level s window of (u, v): planes (newest-2, newest-1, newest)
+    // level s window of (u, v): planes (newest-1, newest), and the x face
+    // difference between newest-1 and the plane before it (computed once, by
+    // level s+1 in the previous iteration: the same operands, the same value)
+    float2 w[T][2], fx[T];
     float2 cc[T];    // level s compensation at its newest plane
 #pragma unroll
     for (int s = 0; s < T; ++s) {
-      w[s][0] = w[s][1] = w[s][2] = make_float2(0.0f, 0.0f);
+      w[s][0] = w[s][1] = fx[s] = make_float2(0.0f, 0.0f);
       cc[s] = make_float2(0.0f, 0.0f);
     }
     constexpr int kPF = 2;
@@ -355,14 +359,13 @@ __global__ void __launch_bounds__(kE *kE, 1)
         pcv[kPF - 1] = __ldg(cV + g);
       }
       w[0][0] = w[0][1];
-      w[0][1] = w[0][2];
-      w[0][2] = in;
+      w[0][1] = in;
       s_w[((0 * 2 + par) * kE + row) * kE + lane] = in;
       float2 carry = cc[0];  // level 0's compensation at plane i-1
       cc[0] = in_c;
 #pragma unroll
       for (int s = 1; s <= T; ++s) {
-        const float2 m = w[s - 1][1];
+        const float2 m = w[s - 1][0];
         float2 zm, zp;
         if constexpr (!ZS) {
           zm.x = __shfl_up_sync(0xffffffffu, m.x, 1);
@@ -384,7 +387,9 @@ __global__ void __launch_bounds__(kE *kE, 1)
           }
           using fm::f2add;
           using fm::f2sub;
-          const float2 lx = f2sub(f2sub(w[s - 1][2], m), f2sub(m, w[s - 1][0]));
+          const float2 fp = f2sub(w[s - 1][1], m);  // x face above; the one below is fx
+          const float2 lx = f2sub(fp, fx[s - 1]);
+          fx[s - 1] = fp;
           const float2 ly = f2sub(f2sub(yp, m), f2sub(m, ym));
           const float2 lz = f2sub(f2sub(zp, m), f2sub(m, zm));
           const float2 lap = f2add(f2add(lx, ly), lz);
@@ -402,8 +407,7 @@ __global__ void __launch_bounds__(kE *kE, 1)
             carry = cc[s];
             cc[s] = cn;
             w[s][0] = w[s][1];
-            w[s][1] = w[s][2];
-            w[s][2] = t;
+            w[s][1] = t;
             s_w[((s * 2 + par) * kE + row) * kE + lane] = t;
           } else {
             const int p = i - T;
