@@ -713,7 +713,7 @@ extern "C" int fm_gs3d_f32k_tb_forward(int nx, int ny, int nz, float *U, float *
   // 0: one row per warp (32x32 threads); 1: the
   // register-blocked kernel, 4 rows per thread, 8 warps; 2: 2 rows per thread, 16 warps;
   // 3: one row per warp with (u, v) advanced as packed binary32 pairs (the default: fastest
-  // measured, 270 against 238 GLUP/s at 256^3, tb 3)
+  // measured, 276 against 238 GLUP/s at 256^3, tb 3)
   const int kern = fm::tune_get("gs3d_f32k.kernel", 3);
   int done = 0;
   while (done < steps) {
