@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(kE *kE, 1)
 }
 
 // gs3d_f32k_tbp<T>: the 32x32-thread pipeline of gs3d_f32k_tb with U and V of
-// a cell held as one binary32 pair and advanced by packed FADD2/FMUL2/FFMA2
+// a cell held as one binary32 pair and advanced by packed FADD2/FFMA2
 // instructions (the fast form applies the same operation sequence to both
 // fields), so each packed instruction does the work of two scalar ones; the
 // shared-memory planes interleave (u, v) so that a y neighbour is one 64-bit
